@@ -1,0 +1,224 @@
+"""Python face of the C ABI over torch CUDA tensors (device memory and streams only).
+
+Each class mirrors one of the reference's commands / C functions and calls straight into
+libbvhgb.so; device buffers are torch tensors, node arrays are int32 tensors of shape
+(numNodes, 12) holding the 48-byte BVHNode records.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import native
+from .native import (Aabb, BvhgbError, Bn13Config, Bn13Stats, Camera, HIT_DTYPE, LbvhConfig, NODE_DTYPE, PIXEL_DTYPE,
+                     TraceConfig, check, load)
+
+REFCOMPAT, KARRAS = 0, 1
+TOPOLOGY = {"refCompat": REFCOMPAT, "karras": KARRAS, REFCOMPAT: REFCOMPAT, KARRAS: KARRAS}
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def _dev_f32(a):
+    if isinstance(a, torch.Tensor):
+        return a.to(device="cuda", dtype=torch.float32).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
+
+
+def _dev_u32(a):
+    if isinstance(a, torch.Tensor):
+        return a.to(device="cuda", dtype=torch.int32).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(a, np.uint32).view(np.int32)).cuda()
+
+
+def nodes_to_numpy(nodes: torch.Tensor) -> np.ndarray:
+    return nodes.detach().cpu().contiguous().numpy().view(NODE_DTYPE).reshape(-1)
+
+
+def nodes_from_numpy(arr: np.ndarray) -> torch.Tensor:
+    return torch.from_numpy(np.ascontiguousarray(arr).view(np.int32).reshape(-1, 12).copy()).cuda()
+
+
+def empty_nodes(n_nodes: int) -> torch.Tensor:
+    return torch.empty((max(n_nodes, 1), 12), dtype=torch.int32, device="cuda")
+
+
+class LBVH:
+    """The `LBVH` command (lib/builder/LBVH.cpp:28-55) over a device-resident mesh."""
+
+    def __init__(self, max_faces: int, morton_bits: int = 30, topology="refCompat"):
+        self.lib = load()
+        self.max_faces = int(max_faces)
+        self.cfg = LbvhConfig(int(morton_bits), TOPOLOGY[topology])
+        ws = C.c_void_p()
+        check(self.lib.bvhgb_lbvh_create(self.max_faces, C.byref(self.cfg), C.byref(ws)), "bvhgb_lbvh_create")
+        self.ws = ws
+
+    def close(self):
+        if self.ws:
+            self.lib.bvhgb_lbvh_destroy(self.ws)
+            self.ws = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def build(self, vert, faces, nodes=None, stream=None) -> torch.Tensor:
+        v, f = _dev_f32(vert), _dev_u32(faces)
+        n = f.shape[0]
+        if nodes is None:
+            nodes = empty_nodes(2 * n - 1)
+        check(self.lib.bvhgb_lbvh_build(self.ws, _ptr(v), _ptr(f), n, _ptr(nodes), _stream(stream)), "bvhgb_lbvh_build")
+        return nodes
+
+    # phases (LBVH_initTriData, LBVH_calcMortonCodes, LBVH_sortMortonCodes, LBVH_buildBVHTree)
+    def init_tri_data(self, vert, faces, stream=None):
+        check(self.lib.bvhgb_lbvh_init_tri_data(self.ws, _ptr(vert), _ptr(faces), faces.shape[0], _stream(stream)),
+              "init_tri_data")
+
+    def calc_morton(self, vert, faces, stream=None):
+        check(self.lib.bvhgb_lbvh_calc_morton(self.ws, _ptr(vert), _ptr(faces), faces.shape[0], _stream(stream)),
+              "calc_morton")
+
+    def sort(self, n, stream=None):
+        check(self.lib.bvhgb_lbvh_sort(self.ws, n, _stream(stream)), "sort")
+
+    def build_tree(self, vert, faces, nodes, stream=None):
+        check(self.lib.bvhgb_lbvh_build_tree(self.ws, _ptr(vert), _ptr(faces), faces.shape[0], _ptr(nodes),
+                                             _stream(stream)), "build_tree")
+
+    def scene_box(self, stream=None) -> np.ndarray:
+        a = Aabb()
+        check(self.lib.bvhgb_lbvh_read_scene_box(self.ws, C.byref(a), _stream(stream)), "read_scene_box")
+        return np.array(list(a.mn) + list(a.mx), np.float32)
+
+    def keys(self, n, sorted_: bool, stream=None):
+        k = np.zeros(n, np.uint32 if self.cfg.mortonBits == 30 else np.uint64)
+        idx = np.zeros(n, np.uint32)
+        check(self.lib.bvhgb_lbvh_read_keys(self.ws, int(sorted_), k.ctypes.data_as(C.c_void_p),
+                                            idx.ctypes.data_as(C.c_void_p), n, _stream(stream)), "read_keys")
+        return k, idx
+
+
+def radix_sort_pairs(keys: torch.Tensor, vals: torch.Tensor, begin_bit=0, end_bit=None, stream=None):
+    """Stable ascending sort of (key, value) pairs; keys int32/int64 tensors read as unsigned."""
+    lib = load()
+    kb = keys.element_size()
+    end_bit = 8 * kb if end_bit is None else end_bit
+    n = keys.shape[0]
+    need = C.c_size_t(0)
+    check(lib.bvhgb_radix_sort_pairs(None, C.byref(need), None, None, None, None, n, kb, begin_bit, end_bit, None),
+          "sort size")
+    temp = torch.empty(max(need.value, 1), dtype=torch.uint8, device="cuda")
+    ko = torch.empty_like(keys)
+    vo = torch.empty_like(vals)
+    check(lib.bvhgb_radix_sort_pairs(_ptr(temp), C.byref(need), _ptr(keys), _ptr(ko), _ptr(vals), _ptr(vo), n, kb,
+                                     begin_bit, end_bit, _stream(stream)), "bvhgb_radix_sort_pairs")
+    return ko, vo
+
+
+def calc_sah(nodes: torch.Tensor, root: int = 0, num_nodes=None, stream=None) -> float:
+    out = C.c_double()
+    n = nodes.shape[0] if num_nodes is None else num_nodes
+    check(load().bvhgb_calc_sah(_ptr(nodes), n, root, C.byref(out), _stream(stream)), "bvhgb_calc_sah")
+    return out.value
+
+
+class Bittner13GPU:
+    """The `bittner13GPU` command (lib/builder/Bittner13GPU.cpp:78-133)."""
+
+    def __init__(self, nodes: torch.Tensor, root: int = 0, num_chunks=32, block_size=128, batch_percent=1.0,
+                 offset_access=False, heap_capacity=4096, num_nodes=None, stream=None):
+        self.lib = load()
+        self.cfg = Bn13Config(num_chunks, block_size, batch_percent, int(offset_access), heap_capacity)
+        ws = C.c_void_p()
+        n = nodes.shape[0] if num_nodes is None else num_nodes
+        check(self.lib.bvhgb_bn13_create(_ptr(nodes), n, root, C.byref(self.cfg), C.byref(ws), _stream(stream)),
+              "bvhgb_bn13_create")
+        self.ws = ws
+        self.nodes = nodes
+
+    def close(self):
+        if self.ws:
+            self.lib.bvhgb_bn13_destroy(self.ws)
+            self.ws = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def batch_size(self) -> int:
+        return self.lib.bvhgb_bn13_batch_size(self.ws)
+
+    def step(self, stream=None):
+        check(self.lib.bvhgb_bn13_step(self.ws, _ptr(self.nodes), _stream(stream)), "bvhgb_bn13_step")
+
+    def run(self, iterations: int, stream=None):
+        check(self.lib.bvhgb_bn13_run(self.ws, _ptr(self.nodes), iterations, _stream(stream)), "bvhgb_bn13_run")
+
+    def stats(self, stream=None) -> dict:
+        st = Bn13Stats()
+        check(self.lib.bvhgb_bn13_get_stats(self.ws, C.byref(st), _stream(stream)), "bvhgb_bn13_get_stats")
+        return {k: getattr(st, k) for k, _ in Bn13Stats._fields_}
+
+
+def make_camera(pos, lookAt, up, fov, width, height) -> Camera:
+    return Camera((C.c_float * 3)(*pos), (C.c_float * 3)(*lookAt), (C.c_float * 3)(*up), float(fov), int(width),
+                  int(height))
+
+
+def make_trace_config(light=(2.0, 2.0, 2.0), face_culling=False, tmin=0.0, tmax=float("inf")) -> TraceConfig:
+    return TraceConfig((C.c_float * 3)(*light), int(face_culling), float(tmin), float(tmax))
+
+
+def trace_image(nodes, vert, faces, camera: dict, root=0, light=(2.0, 2.0, 2.0), face_culling=False, with_hits=True,
+                num_nodes=None, stream=None):
+    """generateRays + tracerImage (CUDAKernels.cu:386-417): returns (pixels int32 [h*w], hits int64 [h*w] | None)."""
+    cam = make_camera(**camera)
+    cfg = make_trace_config(light, face_culling)
+    npx = cam.width * cam.height
+    img = torch.empty(npx, dtype=torch.int32, device="cuda")
+    hits = torch.empty(npx, dtype=torch.int64, device="cuda") if with_hits else None
+    n = nodes.shape[0] if num_nodes is None else num_nodes
+    check(load().bvhgb_trace_image(_ptr(nodes), n, root, _ptr(vert), _ptr(faces), C.byref(cam), C.byref(cfg), _ptr(img),
+                                   _ptr(hits), _stream(stream)), "bvhgb_trace_image")
+    return img, hits
+
+
+def trace_rays(nodes, vert, faces, org, dirs, root=0, tmin=0.0, tmax=float("inf"), face_culling=False, num_nodes=None,
+               stream=None):
+    cfg = make_trace_config((2.0, 2.0, 2.0), face_culling, tmin, tmax)
+    o, d = _dev_f32(org), _dev_f32(dirs)
+    hits = torch.empty(o.shape[0], dtype=torch.int64, device="cuda")
+    n = nodes.shape[0] if num_nodes is None else num_nodes
+    check(load().bvhgb_trace_rays(_ptr(nodes), n, root, _ptr(vert), _ptr(faces), _ptr(o), _ptr(d), o.shape[0],
+                                  C.byref(cfg), _ptr(hits), _stream(stream)), "bvhgb_trace_rays")
+    return hits
+
+
+def trace_errors(reset=True) -> int:
+    v = C.c_uint32()
+    check(load().bvhgb_trace_read_errors(C.byref(v), int(reset)), "bvhgb_trace_read_errors")
+    return v.value
+
+
+def hits_to_numpy(h: torch.Tensor) -> np.ndarray:
+    return h.detach().cpu().numpy().view(HIT_DTYPE).reshape(-1)
+
+
+def pixels_to_numpy(p: torch.Tensor) -> np.ndarray:
+    return p.detach().cpu().numpy().view(PIXEL_DTYPE).reshape(-1)

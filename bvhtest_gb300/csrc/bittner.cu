@@ -1,0 +1,662 @@
+// Parallel Bittner13 SAH optimizer (lib/builder/Bittner13CUDA.cu, lib/base/BVHPatch.hpp).
+//
+// One iteration = select + numChunks chunks. Selection: inefficiency of every inner node, then the
+// onesweep sort on (~order(cost), node) gives the stable descending order of the reference's
+// SortPairsDescending. Each chunk runs four kernels:
+//   patch  : one thread per batch item removes its node and reinserts both children into a private
+//            10-slot copy-on-write patch, finding each position by branch and bound over the induced
+//            cost (findNode1 with the standard-library heap discipline), then claims every node it
+//            patched with atomicMin(owner, rank);
+//   apply  : an item whose every node is still owned by its own rank writes its patch; all others
+//            count as skipped. Lower rank = higher cost wins, so the result does not depend on
+//            scheduling (the reference locks first-come and is not deterministic);
+//   count  : owners are released and each dirty path (grand parent, both reused nodes) counts its
+//            arrivals on the way to the root (kFixTree3_1);
+//   refit  : the last arrival at a node recomputes its box from its children (kFixTree3_2) with
+//            acq_rel counters, so no box is read before it is final.
+// bvhgb_bn13_run captures one iteration into a CUDA graph and replays it.
+#include <vector>
+
+#include "common.cuh"
+#include "sort.cuh"
+
+namespace bvhgb {
+namespace {
+
+constexpr int NSLOT = 10;
+enum : uint32_t {
+  P_GRAND_PARENT = 0, P_1ST_ROOT = 1, P_1ST_BEST = 2, P_NODE = 3, P_1ST_INSERT = 4,
+  P_2ND_ROOT = 5, P_2ND_BEST = 6, P_2ND_INSERT = 7, P_SIBLING = 8, P_PARENT = 9
+};
+enum StatIdx { S_ITEMS = 0, S_APPLIED = 1, S_CONFLICT = 2, S_INVALID = 3, S_OVERFLOW = 4, S_COUNT = 5 };
+
+struct NodeP {
+  uint32_t parent, left, right;
+  uint16_t isLeafFlag, isLeft;
+};
+
+struct HeapItem {
+  uint32_t node;
+  float cost;
+};
+
+struct PatchOut {  // what the apply kernel needs
+  NodeP nd[NSLOT];
+  uint32_t idx[NSLOT];
+};
+
+// Read-only view of the tree during the patch kernel (nothing writes the tree in that launch).
+__device__ __forceinline__ NodeP tree_node(const bvhgb_node *t, uint32_t x) {
+  const float4 *p = reinterpret_cast<const float4 *>(t + x);
+  const float4 b = __ldg(p + 1), c = __ldg(p + 2);
+  NodeP r;
+  r.parent = __float_as_uint(b.z);
+  r.left = __float_as_uint(b.w);
+  r.right = __float_as_uint(c.x);
+  const uint32_t fl = __float_as_uint(c.y);
+  r.isLeafFlag = (uint16_t)(fl & 0xFFFFu);
+  r.isLeft = (uint16_t)(fl >> 16);
+  return r;
+}
+__device__ __forceinline__ Box tree_box(const bvhgb_node *t, uint32_t x) {
+  const float4 *p = reinterpret_cast<const float4 *>(t + x);
+  const float4 a = __ldg(p), b = __ldg(p + 1);
+  Box r;
+  r.mn[0] = a.x; r.mn[1] = a.y; r.mn[2] = a.z;
+  r.mx[0] = a.w; r.mx[1] = b.x; r.mx[2] = b.y;
+  return r;
+}
+__device__ __forceinline__ float tree_sa(const bvhgb_node *t, uint32_t x) { return __ldg(&t[x].surfaceArea); }
+__device__ __forceinline__ bool tree_leaf(const bvhgb_node *t, uint32_t x) { return __ldg(&t[x].isLeafFlag) != 0; }
+
+// BVHPatch (BVHPatch.hpp:87-335), ENABLE_AABB_PATH = 0.
+struct Patch {
+  NodeP nd[NSLOT];
+  uint32_t idx[NSLOT];
+  uint32_t apath[4];
+  Box abox[4];
+  const bvhgb_node *t;
+  uint32_t root;
+
+  __device__ void clear() {
+#pragma unroll
+    for (int i = 0; i < NSLOT; ++i) idx[i] = kNone;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) apath[i] = kNone;
+  }
+  __device__ uint32_t index_subset(uint32_t x) const {
+    if (idx[0] == x) return 0;
+    if (idx[1] == kNone) return kNone;
+    if (idx[1] == x) return 1;
+    if (idx[2] == x) return 2;
+    if (idx[3] == x) return 3;
+    return kNone;
+  }
+  __device__ uint32_t index(uint32_t x) const {
+    for (uint32_t i = 0; i < NSLOT; ++i)
+      if (idx[i] == x) return i;
+    return kNone;
+  }
+  __device__ NodeP get(uint32_t x) const {
+    uint32_t i = index(x);
+    return i == kNone ? tree_node(t, x) : nd[i];
+  }
+  __device__ NodeP get_subset(uint32_t x) const {
+    uint32_t i = index_subset(x);
+    return i == kNone ? tree_node(t, x) : nd[i];
+  }
+  __device__ uint32_t patch_node(uint32_t x, uint32_t slot) {
+    idx[slot] = x;
+    nd[slot] = tree_node(t, x);
+    return slot;
+  }
+  __device__ uint32_t move(uint32_t from, uint32_t to) {
+    idx[to] = idx[from];
+    idx[from] = kNone;
+    nd[to] = nd[from];
+    return to;
+  }
+  __device__ uint32_t sibling(const NodeP &n) const {
+    NodeP p = get(n.parent);
+    return n.isLeft == 0 ? p.left : p.right;
+  }
+  __device__ Box get_aabb(uint32_t x) const {
+    for (int i = 0; i < 4; ++i)
+      if (apath[i] == x) return abox[i];
+    return tree_box(t, x);
+  }
+  // patchAABBFrom (BVHPatch.hpp:293-316)
+  __device__ void patch_aabb_from(uint32_t x, uint32_t pidx) {
+    uint32_t ni = x;
+    NodeP n = get_subset(ni);
+    Box b = get_aabb(n.left);
+    bool lastLeft = true;
+    for (uint32_t i = 0; i < 2; ++i) {
+      uint32_t sib = lastLeft ? n.right : n.left;
+      Box sb = get_aabb(sib);
+      merge_into(b, sb);
+      abox[pidx * 2 + i] = b;
+      apath[pidx * 2 + i] = ni;
+      lastLeft = n.isLeft != 0;
+      if (ni == root) break;
+      ni = n.parent;
+      n = get_subset(ni);
+    }
+  }
+};
+
+// Heap with the hole-based sift of the standard library heap algorithms (CUDAHeap.hpp:33-112);
+// "less(a, b)" is a.cost > b.cost, so h[0] holds the smallest induced cost.
+__device__ __forceinline__ bool hless(const HeapItem &a, const HeapItem &b) { return a.cost > b.cost; }
+
+__device__ __forceinline__ void sift_up(HeapItem *h, long hole, long top, HeapItem v) {
+  long parent = (hole - 1) / 2;
+  while (hole > top && hless(h[parent], v)) {
+    h[hole] = h[parent];
+    hole = parent;
+    parent = (hole - 1) / 2;
+  }
+  h[hole] = v;
+}
+__device__ __forceinline__ void heap_push(HeapItem *h, long lenAfter) { sift_up(h, lenAfter - 1, 0, h[lenAfter - 1]); }
+__device__ __forceinline__ void heap_pop(HeapItem *h, long len) {
+  if (len <= 1) return;
+  const long last = len - 1;
+  const HeapItem v = h[last];
+  h[last] = h[0];
+  const long n = last;
+  long hole = 0, second = 0;
+  while (second < (n - 1) / 2) {
+    second = 2 * (second + 1);
+    if (hless(h[second], h[second - 1])) second--;
+    h[hole] = h[second];
+    hole = second;
+  }
+  if ((n & 1) == 0 && second == (n - 2) / 2) {
+    second = 2 * (second + 1);
+    h[hole] = h[second - 1];
+    hole = second - 1;
+  }
+  sift_up(h, hole, 0, v);
+}
+
+// findNode1 (Bittner13CUDA.cu:141-191).
+__device__ uint32_t find_node(const Patch &p, uint32_t n, HeapItem *pq, uint32_t cap, uint32_t &overflow) {
+  float best_cost = __int_as_float(0x7f800000);
+  uint32_t best = 0;
+  const Box nbox = tree_box(p.t, n);
+  const float sarea = tree_sa(p.t, n);
+  long size = 1;
+  pq[0].node = p.root;
+  pq[0].cost = 0.0f;
+  while (size > 0) {
+    const HeapItem cur = pq[0];
+    if (fadd(cur.cost, sarea) >= best_cost) break;
+    heap_pop(pq, size);
+    size--;
+    const NodeP cn = p.get_subset(cur.node);
+    Box b = p.get_aabb(cur.node);
+    float induced = fmul(-1.0f, surface_area(b));
+    merge_into(b, nbox);
+    const float direct = surface_area(b);
+    const float total = fadd(cur.cost, direct);
+    if (total < best_cost) {
+      best_cost = total;
+      best = cur.node;
+    }
+    induced = fadd(induced, total);
+    if (fadd(induced, sarea) < best_cost && !cn.isLeafFlag) {
+      if ((uint32_t)size + 2 <= cap) {
+        pq[size].node = cn.left;
+        pq[size].cost = induced;
+        pq[size + 1].node = cn.right;
+        pq[size + 1].cost = induced;
+        heap_push(pq, size + 1);
+        heap_push(pq, size + 2);
+        size += 2;
+      } else {
+        overflow++;
+      }
+    }
+  }
+  return best;
+}
+
+// removeNode (Bittner13CUDA.cu:267-305).
+__device__ bool remove_node(Patch &p, uint32_t x, uint32_t ins[2], uint32_t un[2], uint32_t &g_out) {
+  if (tree_leaf(p.t, x) || x == p.root) return false;
+  const uint32_t sn = p.patch_node(x, P_NODE);
+  const uint32_t s = p.sibling(p.nd[sn]);
+  const uint32_t pi = p.nd[sn].parent;
+  if (pi == p.root) return false;
+  const uint32_t ss = p.patch_node(s, P_SIBLING);
+  const uint32_t sp = p.patch_node(pi, P_PARENT);
+  const uint32_t gi = p.nd[sp].parent;
+  const uint32_t sg = p.patch_node(gi, P_GRAND_PARENT);
+  if (p.nd[sp].isLeft) {
+    p.nd[sg].left = s;
+    p.nd[ss].isLeft = 1;
+  } else {
+    p.nd[sg].right = s;
+    p.nd[ss].isLeft = 0;
+  }
+  p.nd[ss].parent = gi;
+  p.patch_aabb_from(gi, 0);
+  const uint32_t l = p.nd[sn].left, r = p.nd[sn].right;
+  if (tree_sa(p.t, l) > tree_sa(p.t, r)) { ins[0] = l; ins[1] = r; }
+  else { ins[0] = r; ins[1] = l; }
+  un[0] = x;
+  un[1] = pi;
+  g_out = gi;
+  return true;
+}
+
+// reinsert (Bittner13CUDA.cu:308-358).
+__device__ bool reinsert(Patch &p, uint32_t x, uint32_t unused, bool update, HeapItem *pq, uint32_t cap,
+                         uint32_t &overflow) {
+  const uint32_t best = find_node(p, x, pq, cap, overflow);
+  if (best == p.root) return false;
+  const uint32_t bpi = p.index(best);
+  uint32_t sb;
+  if (bpi == kNone) sb = p.patch_node(best, update ? P_1ST_BEST : P_2ND_BEST);
+  else if (bpi == P_GRAND_PARENT) sb = P_GRAND_PARENT;
+  else sb = p.move(bpi, update ? P_1ST_BEST : P_2ND_BEST);
+  const uint32_t sx = p.patch_node(x, update ? P_1ST_INSERT : P_2ND_INSERT);
+  const uint32_t su = update ? P_NODE : P_PARENT;
+  const uint32_t ri = p.nd[sb].parent;
+  const uint32_t rpi = p.index(ri);
+  const uint32_t sr = rpi == kNone ? p.patch_node(ri, update ? P_1ST_ROOT : P_2ND_ROOT)
+                                   : p.move(rpi, update ? P_1ST_ROOT : P_2ND_ROOT);
+  if (p.nd[sb].isLeft) {
+    p.nd[sr].left = unused;
+    p.nd[su].isLeft = 1;
+  } else {
+    p.nd[sr].right = unused;
+    p.nd[su].isLeft = 0;
+  }
+  p.nd[su].parent = ri;
+  p.nd[su].left = best;
+  p.nd[su].right = x;
+  p.nd[sb].parent = unused;
+  p.nd[sb].isLeft = 1;
+  p.nd[sx].parent = unused;
+  p.nd[sx].isLeft = 0;
+  if (update) p.patch_aabb_from(unused, 1);
+  return true;
+}
+
+// ---- kernels ------------------------------------------------------------------------------
+
+__global__ void cost_kernel(const bvhgb_node *__restrict__ t, const uint32_t *__restrict__ inner, uint32_t numInner,
+                            uint32_t *__restrict__ keys, uint32_t *__restrict__ vals) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < numInner; i += gridDim.x * blockDim.x) {
+    const uint32_t x = __ldg(inner + i);
+    const float4 *p = reinterpret_cast<const float4 *>(t + x);
+    const float4 b = __ldg(p + 1), c = __ldg(p + 2);
+    float cost = 0.0f;
+    if ((__float_as_uint(c.y) & 0xFFFFu) == 0) {
+      const float sa = c.w;
+      const float l = __ldg(&t[__float_as_uint(b.w)].surfaceArea);
+      const float r = __ldg(&t[__float_as_uint(c.x)].surfaceArea);
+      const float num = fmul(fmul(fmul(sa, sa), sa), 2.0f);
+      const float den = fmul(fadd(l, r), l < r ? l : r);
+      cost = fdiv(num, den);
+    }
+    keys[i] = ~f2ord(cost);  // ascending key order = descending cost
+    vals[i] = x;
+  }
+}
+
+__global__ void patch_kernel(const bvhgb_node *__restrict__ t, uint32_t root, const uint32_t *__restrict__ todo,
+                             uint32_t numTodo, uint32_t chunk, uint32_t numChunks, uint32_t chunkSize,
+                             uint32_t offsetAccess, PatchOut *__restrict__ out, uint32_t *__restrict__ valid,
+                             uint32_t *__restrict__ toFix, uint32_t *__restrict__ owner, HeapItem *__restrict__ heaps,
+                             uint32_t cap, unsigned long long *__restrict__ stats) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= chunkSize) return;
+  const uint32_t pos = offsetAccess ? k * numChunks + chunk : chunk * chunkSize + k;
+  Patch p;
+  p.t = t;
+  p.root = root;
+  p.clear();
+  uint32_t overflow = 0;
+  uint32_t ins[2], un[2], g = kNone;
+  bool ok = pos < numTodo;
+  const uint32_t node = ok ? __ldg(todo + pos) : kNone;
+  HeapItem *pq = heaps + (size_t)k * cap;
+  ok = ok && remove_node(p, node, ins, un, g);
+  ok = ok && reinsert(p, ins[0], un[0], true, pq, cap, overflow);
+  ok = ok && reinsert(p, ins[1], un[1], false, pq, cap, overflow);
+  valid[k] = ok ? 1u : 0u;
+  toFix[3 * k + 0] = ok ? g : kNone;
+  toFix[3 * k + 1] = ok ? un[0] : kNone;
+  toFix[3 * k + 2] = ok ? un[1] : kNone;
+#pragma unroll
+  for (int s = 0; s < NSLOT; ++s) {
+    out[k].nd[s] = p.nd[s];
+    out[k].idx[s] = ok ? p.idx[s] : kNone;
+    if (ok && p.idx[s] != kNone) atomicMin(&owner[p.idx[s]], k);
+  }
+  if (!ok) atomicAdd(&stats[S_INVALID], 1ull);
+  if (overflow) atomicAdd(&stats[S_OVERFLOW], (unsigned long long)overflow);
+  atomicAdd(&stats[S_ITEMS], 1ull);
+}
+
+__global__ void apply_kernel(bvhgb_node *t, const PatchOut *__restrict__ in, uint32_t *__restrict__ valid,
+                             uint32_t *__restrict__ toFix, const uint32_t *__restrict__ owner, uint32_t chunkSize,
+                             unsigned long long *__restrict__ stats) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= chunkSize || !valid[k]) return;
+  bool win = true;
+#pragma unroll
+  for (int s = 0; s < NSLOT; ++s) {
+    const uint32_t x = in[k].idx[s];
+    if (x != kNone && owner[x] != k) win = false;
+  }
+  if (!win) {
+    valid[k] = 0;
+    toFix[3 * k + 0] = toFix[3 * k + 1] = toFix[3 * k + 2] = kNone;
+    atomicAdd(&stats[S_CONFLICT], 1ull);
+    return;
+  }
+#pragma unroll
+  for (int s = 0; s < NSLOT; ++s) {
+    const uint32_t x = in[k].idx[s];
+    if (x == kNone) continue;
+    const NodeP n = in[k].nd[s];
+    t[x].parent = n.parent;
+    t[x].left = n.left;
+    t[x].right = n.right;
+    t[x].isLeft = n.isLeft;
+  }
+  atomicAdd(&stats[S_APPLIED], 1ull);
+}
+
+// Release the claims and count, per node, how many dirty paths arrive (kFixTree3_1).
+__global__ void count_kernel(const bvhgb_node *__restrict__ t, uint32_t root, const PatchOut *__restrict__ in,
+                             const uint32_t *__restrict__ toFix, uint32_t *__restrict__ owner,
+                             uint32_t *__restrict__ counter, uint32_t chunkSize, uint32_t numNodes,
+                             uint32_t *__restrict__ err) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= chunkSize) return;
+#pragma unroll
+  for (int s = 0; s < NSLOT; ++s) {
+    const uint32_t x = in[k].idx[s];
+    if (x != kNone) owner[x] = kNone;
+  }
+  for (int j = 0; j < 3; ++j) {
+    uint32_t x = toFix[3 * k + j];
+    if (x == kNone) continue;
+    for (uint32_t steps = 0;; ++steps) {
+      if (x >= numNodes || steps > numNodes) {
+        atomicOr(err, kErrBadIndex);
+        break;
+      }
+      if (atomicAdd(&counter[x], 1u) != 0u) break;
+      if (x == root) break;
+      x = t[x].parent;
+    }
+  }
+}
+
+// The last path to arrive at a node recomputes its box (kFixTree3_2).
+__global__ void refit_kernel(bvhgb_node *t, uint32_t root, const uint32_t *__restrict__ toFix,
+                             uint32_t *__restrict__ counter, uint32_t chunkSize, uint32_t numNodes,
+                             uint32_t *__restrict__ err) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * chunkSize) return;
+  uint32_t x = toFix[i];
+  if (x == kNone) return;
+  for (uint32_t steps = 0;; ++steps) {
+    if (x >= numNodes || steps > numNodes) {
+      atomicOr(err, kErrBadIndex);
+      return;
+    }
+    if (atom_add_acq_rel(&counter[x], 0xFFFFFFFFu) != 1u) return;  // not the last arrival
+    const uint32_t l = ld_cg(&t[x].left), r = ld_cg(&t[x].right);
+    if (ld_cg(reinterpret_cast<const uint32_t *>(&t[x].isLeafFlag)) & 0xFFFFu) return;
+    Box b = load_box_cg(t + l);
+    const Box rb = load_box_cg(t + r);
+    merge_into(b, rb);
+    float4 *p = reinterpret_cast<float4 *>(t + x);
+    const float4 old1 = __ldcg(p + 1);
+    p[0] = make_float4(b.mn[0], b.mn[1], b.mn[2], b.mx[0]);
+    p[1] = make_float4(b.mx[1], b.mx[2], old1.z, old1.w);
+    t[x].surfaceArea = surface_area(b);
+    if (x == root) return;
+    x = ld_cg(&t[x].parent);
+  }
+}
+
+__global__ void init_inner_kernel(const bvhgb_node *__restrict__ t, uint32_t n, uint32_t *__restrict__ flag) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    flag[i] = __ldg(&t[i].isLeafFlag) == 0 ? 1u : 0u;
+}
+
+}  // namespace
+}  // namespace bvhgb
+
+using namespace bvhgb;
+
+struct bvhgb_bn13_workspace {
+  bvhgb_bn13_config cfg{};
+  uint32_t numNodes = 0, root = 0, numInner = 0, numChunks = 0, chunkSize = 0;
+  uint32_t *inner = nullptr, *keys = nullptr, *vals = nullptr, *keysSorted = nullptr, *todo = nullptr;
+  void *sortTemp = nullptr;
+  PatchOut *patches = nullptr;
+  uint32_t *valid = nullptr, *toFix = nullptr, *owner = nullptr, *counter = nullptr, *err = nullptr;
+  HeapItem *heaps = nullptr;
+  unsigned long long *stats = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  bvhgb_node *graphNodes = nullptr;
+};
+
+namespace {
+
+int select_nodes(bvhgb_bn13_workspace *ws, const bvhgb_node *nodes, cudaStream_t s) {
+  if (ws->numInner == 0) return BVHGB_OK;
+  const uint32_t grid = min(ceil_div(ws->numInner, 256), (uint32_t)sm_count() * 8);
+  cost_kernel<<<grid, 256, 0, s>>>(nodes, ws->inner, ws->numInner, ws->keys, ws->vals);
+  BVHGB_LAUNCH_CHECK("bn13 cost");
+  return sort_pairs(ws->sortTemp, ws->keys, ws->keysSorted, ws->vals, ws->todo, ws->numInner, 4, 0, 32, s);
+}
+
+int run_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t c, cudaStream_t s) {
+  const uint32_t cs = ws->chunkSize;
+  if (cs == 0) return BVHGB_OK;
+  const uint32_t bs = ws->cfg.blockSize ? ws->cfg.blockSize : 128;
+  const uint32_t grid = ceil_div(cs, bs);
+  patch_kernel<<<grid, bs, 0, s>>>(nodes, ws->root, ws->todo, ws->numInner, c, ws->numChunks, cs, ws->cfg.offsetAccess,
+                                   ws->patches, ws->valid, ws->toFix, ws->owner, ws->heaps, ws->cfg.heapCapacity,
+                                   ws->stats);
+  BVHGB_LAUNCH_CHECK("bn13 patch");
+  apply_kernel<<<grid, bs, 0, s>>>(nodes, ws->patches, ws->valid, ws->toFix, ws->owner, cs, ws->stats);
+  BVHGB_LAUNCH_CHECK("bn13 apply");
+  count_kernel<<<grid, bs, 0, s>>>(nodes, ws->root, ws->patches, ws->toFix, ws->owner, ws->counter, cs, ws->numNodes,
+                                   ws->err);
+  BVHGB_LAUNCH_CHECK("bn13 count");
+  refit_kernel<<<ceil_div(3ull * cs, bs), bs, 0, s>>>(nodes, ws->root, ws->toFix, ws->counter, cs, ws->numNodes, ws->err);
+  BVHGB_LAUNCH_CHECK("bn13 refit");
+  return BVHGB_OK;
+}
+
+int do_step(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, cudaStream_t s) {
+  int st = select_nodes(ws, nodes, s);
+  if (st) return st;
+  for (uint32_t c = 0; c < ws->numChunks; ++c)
+    if ((st = run_chunk(ws, nodes, c, s))) return st;
+  return BVHGB_OK;
+}
+
+}  // namespace
+
+extern "C" BVHGB_API int bvhgb_bn13_create(const bvhgb_node *nodes, uint32_t numNodes, uint32_t root,
+                                           const bvhgb_bn13_config *cfg, bvhgb_bn13_workspace **out,
+                                           bvhgb_stream stream) {
+  if (!out || !nodes || numNodes == 0 || root >= numNodes) return BVHGB_INVALID_ARGUMENT;
+  *out = nullptr;
+  auto *ws = new bvhgb_bn13_workspace();
+  ws->cfg = cfg ? *cfg : bvhgb_bn13_config{32u, 128u, 1.0f, 0u, 4096u};
+  if (ws->cfg.numChunks == 0) ws->cfg.numChunks = 1;
+  if (ws->cfg.heapCapacity < 4) ws->cfg.heapCapacity = 4096;
+  if (ws->cfg.blockSize == 0 || ws->cfg.blockSize > 1024) ws->cfg.blockSize = 128;
+  float bp = ws->cfg.batchPercent;
+  if (bp <= 0.01f) bp = 0.01f;  // Bittner13GPU.cpp:59-60
+  if (bp >= 75.0f) bp = 75.0f;
+  ws->cfg.batchPercent = bp;
+  int pst = sort_prepare();
+  if (pst) {
+    delete ws;
+    return pst;
+  }
+  ws->numNodes = numNodes;
+  ws->root = root;
+  ws->numChunks = ws->cfg.numChunks;
+  const uint32_t lNum = (uint32_t)((bp / 100.0f) * (float)numNodes);  // Bittner13GPU.cpp:79-80
+  ws->chunkSize = lNum / ws->numChunks;
+  cudaStream_t s = as_stream(stream);
+
+  // initData (Bittner13CUDA.cu:939-987): inner nodes in ascending index order.
+  std::vector<uint32_t> hflags(numNodes);
+  uint32_t *dflag = nullptr;
+  cudaError_t e = cudaMalloc(&dflag, 4ull * numNodes);
+  if (e == cudaSuccess) {
+    init_inner_kernel<<<min(ceil_div(numNodes, 256), 4096u), 256, 0, s>>>(nodes, numNodes, dflag);
+    count_launch();
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hflags.data(), dflag, 4ull * numNodes, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(dflag);
+  std::vector<uint32_t> inner;
+  inner.reserve(numNodes / 2 + 1);
+  for (uint32_t i = 0; i < numNodes; ++i)
+    if (hflags[i]) inner.push_back(i);
+  ws->numInner = (uint32_t)inner.size();
+  const size_t ni = inner.size() ? inner.size() : 1;
+  const size_t cs = ws->chunkSize ? ws->chunkSize : 1;
+  const size_t sortBytes = sort_temp_bytes(ws->numInner, 4, 0, 32);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->inner, 4 * ni);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->keys, 4 * ni);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->vals, 4 * ni);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->keysSorted, 4 * ni);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->todo, 4 * ni);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->sortTemp, sortBytes ? sortBytes : 256);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->patches, sizeof(PatchOut) * cs);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->valid, 4 * cs);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->toFix, 12 * cs);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->owner, 4ull * numNodes);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->counter, 4ull * numNodes);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->err, 4);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->heaps, sizeof(HeapItem) * cs * ws->cfg.heapCapacity);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->stats, sizeof(unsigned long long) * S_COUNT);
+  if (e == cudaSuccess && inner.size())
+    e = cudaMemcpyAsync(ws->inner, inner.data(), 4 * inner.size(), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ws->counter, 0, 4ull * numNodes, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ws->owner, 0xFF, 4ull * numNodes, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ws->err, 0, 4, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ws->stats, 0, sizeof(unsigned long long) * S_COUNT, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    set_last_error("bvhgb_bn13_create", e);
+    bvhgb_bn13_destroy(ws);
+    return e == cudaErrorMemoryAllocation ? BVHGB_OUT_OF_MEMORY : BVHGB_CUDA_ERROR;
+  }
+  *out = ws;
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_bn13_destroy(bvhgb_bn13_workspace *ws) {
+  if (!ws) return BVHGB_OK;
+  if (ws->graph) cudaGraphExecDestroy(ws->graph);
+  cudaFree(ws->inner);
+  cudaFree(ws->keys);
+  cudaFree(ws->vals);
+  cudaFree(ws->keysSorted);
+  cudaFree(ws->todo);
+  cudaFree(ws->sortTemp);
+  cudaFree(ws->patches);
+  cudaFree(ws->valid);
+  cudaFree(ws->toFix);
+  cudaFree(ws->owner);
+  cudaFree(ws->counter);
+  cudaFree(ws->err);
+  cudaFree(ws->heaps);
+  cudaFree(ws->stats);
+  delete ws;
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API uint32_t bvhgb_bn13_batch_size(const bvhgb_bn13_workspace *ws) {
+  return ws ? ws->chunkSize * ws->numChunks : 0;
+}
+
+extern "C" BVHGB_API int bvhgb_bn13_select_nodes(bvhgb_bn13_workspace *ws, const bvhgb_node *nodes, bvhgb_stream stream) {
+  if (!ws || !nodes) return BVHGB_INVALID_ARGUMENT;
+  return select_nodes(ws, nodes, as_stream(stream));
+}
+
+extern "C" BVHGB_API int bvhgb_bn13_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t chunk, bvhgb_stream stream) {
+  if (!ws || !nodes || chunk >= ws->numChunks) return BVHGB_INVALID_ARGUMENT;
+  return run_chunk(ws, nodes, chunk, as_stream(stream));
+}
+
+extern "C" BVHGB_API int bvhgb_bn13_step(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, bvhgb_stream stream) {
+  if (!ws || !nodes) return BVHGB_INVALID_ARGUMENT;
+  return do_step(ws, nodes, as_stream(stream));
+}
+
+extern "C" BVHGB_API int bvhgb_bn13_run(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t iterations,
+                                        bvhgb_stream stream) {
+  if (!ws || !nodes) return BVHGB_INVALID_ARGUMENT;
+  if (iterations == 0) return BVHGB_OK;
+  cudaStream_t s = as_stream(stream);
+  // Capture one iteration on a private stream, then replay it on the caller's stream.
+  if (ws->graph && ws->graphNodes != nodes) {
+    cudaGraphExecDestroy(ws->graph);
+    ws->graph = nullptr;
+  }
+  if (!ws->graph) {
+    int pst = sort_prepare();
+    if (pst) return pst;
+    cudaStream_t cap = nullptr;
+    BVHGB_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    int st = BVHGB_OK;
+    if (e == cudaSuccess) {
+      st = do_step(ws, nodes, cap);
+      e = cudaStreamEndCapture(cap, &g);
+    }
+    if (e == cudaSuccess && st == BVHGB_OK) e = cudaGraphInstantiate(&ws->graph, g, 0);
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(cap);
+    if (st) return st;
+    if (e != cudaSuccess) {
+      set_last_error("bvhgb_bn13_run capture", e);
+      ws->graph = nullptr;
+      return BVHGB_CUDA_ERROR;
+    }
+    ws->graphNodes = nodes;
+  }
+  for (uint32_t i = 0; i < iterations; ++i) {
+    BVHGB_CUDA_TRY(cudaGraphLaunch(ws->graph, s));
+  }
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_bn13_get_stats(bvhgb_bn13_workspace *ws, bvhgb_bn13_stats *stats, bvhgb_stream stream) {
+  if (!ws || !stats) return BVHGB_INVALID_ARGUMENT;
+  unsigned long long h[S_COUNT];
+  uint32_t err = 0;
+  cudaStream_t s = as_stream(stream);
+  BVHGB_CUDA_TRY(cudaMemcpyAsync(h, ws->stats, sizeof(h), cudaMemcpyDeviceToHost, s));
+  BVHGB_CUDA_TRY(cudaMemcpyAsync(&err, ws->err, 4, cudaMemcpyDeviceToHost, s));
+  BVHGB_CUDA_TRY(cudaStreamSynchronize(s));
+  stats->items = h[S_ITEMS];
+  stats->applied = h[S_APPLIED];
+  stats->skippedConflict = h[S_CONFLICT];
+  stats->skippedInvalid = h[S_INVALID];
+  stats->heapOverflow = h[S_OVERFLOW];
+  return err ? BVHGB_BVH_ERROR : BVHGB_OK;
+}

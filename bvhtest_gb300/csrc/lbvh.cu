@@ -1,0 +1,410 @@
+// LBVH build: scene box, Morton codes, onesweep sort, and a fused bottom-up topology + refit.
+//
+// Reference: lib/builder/LBVH_CUDA.cu. Kernel plan (HBM-bound, no tensor cores):
+//   lbvh_bounds  : per-triangle box (+-FLT_EPSILON) reduced into the scene box, whose initial value
+//                  is the origin box (LBVH_CUDA.cu:60-119). Reads faces + vertices once.
+//   lbvh_morton  : re-reads the triangle, centroid -> 30- or 63-bit Morton key + index
+//                  (LBVH_CUDA.cu:132-183); also resets the build's exchange slots.
+//   sort         : sort.cu (replaces cub::DeviceRadixSort, LBVH_CUDA.cu:185-193).
+//   lbvh_build   : one thread per sorted leaf writes the leaf and climbs (Apetrei 2014 style): at each
+//                  step it picks the parent from the two neighbouring key deltas, meets its sibling
+//                  through one acq_rel exchange on the split slot, and the second thread to arrive
+//                  merges the boxes and writes the parent with the Karras node index the reference
+//                  assigns (kGenLeafNodes + kBuildTree + kFixAABBTree, LBVH_CUDA.cu:273-374).
+#include <cstring>
+
+#include "common.cuh"
+#include "sort.cuh"
+
+struct bvhgb_lbvh_workspace {
+  uint32_t maxFaces = 0;
+  bvhgb_lbvh_config cfg{};
+  uint32_t keyBytes = 4;
+  uint32_t *scene = nullptr;  // 6 order-mapped floats + error word
+  void *keys = nullptr;
+  void *keysSorted = nullptr;
+  uint32_t *vals = nullptr;
+  uint32_t *valsSorted = nullptr;
+  uint32_t *slots = nullptr;
+  void *sortTemp = nullptr;
+  size_t sortTempBytes = 0;
+};
+
+namespace bvhgb {
+namespace {
+
+constexpr int kBoundsThreads = 256;
+constexpr int kMortonThreads = 256;
+constexpr int kBuildThreads = 128;
+
+// kInitTriData (LBVH_CUDA.cu:60-96): box from the three vertices with the reference's compare
+// order, grown by FLT_EPSILON; centroid ((v1 + v2) + v3) / 3.
+__device__ __forceinline__ void tri_box(const float *__restrict__ vert, const uint32_t *__restrict__ faces, uint32_t f,
+                                        Box &b, float *c) {
+  uint32_t i1 = __ldg(faces + 3 * (size_t)f), i2 = __ldg(faces + 3 * (size_t)f + 1), i3 = __ldg(faces + 3 * (size_t)f + 2);
+  float v1[3], v2[3], v3[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    v1[k] = __ldg(vert + 3 * (size_t)i1 + k);
+    v2[k] = __ldg(vert + 3 * (size_t)i2 + k);
+    v3[k] = __ldg(vert + 3 * (size_t)i3 + k);
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float mn = v1[k], mx = v2[k];
+    if (v2[k] < mn) mn = v2[k];
+    if (v3[k] < mn) mn = v3[k];
+    if (v1[k] > mx) mx = v1[k];
+    if (v3[k] > mx) mx = v3[k];
+    b.mn[k] = fsub(mn, FLT_EPSILON);
+    b.mx[k] = fadd(mx, FLT_EPSILON);
+    if (c) c[k] = fdiv(fadd(fadd(v1[k], v2[k]), v3[k]), 3.0f);
+  }
+}
+
+__global__ void lbvh_init_kernel(uint32_t *scene) {
+  if (threadIdx.x < 6) scene[threadIdx.x] = f2ord(0.0f);  // origin box [(0,0,0),(0,0,0)]
+  if (threadIdx.x == 6) scene[6] = 0;                     // error word
+}
+
+__global__ void __launch_bounds__(kBoundsThreads) lbvh_bounds_kernel(const float *__restrict__ vert,
+                                                                     const uint32_t *__restrict__ faces, uint32_t n,
+                                                                     uint32_t *scene) {
+  // Starting the local box at the origin is the same as merging the reduction's initial value.
+  float mn[3] = {0.0f, 0.0f, 0.0f}, mx[3] = {0.0f, 0.0f, 0.0f};
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    Box b;
+    tri_box(vert, faces, (uint32_t)i, b, nullptr);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      mn[k] = fminf(mn[k], b.mn[k]);
+      mx[k] = fmaxf(mx[k], b.mx[k]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mn[k] = fminf(mn[k], __shfl_xor_sync(0xFFFFFFFFu, mn[k], o));
+      mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xFFFFFFFFu, mx[k], o));
+    }
+  }
+  __shared__ float red[kBoundsThreads / 32][6];
+  const uint32_t warp = threadIdx.x >> 5;
+  if (lane_id() == 0) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { red[warp][k] = mn[k]; red[warp][3 + k] = mx[k]; }
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    float v = red[0][threadIdx.x];
+    for (int w = 1; w < kBoundsThreads / 32; ++w)
+      v = threadIdx.x < 3 ? fminf(v, red[w][threadIdx.x]) : fmaxf(v, red[w][threadIdx.x]);
+    if (threadIdx.x < 3) atomicMin(&scene[threadIdx.x], f2ord(v));
+    else atomicMax(&scene[threadIdx.x], f2ord(v));
+  }
+}
+
+// Expands the low 10 / 21 bits of v so that two zero bits follow every bit.
+__device__ __forceinline__ uint32_t spread10(uint32_t v) {
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+__device__ __forceinline__ uint64_t spread21(uint64_t v) {
+  v &= 0x1FFFFFull;
+  v = (v | (v << 32)) & 0x001F00000000FFFFull;
+  v = (v | (v << 16)) & 0x001F0000FF0000FFull;
+  v = (v | (v << 8)) & 0x100F00F00F00F00Full;
+  v = (v | (v << 4)) & 0x10C30C30C30C30C3ull;
+  v = (v | (v << 2)) & 0x1249249249249249ull;
+  return v;
+}
+
+// kCalcMortonCodes (LBVH_CUDA.cu:140-166): (c + offset) * scale * cells, clamped, truncated.
+__device__ __forceinline__ uint32_t quantise(float c, float off, float scale, float cells, float maxcell) {
+  c = fadd(c, off);
+  c = fmul(c, scale);
+  c = fmul(c, cells);
+  if (c < 0.0f) c = 0.0f;
+  if (c > maxcell) c = maxcell;
+  return (uint32_t)c;
+}
+
+template <int BITS>
+__global__ void __launch_bounds__(kMortonThreads) lbvh_morton_kernel(const float *__restrict__ vert,
+                                                                     const uint32_t *__restrict__ faces, uint32_t n,
+                                                                     const uint32_t *__restrict__ scene, void *keysOut,
+                                                                     uint32_t *__restrict__ vals,
+                                                                     uint32_t *__restrict__ slots) {
+  // Host part of LBVH_calcMortonCodes (LBVH_CUDA.cu:171-180), evaluated per block.
+  float off[3], sc[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float mn = ord2f(scene[k]), mx = ord2f(scene[3 + k]);
+    off[k] = fsub(0.0f, mn);
+    sc[k] = fdiv(1.0f, fadd(mx, off[k]));
+  }
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    Box b;
+    float c[3];
+    tri_box(vert, faces, (uint32_t)i, b, c);
+    if (BITS == 30) {
+      uint32_t x = quantise(c[0], off[0], sc[0], 1024.0f, 1023.0f);
+      uint32_t y = quantise(c[1], off[1], sc[1], 1024.0f, 1023.0f);
+      uint32_t z = quantise(c[2], off[2], sc[2], 1024.0f, 1023.0f);
+      static_cast<uint32_t *>(keysOut)[i] = spread10(x) * 4u + spread10(y) * 2u + spread10(z);
+    } else {
+      uint64_t x = quantise(c[0], off[0], sc[0], 2097152.0f, 2097151.0f);
+      uint64_t y = quantise(c[1], off[1], sc[1], 2097152.0f, 2097151.0f);
+      uint64_t z = quantise(c[2], off[2], sc[2], 2097152.0f, 2097151.0f);
+      static_cast<uint64_t *>(keysOut)[i] = spread21(x) * 4u + spread21(y) * 2u + spread21(z);
+    }
+    vals[i] = (uint32_t)i;
+    if (i + 1 < n) slots[i] = kNone;
+  }
+}
+
+// delta(i, j) (LBVH_CUDA.cu:208-212) for in-range i != j.
+template <int MODE, typename K>
+__device__ __forceinline__ int delta(const K *__restrict__ keys, uint32_t i, uint32_t j) {
+  if (MODE == BVHGB_TOPO_REFCOMPAT) return __clz((int)(i ^ j));
+  K a = __ldg(keys + i), b = __ldg(keys + j);
+  if (a != b) return sizeof(K) == 8 ? __clzll((long long)(a ^ b)) : __clz((int)(a ^ b));
+  return (int)(8 * sizeof(K)) + __clz((int)(i ^ j));
+}
+
+// True when the node covering [l, r] is the LEFT child of its parent (parent split = r).
+template <int MODE, typename K>
+__device__ __forceinline__ bool parent_is_right(const K *keys, uint32_t l, uint32_t r, uint32_t n) {
+  if (l == 0) return true;
+  if (r == n - 1) return false;
+  return delta<MODE, K>(keys, r, r + 1) > delta<MODE, K>(keys, l - 1, l);
+}
+
+__device__ __forceinline__ void store_record(bvhgb_node *nd, const Box &b, uint32_t parent, uint32_t left,
+                                             uint32_t right, uint32_t leaf, uint32_t isLeft, uint32_t level) {
+  float4 *p = reinterpret_cast<float4 *>(nd);
+  float sa = surface_area(b);
+  p[0] = make_float4(b.mn[0], b.mn[1], b.mn[2], b.mx[0]);
+  p[1] = make_float4(b.mx[1], b.mx[2], __uint_as_float(parent), __uint_as_float(left));
+  p[2] = make_float4(__uint_as_float(right), __uint_as_float(leaf | (isLeft << 16)), __uint_as_float(level),
+                     sa);
+}
+
+__device__ __forceinline__ void set_parent(bvhgb_node *nd, uint32_t parent, uint16_t isLeft) {
+  nd->parent = parent;
+  nd->isLeft = isLeft;
+}
+
+template <int MODE, typename K>
+__global__ void __launch_bounds__(kBuildThreads) lbvh_build_kernel(const float *__restrict__ vert,
+                                                                   const uint32_t *__restrict__ faces,
+                                                                   const K *__restrict__ keys,
+                                                                   const uint32_t *__restrict__ idx, uint32_t n,
+                                                                   bvhgb_node *nodes, uint32_t *slots) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  // Leaf (kGenLeafNodes, LBVH_CUDA.cu:273-292): left = face, right = 1, level = UINT8_MAX.
+  const uint32_t face = __ldg(idx + i);
+  Box box;
+  tri_box(vert, faces, face, box, nullptr);
+  const uint32_t leafIdx = n - 1 + i;
+  if (n == 1) {
+    store_record(nodes + leafIdx, box, 0u, face, 1u, 1u, 0u, 255u);
+    return;
+  }
+  store_record(nodes + leafIdx, box, kNone, face, 1u, 1u, 0u, 255u);
+
+  uint32_t l = i, r = i;
+  bool right = parent_is_right<MODE, K>(keys, l, r, n);
+  for (;;) {
+    const uint32_t split = right ? r : l - 1;
+    // Meet the sibling: the first thread leaves its far end in the slot and stops.
+    const uint32_t other = atom_exch_acq_rel(&slots[split], right ? l : r);
+    if (other == kNone) return;
+    const uint32_t L = right ? l : other, R = right ? other : r;
+    const uint32_t a = (L == split) ? n - 1 + split : split;          // left child  [L, split]
+    const uint32_t b = (split + 1 == R) ? n - 1 + split + 1 : split + 1;  // right child [split+1, R]
+    const Box sib = load_box_cg(nodes + (right ? b : a));
+    Box pb;
+    if (right) { pb = box; merge_into(pb, sib); }   // left child's box merged with the right's
+    else { pb = sib; merge_into(pb, box); }
+    l = L;
+    r = R;
+    const bool root = (l == 0 && r == n - 1);
+    uint32_t pidx = 0;
+    if (!root) {
+      right = parent_is_right<MODE, K>(keys, l, r, n);
+      pidx = right ? r : l;  // Karras index: a left child is numbered by its last key, a right child by its first
+    }
+    store_record(nodes + pidx, pb, root ? 0u : kNone, a, b, 0u, 0u, 0u);
+    set_parent(nodes + a, pidx, 1);
+    set_parent(nodes + b, pidx, 0);
+    if (root) return;
+    box = pb;
+  }
+}
+
+template <int MODE>
+int launch_build(const bvhgb_lbvh_workspace *ws, const float *vert, const uint32_t *faces, uint32_t n,
+                 bvhgb_node *nodes, cudaStream_t s) {
+  dim3 grid(ceil_div(n, kBuildThreads));
+  if (ws->keyBytes == 4)
+    lbvh_build_kernel<MODE, uint32_t><<<grid, kBuildThreads, 0, s>>>(
+        vert, faces, static_cast<const uint32_t *>(ws->keysSorted), ws->valsSorted, n, nodes, ws->slots);
+  else
+    lbvh_build_kernel<MODE, uint64_t><<<grid, kBuildThreads, 0, s>>>(
+        vert, faces, static_cast<const uint64_t *>(ws->keysSorted), ws->valsSorted, n, nodes, ws->slots);
+  BVHGB_LAUNCH_CHECK("lbvh build");
+  return BVHGB_OK;
+}
+
+int check_ws(const bvhgb_lbvh_workspace *ws, uint32_t n) {
+  if (!ws) return BVHGB_INVALID_ARGUMENT;
+  if (n > ws->maxFaces) return BVHGB_TOO_LARGE;
+  return BVHGB_OK;
+}
+
+}  // namespace
+}  // namespace bvhgb
+
+using namespace bvhgb;
+
+extern "C" BVHGB_API int bvhgb_lbvh_create(uint32_t maxFaces, const bvhgb_lbvh_config *cfg, bvhgb_lbvh_workspace **out) {
+  if (!out) return BVHGB_INVALID_ARGUMENT;
+  *out = nullptr;
+  bvhgb_lbvh_config c = cfg ? *cfg : bvhgb_lbvh_config{30u, BVHGB_TOPO_REFCOMPAT};
+  if ((c.mortonBits != 30 && c.mortonBits != 63) || c.topology > BVHGB_TOPO_KARRAS) return BVHGB_INVALID_ARGUMENT;
+  if (maxFaces >= (1u << 30)) return BVHGB_TOO_LARGE;
+  int pst = sort_prepare();
+  if (pst) return pst;
+  auto *ws = new bvhgb_lbvh_workspace();
+  ws->maxFaces = maxFaces;
+  ws->cfg = c;
+  ws->keyBytes = c.mortonBits == 30 ? 4u : 8u;
+  const size_t m = maxFaces ? maxFaces : 1;
+  ws->sortTempBytes = sort_temp_bytes(maxFaces, ws->keyBytes, 0, c.mortonBits);
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = cudaMalloc(&ws->scene, 256);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->keys, ws->keyBytes * m);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->keysSorted, ws->keyBytes * m);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->vals, 4 * m);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->valsSorted, 4 * m);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->slots, 4 * m);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->sortTemp, ws->sortTempBytes ? ws->sortTempBytes : 256);
+  if (e != cudaSuccess) {
+    set_last_error("bvhgb_lbvh_create", e);
+    bvhgb_lbvh_destroy(ws);
+    return e == cudaErrorMemoryAllocation ? BVHGB_OUT_OF_MEMORY : BVHGB_CUDA_ERROR;
+  }
+  *out = ws;
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_lbvh_destroy(bvhgb_lbvh_workspace *ws) {
+  if (!ws) return BVHGB_OK;
+  cudaFree(ws->scene);
+  cudaFree(ws->keys);
+  cudaFree(ws->keysSorted);
+  cudaFree(ws->vals);
+  cudaFree(ws->valsSorted);
+  cudaFree(ws->slots);
+  cudaFree(ws->sortTemp);
+  delete ws;
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_lbvh_init_tri_data(bvhgb_lbvh_workspace *ws, const float *vert, const uint32_t *faces,
+                                                  uint32_t n, bvhgb_stream stream) {
+  int st = check_ws(ws, n);
+  if (st) return st;
+  cudaStream_t s = as_stream(stream);
+  lbvh_init_kernel<<<1, 32, 0, s>>>(ws->scene);
+  BVHGB_LAUNCH_CHECK("lbvh init");
+  if (n == 0) return BVHGB_OK;
+  if (!vert || !faces) return BVHGB_INVALID_ARGUMENT;
+  uint32_t grid = min(ceil_div(n, kBoundsThreads * 4), (uint32_t)sm_count() * 8);
+  lbvh_bounds_kernel<<<grid, kBoundsThreads, 0, s>>>(vert, faces, n, ws->scene);
+  BVHGB_LAUNCH_CHECK("lbvh bounds");
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_lbvh_calc_morton(bvhgb_lbvh_workspace *ws, const float *vert, const uint32_t *faces,
+                                                uint32_t n, bvhgb_stream stream) {
+  int st = check_ws(ws, n);
+  if (st) return st;
+  if (n == 0) return BVHGB_OK;
+  if (!vert || !faces) return BVHGB_INVALID_ARGUMENT;
+  cudaStream_t s = as_stream(stream);
+  uint32_t grid = ceil_div(n, kMortonThreads * 2);
+  if (ws->cfg.mortonBits == 30)
+    lbvh_morton_kernel<30><<<grid, kMortonThreads, 0, s>>>(vert, faces, n, ws->scene, ws->keys, ws->vals, ws->slots);
+  else
+    lbvh_morton_kernel<63><<<grid, kMortonThreads, 0, s>>>(vert, faces, n, ws->scene, ws->keys, ws->vals, ws->slots);
+  BVHGB_LAUNCH_CHECK("lbvh morton");
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_lbvh_sort(bvhgb_lbvh_workspace *ws, uint32_t n, bvhgb_stream stream) {
+  int st = check_ws(ws, n);
+  if (st) return st;
+  return sort_pairs(ws->sortTemp, ws->keys, ws->keysSorted, ws->vals, ws->valsSorted, n, ws->keyBytes, 0,
+                    ws->cfg.mortonBits, as_stream(stream));
+}
+
+extern "C" BVHGB_API int bvhgb_lbvh_build_tree(bvhgb_lbvh_workspace *ws, const float *vert, const uint32_t *faces,
+                                               uint32_t n, bvhgb_node *nodes, bvhgb_stream stream) {
+  int st = check_ws(ws, n);
+  if (st) return st;
+  if (n == 0) return BVHGB_OK;
+  if (!vert || !faces || !nodes) return BVHGB_INVALID_ARGUMENT;
+  if (ws->cfg.topology == BVHGB_TOPO_REFCOMPAT)
+    return launch_build<BVHGB_TOPO_REFCOMPAT>(ws, vert, faces, n, nodes, as_stream(stream));
+  return launch_build<BVHGB_TOPO_KARRAS>(ws, vert, faces, n, nodes, as_stream(stream));
+}
+
+extern "C" BVHGB_API int bvhgb_lbvh_build(bvhgb_lbvh_workspace *ws, const float *vert, const uint32_t *faces,
+                                          uint32_t n, bvhgb_node *nodes, bvhgb_stream stream) {
+  int st = check_ws(ws, n);
+  if (st) return st;
+  if (n == 0) return BVHGB_OK;
+  if (!vert || !faces || !nodes) return BVHGB_INVALID_ARGUMENT;
+  if ((st = bvhgb_lbvh_init_tri_data(ws, vert, faces, n, stream))) return st;
+  if ((st = bvhgb_lbvh_calc_morton(ws, vert, faces, n, stream))) return st;
+  if ((st = bvhgb_lbvh_sort(ws, n, stream))) return st;
+  return bvhgb_lbvh_build_tree(ws, vert, faces, n, nodes, stream);
+}
+
+extern "C" BVHGB_API int bvhgb_lbvh_read_scene_box(bvhgb_lbvh_workspace *ws, bvhgb_aabb *scene, bvhgb_stream stream) {
+  if (!ws || !scene) return BVHGB_INVALID_ARGUMENT;
+  uint32_t h[6];
+  cudaStream_t s = as_stream(stream);
+  BVHGB_CUDA_TRY(cudaMemcpyAsync(h, ws->scene, sizeof(h), cudaMemcpyDeviceToHost, s));
+  BVHGB_CUDA_TRY(cudaStreamSynchronize(s));
+  float f[6];
+  for (int k = 0; k < 6; ++k) {
+    uint32_t u = h[k];
+    uint32_t bits = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
+    std::memcpy(&f[k], &bits, 4);
+  }
+  scene->minMax[0] = {f[0], f[1], f[2]};
+  scene->minMax[1] = {f[3], f[4], f[5]};
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_lbvh_read_keys(bvhgb_lbvh_workspace *ws, int sorted, void *keys_host, uint32_t *idx_host,
+                                              uint32_t n, bvhgb_stream stream) {
+  int st = check_ws(ws, n);
+  if (st) return st;
+  cudaStream_t s = as_stream(stream);
+  if (keys_host)
+    BVHGB_CUDA_TRY(cudaMemcpyAsync(keys_host, sorted ? ws->keysSorted : ws->keys, (size_t)ws->keyBytes * n,
+                                   cudaMemcpyDeviceToHost, s));
+  if (idx_host)
+    BVHGB_CUDA_TRY(cudaMemcpyAsync(idx_host, sorted ? ws->valsSorted : ws->vals, 4ull * n, cudaMemcpyDeviceToHost, s));
+  BVHGB_CUDA_TRY(cudaStreamSynchronize(s));
+  return BVHGB_OK;
+}

@@ -1,0 +1,320 @@
+// Onesweep-style stable LSD radix sort of (key, uint32 value) pairs, 8-bit digits.
+//
+// Replaces cub::DeviceRadixSort::SortPairs (lib/builder/LBVH_CUDA.cu:185-193) and
+// SortPairsDescending (lib/builder/Bittner13CUDA.cu:674-680). Design (Adinets & Merrill 2022):
+//   1. one read of all keys builds the digit histograms of every pass;
+//   2. a tiny scan turns them into global digit offsets;
+//   3. per pass, one kernel: each CTA takes the next tile index from an atomic counter (so the
+//      tiles it looks back on are already running), ranks its 4096 keys stably with warp
+//      match/ballot, publishes per-digit counts, resolves its exclusive prefix by decoupled
+//      look-back (bounded spin), stages the tile in shared memory in digit order and writes it
+//      out in runs, so each digit's run is a contiguous store.
+#include "common.cuh"
+#include "sort.cuh"
+
+namespace bvhgb {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kItems = 16;
+constexpr int kTile = kThreads * kItems;  // 4096 keys per CTA
+constexpr int kWarps = kThreads / 32;
+constexpr int kRadix = 256;
+constexpr int kBins = kRadix + 1;  // + a bin for padding keys of the last tile
+constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr uint32_t kFlagInc = 2u << 30;
+constexpr uint32_t kFlagMask = 3u << 30;
+constexpr uint32_t kValMask = (1u << 30) - 1u;
+
+// The last digit may be narrower than 8 bits when (endBit - beginBit) is not a multiple of 8.
+__host__ __device__ __forceinline__ uint32_t digit_mask(uint32_t shift, uint32_t endBit) {
+  const uint32_t w = endBit - shift;
+  return w >= 8 ? 0xFFu : ((1u << w) - 1u);
+}
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct Layout {
+  size_t hist, counters, err, status, altKeys, altVals, total;
+  uint32_t passes, tiles;
+};
+
+Layout make_layout(uint32_t n, uint32_t keyBytes, uint32_t beginBit, uint32_t endBit) {
+  Layout L{};
+  L.passes = (endBit > beginBit) ? (endBit - beginBit + 7) / 8 : 0;
+  L.tiles = n ? (uint32_t)((n + kTile - 1) / kTile) : 0;
+  size_t off = 0;
+  L.hist = off;     off = align256(off + sizeof(uint32_t) * kRadix * (L.passes ? L.passes : 1));
+  L.counters = off; off = align256(off + sizeof(uint32_t) * (L.passes ? L.passes : 1));
+  L.err = off;      off = align256(off + sizeof(uint32_t));
+  L.status = off;   off = align256(off + sizeof(uint32_t) * kRadix * (size_t)L.tiles * (L.passes ? L.passes : 1));
+  L.altKeys = off;  off = align256(off + (size_t)keyBytes * n);
+  L.altVals = off;  off = align256(off + sizeof(uint32_t) * (size_t)n);
+  L.total = off;
+  return L;
+}
+
+template <typename K>
+__global__ void __launch_bounds__(kThreads) histogram_kernel(const K *__restrict__ keys, uint32_t n,
+                                                             uint32_t beginBit, uint32_t endBit, uint32_t passes,
+                                                             uint32_t *__restrict__ hist) {
+  extern __shared__ uint32_t sh[];  // passes * 256
+  for (uint32_t i = threadIdx.x; i < passes * kRadix; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    K k = keys[i];
+    for (uint32_t p = 0; p < passes; ++p) {
+      const uint32_t sh0 = beginBit + 8 * p;
+      uint32_t d = (uint32_t)(k >> sh0) & digit_mask(sh0, endBit);
+      atomicAdd(&sh[p * kRadix + d], 1u);
+    }
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < passes * kRadix; i += blockDim.x)
+    if (sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+
+// Exclusive scan of each pass's 256 counts, in place. One CTA per pass.
+__global__ void __launch_bounds__(kRadix) scan_kernel(uint32_t *hist) {
+  __shared__ uint32_t s[kRadix];
+  uint32_t *h = hist + blockIdx.x * kRadix;
+  uint32_t v = h[threadIdx.x];
+  s[threadIdx.x] = v;
+  __syncthreads();
+  for (int off = 1; off < kRadix; off <<= 1) {
+    uint32_t t = threadIdx.x >= (unsigned)off ? s[threadIdx.x - off] : 0u;
+    __syncthreads();
+    s[threadIdx.x] += t;
+    __syncthreads();
+  }
+  h[threadIdx.x] = s[threadIdx.x] - v;
+}
+
+template <typename K>
+struct OnesweepSmem {
+  uint32_t warpHist[kWarps][kBins];
+  uint32_t tileStart[kRadix];
+  uint32_t globalBase[kRadix];
+  uint32_t tileIdx;
+  K keys[kTile];
+  uint32_t vals[kTile];
+};
+
+template <typename K>
+__global__ void __launch_bounds__(kThreads) onesweep_kernel(const K *__restrict__ keysIn, K *__restrict__ keysOut,
+                                                            const uint32_t *__restrict__ valsIn,
+                                                            uint32_t *__restrict__ valsOut, uint32_t n,
+                                                            uint32_t shift, uint32_t mask,
+                                                            const uint32_t *__restrict__ offsets,
+                                                            uint32_t *tileCounter, uint32_t *status, uint32_t *err) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  OnesweepSmem<K> &sm = *reinterpret_cast<OnesweepSmem<K> *>(smraw);
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+
+  if (threadIdx.x == 0) sm.tileIdx = atomicAdd(tileCounter, 1u);
+  for (uint32_t i = lane; i < kBins; i += 32) sm.warpHist[warp][i] = 0;
+  __syncthreads();
+  const uint32_t tile = sm.tileIdx;
+  const uint64_t base = (uint64_t)tile * kTile;
+  const uint32_t valid = (uint32_t)min((uint64_t)kTile, (uint64_t)n - base);
+
+  // Warp-striped load: warp w owns keys [w*kItems*32, (w+1)*kItems*32) of the tile.
+  K key[kItems];
+  uint32_t val[kItems], dig[kItems], loc[kItems];
+#pragma unroll
+  for (int j = 0; j < kItems; ++j) {
+    uint32_t t = warp * (kItems * 32) + j * 32 + lane;
+    if (t < valid) {
+      key[j] = keysIn[base + t];
+      val[j] = valsIn[base + t];
+      dig[j] = (uint32_t)(key[j] >> shift) & mask;
+    } else {
+      key[j] = 0;
+      val[j] = 0;
+      dig[j] = kRadix;  // padding bin
+    }
+  }
+  // Stable rank within the warp: items in order, lanes in order.
+  const uint32_t ltMask = (1u << lane) - 1u;
+#pragma unroll
+  for (int j = 0; j < kItems; ++j) {
+    uint32_t peers = __match_any_sync(0xFFFFFFFFu, dig[j]);
+    uint32_t leader = __ffs(peers) - 1u;
+    uint32_t before = 0;
+    if (lane == leader) {
+      before = sm.warpHist[warp][dig[j]];
+      sm.warpHist[warp][dig[j]] = before + __popc(peers);
+    }
+    before = __shfl_sync(peers, before, leader);
+    loc[j] = before + __popc(peers & ltMask);
+    __syncwarp();
+  }
+  __syncthreads();
+
+  // Per digit: exclusive over warps, tile count, publish, look back.
+  uint32_t count = 0;
+  if (threadIdx.x < kRadix) {
+    const uint32_t d = threadIdx.x;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+      uint32_t c = sm.warpHist[w][d];
+      sm.warpHist[w][d] = count;
+      count += c;
+    }
+    uint32_t *st = status + (size_t)tile * kRadix + d;
+    st_release(st, (tile == 0 ? kFlagInc : kFlagAgg) | count);
+    uint32_t excl = 0;
+    if (tile > 0) {
+      uint32_t pred = tile - 1;
+      for (;;) {
+        const uint32_t *ps = status + (size_t)pred * kRadix + d;
+        uint32_t v = ld_acquire(ps);
+        uint32_t spins = 0;
+        while ((v & kFlagMask) == 0u) {
+          if (++spins > kSpinLimit) {
+            atomicOr(err, kErrTimeout);
+            break;
+          }
+          __nanosleep(32);
+          v = ld_acquire(ps);
+        }
+        excl += v & kValMask;
+        if ((v & kFlagInc) || pred == 0 || (v & kFlagMask) == 0u) break;
+        --pred;
+      }
+      st_release(st, kFlagInc | (excl + count));
+    }
+    sm.globalBase[d] = offsets[d] + excl;
+    sm.tileStart[d] = count;  // scanned below
+  }
+  __syncthreads();
+  // Exclusive scan of the tile counts over digits (in place, first warp).
+  if (warp == 0) {
+    uint32_t run = 0;
+    for (int c = 0; c < kRadix / 32; ++c) {
+      uint32_t v = sm.tileStart[c * 32 + lane];
+      uint32_t x = v;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= (unsigned)o) x += y;
+      }
+      sm.tileStart[c * 32 + lane] = run + x - v;
+      run += __shfl_sync(0xFFFFFFFFu, x, 31);
+    }
+  }
+  __syncthreads();
+  // Stage the tile in digit order.
+#pragma unroll
+  for (int j = 0; j < kItems; ++j) {
+    if (dig[j] < kRadix) {
+      uint32_t pos = sm.tileStart[dig[j]] + sm.warpHist[warp][dig[j]] + loc[j];
+      sm.keys[pos] = key[j];
+      sm.vals[pos] = val[j];
+    }
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < valid; i += kThreads) {
+    K k = sm.keys[i];
+    uint32_t d = (uint32_t)(k >> shift) & mask;
+    uint32_t dst = sm.globalBase[d] + (i - sm.tileStart[d]);
+    keysOut[dst] = k;
+    valsOut[dst] = sm.vals[i];
+  }
+}
+
+template <typename K>
+int sort_impl(void *temp, const Layout &L, const K *keysIn, K *keysOut, const uint32_t *valsIn, uint32_t *valsOut,
+              uint32_t n, uint32_t beginBit, uint32_t endBit, cudaStream_t s) {
+  char *t = static_cast<char *>(temp);
+  uint32_t *hist = reinterpret_cast<uint32_t *>(t + L.hist);
+  uint32_t *counters = reinterpret_cast<uint32_t *>(t + L.counters);
+  uint32_t *err = reinterpret_cast<uint32_t *>(t + L.err);
+  uint32_t *status = reinterpret_cast<uint32_t *>(t + L.status);
+  K *altK = reinterpret_cast<K *>(t + L.altKeys);
+  uint32_t *altV = reinterpret_cast<uint32_t *>(t + L.altVals);
+  if (n == 0) return BVHGB_OK;
+  if (L.passes == 0) {
+    BVHGB_CUDA_TRY(cudaMemcpyAsync(keysOut, keysIn, sizeof(K) * n, cudaMemcpyDeviceToDevice, s));
+    BVHGB_CUDA_TRY(cudaMemcpyAsync(valsOut, valsIn, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s));
+    return BVHGB_OK;
+  }
+  BVHGB_CUDA_TRY(cudaMemsetAsync(t, 0, L.altKeys, s));
+  uint32_t hgrid = min(ceil_div(n, kThreads * 8), (uint32_t)sm_count() * 4);
+  histogram_kernel<K><<<hgrid, kThreads, sizeof(uint32_t) * kRadix * L.passes, s>>>(keysIn, n, beginBit, endBit, L.passes, hist);
+  BVHGB_LAUNCH_CHECK("radix histogram");
+  scan_kernel<<<L.passes, kRadix, 0, s>>>(hist);
+  BVHGB_LAUNCH_CHECK("radix scan");
+  const size_t smem = sizeof(OnesweepSmem<K>);
+  int st = sort_prepare();
+  if (st) return st;
+  // Ping-pong so that the last pass lands in keysOut/valsOut.
+  const K *srcK = keysIn;
+  const uint32_t *srcV = valsIn;
+  for (uint32_t p = 0; p < L.passes; ++p) {
+    bool toOut = ((L.passes - 1 - p) % 2) == 0;
+    K *dstK = toOut ? keysOut : altK;
+    uint32_t *dstV = toOut ? valsOut : altV;
+    const uint32_t shift = beginBit + 8 * p;
+    onesweep_kernel<K><<<L.tiles, kThreads, smem, s>>>(srcK, dstK, srcV, dstV, n, shift, digit_mask(shift, endBit),
+                                                       hist + p * kRadix,
+                                                       counters + p, status + (size_t)p * L.tiles * kRadix, err);
+    BVHGB_LAUNCH_CHECK("radix onesweep");
+    srcK = dstK;
+    srcV = dstV;
+  }
+  return BVHGB_OK;
+}
+
+}  // namespace
+
+int sort_prepare() {
+  // Opt in to more than 48 KB of dynamic shared memory once per process (before any capture).
+  static int done = 0;
+  if (done) return BVHGB_OK;
+  BVHGB_CUDA_TRY(cudaFuncSetAttribute(onesweep_kernel<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sizeof(OnesweepSmem<uint32_t>)));
+  BVHGB_CUDA_TRY(cudaFuncSetAttribute(onesweep_kernel<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sizeof(OnesweepSmem<uint64_t>)));
+  done = 1;
+  return BVHGB_OK;
+}
+
+size_t sort_temp_bytes(uint32_t n, uint32_t keyBytes, uint32_t beginBit, uint32_t endBit) {
+  return make_layout(n, keyBytes, beginBit, endBit).total;
+}
+
+uint32_t *sort_error_word(void *temp, uint32_t n, uint32_t keyBytes, uint32_t beginBit, uint32_t endBit) {
+  Layout L = make_layout(n, keyBytes, beginBit, endBit);
+  return reinterpret_cast<uint32_t *>(static_cast<char *>(temp) + L.err);
+}
+
+int sort_pairs(void *temp, const void *keysIn, void *keysOut, const uint32_t *valsIn, uint32_t *valsOut, uint32_t n,
+               uint32_t keyBytes, uint32_t beginBit, uint32_t endBit, cudaStream_t s) {
+  Layout L = make_layout(n, keyBytes, beginBit, endBit);
+  if (keyBytes == 4)
+    return sort_impl<uint32_t>(temp, L, static_cast<const uint32_t *>(keysIn), static_cast<uint32_t *>(keysOut), valsIn,
+                               valsOut, n, beginBit, endBit, s);
+  return sort_impl<uint64_t>(temp, L, static_cast<const uint64_t *>(keysIn), static_cast<uint64_t *>(keysOut), valsIn,
+                             valsOut, n, beginBit, endBit, s);
+}
+
+}  // namespace bvhgb
+
+extern "C" BVHGB_API int bvhgb_radix_sort_pairs(void *temp, size_t *tempBytes, const void *keysIn, void *keysOut,
+                                                const uint32_t *valsIn, uint32_t *valsOut, uint32_t n,
+                                                uint32_t keyBytes, uint32_t beginBit, uint32_t endBit,
+                                                bvhgb_stream stream) {
+  if (!tempBytes || (keyBytes != 4 && keyBytes != 8) || beginBit > endBit || endBit > 8 * keyBytes)
+    return BVHGB_INVALID_ARGUMENT;
+  if (n >= (1u << 30)) return BVHGB_TOO_LARGE;
+  size_t need = bvhgb::sort_temp_bytes(n, keyBytes, beginBit, endBit);
+  if (!temp) {
+    *tempBytes = need;
+    return BVHGB_OK;
+  }
+  if (*tempBytes < need || (n && (!keysIn || !keysOut || !valsIn || !valsOut))) return BVHGB_INVALID_ARGUMENT;
+  return bvhgb::sort_pairs(temp, keysIn, keysOut, valsIn, valsOut, n, keyBytes, beginBit, endBit,
+                           bvhgb::as_stream(stream));
+}

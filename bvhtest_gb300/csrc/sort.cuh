@@ -1,0 +1,18 @@
+// Internal interface of the onesweep radix sort (sort.cu).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace bvhgb {
+// Sets the kernels' shared-memory attributes; call once before any stream capture.
+int sort_prepare();
+// Scratch bytes for sorting n pairs on key bits [beginBit, endBit).
+size_t sort_temp_bytes(uint32_t n, uint32_t keyBytes, uint32_t beginBit, uint32_t endBit);
+// Device word that the look-back sets to a non-zero error bit if a bounded wait gives up.
+uint32_t *sort_error_word(void *temp, uint32_t n, uint32_t keyBytes, uint32_t beginBit, uint32_t endBit);
+// Stable ascending sort; temp must hold sort_temp_bytes(...) bytes.
+int sort_pairs(void *temp, const void *keysIn, void *keysOut, const uint32_t *valsIn, uint32_t *valsOut, uint32_t n,
+               uint32_t keyBytes, uint32_t beginBit, uint32_t endBit, cudaStream_t s);
+}  // namespace bvhgb

@@ -1,0 +1,82 @@
+"""Seeded synthetic scenes with the shapes and distributions of the benchmark configurations.
+
+The reference's own mesh files are not available, so these generators stand in for them. Every
+scene is a soup of independent fp32 triangles (three unique vertices each, faces = iota), drawn
+from numpy's Philox counter-based generator so the same seed gives the same bytes on x86-64
+and aarch64.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def _rng(seed: int) -> np.random.Generator:
+    return np.random.Generator(np.random.Philox(int(seed)))
+
+
+def _soup(vert: np.ndarray):
+    vert = np.ascontiguousarray(vert.reshape(-1, 3), dtype=np.float32)
+    faces = np.arange(vert.shape[0], dtype=np.uint32).reshape(-1, 3)
+    return vert, faces
+
+
+def uniform_soup(n: int = 65536, sigma: float = 0.004, seed: int = 1):
+    """Small plain-method scene: centroids uniform in [0,1]^3, each vertex = centroid + N(0, sigma^2)
+    per axis (65,536 triangles by default)."""
+    g = _rng(seed)
+    c = g.random((n, 1, 3), dtype=np.float64).astype(np.float32)
+    off = g.normal(0.0, sigma, (n, 3, 3)).astype(np.float32)
+    return _soup(c + off)
+
+
+def gmm_soup(n: int, clusters: int = 64, seed: int = 2, sigma_lo: float = 0.05, sigma_hi: float = 0.8,
+             extent: float = 10.0, vertex_sigma: float = 0.01):
+    """Isotropic Gaussian mixture: means uniform in [0, extent]^3, sigma log-uniform in
+    [sigma_lo, sigma_hi]; each triangle = a centroid drawn from the mixture plus per-vertex
+    N(0, vertex_sigma^2) offsets."""
+    g = _rng(seed)
+    means = g.random((clusters, 3)) * extent
+    sig = np.exp(g.uniform(np.log(sigma_lo), np.log(sigma_hi), clusters))
+    comp = g.integers(0, clusters, n)
+    c = means[comp] + g.normal(0.0, 1.0, (n, 3)) * sig[comp, None]
+    off = g.normal(0.0, vertex_sigma, (n, 3, 3))
+    return _soup((c[:, None, :] + off).astype(np.float32))
+
+
+def ground_grid(cells: int, size: float = 10.0):
+    """cells x cells quads at y = 0 over [0, size]^2, two triangles each."""
+    xs = np.linspace(0.0, size, cells + 1, dtype=np.float64)
+    x0, z0 = np.meshgrid(xs[:-1], xs[:-1], indexing="ij")
+    x1, z1 = np.meshgrid(xs[1:], xs[1:], indexing="ij")
+    x0, z0, x1, z1 = (a.reshape(-1) for a in (x0, z0, x1, z1))
+    y = np.zeros_like(x0)
+    t1 = np.stack([np.stack([x0, y, z0], 1), np.stack([x1, y, z0], 1), np.stack([x1, y, z1], 1)], 1)
+    t2 = np.stack([np.stack([x0, y, z0], 1), np.stack([x1, y, z1], 1), np.stack([x0, y, z1], 1)], 1)
+    return np.concatenate([t1, t2], 0).astype(np.float32)
+
+
+def large_scene(n: int = 4194304, seed: int = 2, grid_cells: int = 724):
+    """Large single scene: a ground grid of grid_cells^2 * 2 triangles (724 -> 1,048,352, about 25%)
+    plus a 64-component mixture filling the rest, 4,194,304 triangles in total."""
+    grid = ground_grid(grid_cells)
+    rest = n - grid.shape[0]
+    g_vert, _ = gmm_soup(rest, 64, seed)
+    vert = np.concatenate([g_vert.reshape(-1, 3, 3), grid], 0)
+    return _soup(vert)
+
+
+def camera_default():
+    """Pinhole at (0.5, 0.5, -1.5) looking +z at (0.5, 0.5, 0), up +y, 60 degree vertical FOV,
+    512 x 512 pixels."""
+    return dict(pos=(0.5, 0.5, -1.5), lookAt=(0.5, 0.5, 0.0), up=(0.0, 1.0, 0.0), fov=60.0, width=512, height=512)
+
+
+def random_rays(n: int, lo, hi, seed: int = 3):
+    """Origins uniform in the box [lo, hi], directions uniform on the unit sphere."""
+    g = _rng(seed)
+    lo = np.asarray(lo, np.float64)
+    hi = np.asarray(hi, np.float64)
+    org = lo + g.random((n, 3)) * (hi - lo)
+    d = g.normal(0.0, 1.0, (n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return org.astype(np.float32), d.astype(np.float32)

@@ -1,0 +1,264 @@
+/*
+ * bvhgb — GB300-native (sm_103a) GPU BVH pipeline behind a plain C ABI.
+ *
+ * Drop-in boundary for BVHTest's GPU path (mensinda/BVHTest): LBVH build (lib/builder/LBVH_CUDA.*),
+ * parallel Bittner13 optimizer (lib/builder/Bittner13CUDA.*), closest-hit tracer
+ * (lib/tracer/CUDAKernels.*) and the transfer helpers (lib/cuda/cudaFN.*). Every entry point
+ * returns a bvhgb_status, takes plain pointers and sizes, and runs stream-ordered on the stream
+ * it is given (NULL = legacy default stream). Device pointers are caller-owned unless a function
+ * says otherwise; workspaces are opaque and owned by the library.
+ *
+ * Layouts of the shared data model are byte-identical to the reference (lib/base/BVH.hpp).
+ */
+#ifndef BVHGB_H
+#define BVHGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define BVHGB_API __attribute__((visibility("default")))
+#else
+#define BVHGB_API
+#endif
+
+typedef void *bvhgb_stream; /* a cudaStream_t */
+
+/* ErrorCode (lib/base/Command.hpp:33-42) keeps its values; 8.. are additions. */
+typedef enum bvhgb_status {
+  BVHGB_OK = 0,
+  BVHGB_WARNING = 1,
+  BVHGB_IO_ERROR = 2,
+  BVHGB_PARSE_ERROR = 3,
+  BVHGB_BVH_ERROR = 4,
+  BVHGB_GL_ERROR = 5, /* never returned: no graphics path */
+  BVHGB_CUDA_ERROR = 6,
+  BVHGB_GENERIC_ERROR = 7,
+  BVHGB_INVALID_ARGUMENT = 8,
+  BVHGB_DEVICE_TIMEOUT = 9, /* a bounded device-side wait gave up; results are not valid */
+  BVHGB_OUT_OF_MEMORY = 10,
+  BVHGB_TOO_LARGE = 11 /* a size above a documented maximum */
+} bvhgb_status;
+
+/* ---- shared data model (lib/base/BVH.hpp) ------------------------------------------------- */
+
+typedef struct bvhgb_vec3 { float x, y, z; } bvhgb_vec3;                  /* glm::vec3 */
+typedef struct bvhgb_triangle { uint32_t v1, v2, v3; } bvhgb_triangle;    /* BVH.hpp:38-42 */
+typedef struct bvhgb_aabb { bvhgb_vec3 minMax[2]; } bvhgb_aabb;           /* BVH.hpp:59-60 */
+
+/* BVHNode (BVH.hpp:113-123), 48 bytes, 16-byte aligned. Inner nodes of an LBVH are
+ * [0, N-1), leaves [N-1, 2N-1); a leaf's left = first face, right = face count. */
+typedef struct bvhgb_node {
+  bvhgb_aabb bbox;
+  uint32_t parent;
+  uint32_t left;
+  uint32_t right;
+  uint16_t isLeafFlag;
+  uint16_t isLeft;
+  uint16_t level;
+  uint16_t pad;
+  float surfaceArea;
+} bvhgb_node;
+
+/* MeshRaw (BVH.hpp:50-57): device-only arrays. */
+typedef struct bvhgb_mesh_raw {
+  bvhgb_vec3 *vert;
+  bvhgb_vec3 *norm;
+  bvhgb_triangle *faces;
+  uint32_t numVert;
+  uint32_t numNorm;
+  uint32_t numFaces;
+} bvhgb_mesh_raw;
+
+/* Device-side image of the reference's BVH class (BVH.hpp:138-144). */
+typedef struct bvhgb_device_bvh {
+  bvhgb_node *bvh;
+  size_t vSize;
+  size_t vCapacity;
+  uint32_t vRootIndex;
+  uint16_t vMaxLevel;
+  uint16_t pad;
+} bvhgb_device_bvh;
+
+/* CUDAMemoryBVHPointer (BVH.hpp:234-238). */
+typedef struct bvhgb_bvh_pointer {
+  bvhgb_device_bvh *bvh;
+  bvhgb_node *nodes;
+  uint32_t numNodes;
+} bvhgb_bvh_pointer;
+
+/* CUDAPixel (lib/tracer/CUDAKernels.hpp:33-37). */
+typedef struct bvhgb_pixel {
+  uint8_t hit;
+  uint8_t diffuse;
+  uint16_t intCount;
+} bvhgb_pixel;
+
+/* Closest hit per ray (an addition: the reference keeps only the shaded pixel). */
+typedef struct bvhgb_hit {
+  uint32_t primId; /* 0xFFFFFFFF = miss */
+  float t;
+} bvhgb_hit;
+
+/* ---- library -------------------------------------------------------------------------------- */
+
+BVHGB_API const char *bvhgb_version(void);
+BVHGB_API const char *bvhgb_status_string(int status);
+/* Last CUDA error text seen by this thread (empty if none). */
+BVHGB_API const char *bvhgb_last_error(void);
+/* Number of kernels this library has launched (process-wide, monotonic). */
+BVHGB_API uint64_t bvhgb_launch_count(void);
+
+/* ---- LBVH build (lib/builder/LBVH_CUDA.hpp:49-59, LBVH.cpp:28-55) ------------------------- */
+
+enum { BVHGB_TOPO_REFCOMPAT = 0, BVHGB_TOPO_KARRAS = 1 };
+
+typedef struct bvhgb_lbvh_config {
+  uint32_t mortonBits; /* 30 (reference) or 63 */
+  uint32_t topology;   /* BVHGB_TOPO_REFCOMPAT: the reference's index-only radix tree (its __clz
+                          keeps the low 32 bits of (morton << 32 | index)); BVHGB_TOPO_KARRAS:
+                          the radix tree of the full (morton, index) keys */
+} bvhgb_lbvh_config;
+
+typedef struct bvhgb_lbvh_workspace bvhgb_lbvh_workspace;
+
+/* LBVH_allocateWorkingMemory (LBVH_CUDA.cu:426-475): device scratch for up to maxFaces. */
+BVHGB_API int bvhgb_lbvh_create(uint32_t maxFaces, const bvhgb_lbvh_config *cfg, bvhgb_lbvh_workspace **out);
+/* LBVH_freeWorkingMemory (LBVH_CUDA.cu:477-488). */
+BVHGB_API int bvhgb_lbvh_destroy(bvhgb_lbvh_workspace *ws);
+/* LBVH::runImpl (LBVH.cpp:41-50): tri boxes + scene box, Morton codes, sort, topology and
+ * refit into nodes[0 .. 2*numFaces-1). vert: float3[*], faces: uint3[numFaces] (device).
+ * Writes nodes[0].parent = 0; inner levels are 0 and leaf levels 255 (fix with
+ * bvhgb_fix_levels_host after copying to the host). */
+BVHGB_API int bvhgb_lbvh_build(bvhgb_lbvh_workspace *ws, const float *vert, const uint32_t *faces,
+                               uint32_t numFaces, bvhgb_node *nodes, bvhgb_stream stream);
+/* The phases of bvhgb_lbvh_build, for tests and the legacy wrappers:
+ * LBVH_initTriData (:98-119) -> scene box kept on the device; LBVH_calcMortonCodes (:168-183);
+ * LBVH_sortMortonCodes (:185-193); LBVH_buildBVHTree + LBVH_fixAABB (:326-385, fused). */
+BVHGB_API int bvhgb_lbvh_init_tri_data(bvhgb_lbvh_workspace *ws, const float *vert, const uint32_t *faces,
+                                       uint32_t numFaces, bvhgb_stream stream);
+BVHGB_API int bvhgb_lbvh_calc_morton(bvhgb_lbvh_workspace *ws, const float *vert, const uint32_t *faces,
+                                     uint32_t numFaces, bvhgb_stream stream);
+BVHGB_API int bvhgb_lbvh_sort(bvhgb_lbvh_workspace *ws, uint32_t numFaces, bvhgb_stream stream);
+BVHGB_API int bvhgb_lbvh_build_tree(bvhgb_lbvh_workspace *ws, const float *vert, const uint32_t *faces,
+                                    uint32_t numFaces, bvhgb_node *nodes, bvhgb_stream stream);
+/* Copies of intermediate device results (synchronous on 'stream'). keys: uint32 (30-bit) or
+ * uint64 (63-bit) per face; sorted = after bvhgb_lbvh_sort. scene: 6 floats. */
+BVHGB_API int bvhgb_lbvh_read_scene_box(bvhgb_lbvh_workspace *ws, bvhgb_aabb *scene, bvhgb_stream stream);
+BVHGB_API int bvhgb_lbvh_read_keys(bvhgb_lbvh_workspace *ws, int sorted, void *keys_host, uint32_t *idx_host,
+                                   uint32_t numFaces, bvhgb_stream stream);
+
+/* ---- radix sort (used by the build and the optimizer; exposed for tests) --------------------- */
+
+/* Stable ascending LSD sort of (key, uint32 value) pairs on bits [beginBit, endBit) of the key.
+ * keyBytes: 4 or 8. temp == NULL: *tempBytes receives the scratch size and nothing runs. */
+BVHGB_API int bvhgb_radix_sort_pairs(void *temp, size_t *tempBytes, const void *keysIn, void *keysOut,
+                                     const uint32_t *valsIn, uint32_t *valsOut, uint32_t n, uint32_t keyBytes,
+                                     uint32_t beginBit, uint32_t endBit, bvhgb_stream stream);
+
+/* ---- SAH (Bittner13CUDA.cu:776-803, BVH.cpp:23-37) ------------------------------------------- */
+
+/* (sum of all node areas except the root) / root area, cInner = cLeaf = 1; deterministic
+ * reduction in double. Synchronous on 'stream'. */
+BVHGB_API int bvhgb_calc_sah(const bvhgb_node *nodes, uint32_t numNodes, uint32_t root, double *sah,
+                             bvhgb_stream stream);
+
+/* ---- Bittner13 optimizer (lib/builder/Bittner13CUDA.hpp:68-83, Bittner13GPU.cpp:78-133) ---- */
+
+typedef struct bvhgb_bn13_config {
+  uint32_t numChunks;    /* numChunks = 32 */
+  uint32_t blockSize;    /* CUDABlockSize = 128 */
+  float batchPercent;    /* batchPercent = 1.0, clamped to [0.01, 75] */
+  uint32_t offsetAccess; /* offsetAccess = false */
+  uint32_t heapCapacity; /* branch-and-bound queue entries per item (reference: 4096) */
+} bvhgb_bn13_config;
+
+typedef struct bvhgb_bn13_stats {
+  uint64_t items;            /* batch items processed */
+  uint64_t applied;          /* reinsertions applied */
+  uint64_t skippedConflict;  /* lost the conflict check (numSkipped in the reference) */
+  uint64_t skippedInvalid;   /* removeNode refused or best position == root */
+  uint64_t heapOverflow;     /* queue pushes dropped at heapCapacity */
+} bvhgb_bn13_stats;
+
+typedef struct bvhgb_bn13_workspace bvhgb_bn13_workspace;
+
+/* allocateMemory + initData (Bittner13CUDA.cu:836-987) for a tree of numNodes nodes. */
+BVHGB_API int bvhgb_bn13_create(const bvhgb_node *nodes, uint32_t numNodes, uint32_t root,
+                                const bvhgb_bn13_config *cfg, bvhgb_bn13_workspace **out, bvhgb_stream stream);
+BVHGB_API int bvhgb_bn13_destroy(bvhgb_bn13_workspace *ws);
+/* bn13_doAlgorithmStep (:768-772): selection + all chunks of one iteration. */
+BVHGB_API int bvhgb_bn13_step(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, bvhgb_stream stream);
+/* maxNumStepps iterations captured once into a CUDA graph and replayed. */
+BVHGB_API int bvhgb_bn13_run(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t iterations, bvhgb_stream stream);
+/* bn13_selectNodes (:659-726) and bn13_rmAndReinsChunk (:729-766). */
+BVHGB_API int bvhgb_bn13_select_nodes(bvhgb_bn13_workspace *ws, const bvhgb_node *nodes, bvhgb_stream stream);
+BVHGB_API int bvhgb_bn13_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t chunk, bvhgb_stream stream);
+/* calcNumSkipped (:806-821) and friends; synchronous on 'stream'. */
+BVHGB_API int bvhgb_bn13_get_stats(bvhgb_bn13_workspace *ws, bvhgb_bn13_stats *stats, bvhgb_stream stream);
+/* Number of items per iteration (numChunks * chunkSize, Bittner13GPU.cpp:90-92). */
+BVHGB_API uint32_t bvhgb_bn13_batch_size(const bvhgb_bn13_workspace *ws);
+
+/* ---- tracer (lib/tracer/CUDAKernels.hpp:39-77, CUDATracer.cpp:86-118) ------------------------ */
+
+typedef struct bvhgb_camera {
+  float pos[3];
+  float lookAt[3];
+  float up[3];
+  float fov; /* vertical, degrees (Camera.hpp:27-32) */
+  uint32_t width;
+  uint32_t height;
+} bvhgb_camera;
+
+typedef struct bvhgb_trace_config {
+  float light[3];       /* lightLocation = (2, 2, 2) (TracerBase.hpp:25) */
+  uint32_t faceCulling; /* CUDA_FACE_CULLING: front faces only */
+  float tmin;           /* hits need t > tmin (0) */
+  float tmax;           /* ... and t <= tmax (+inf) */
+} bvhgb_trace_config;
+
+/* generateRays + tracerImage (CUDAKernels.cu:386-417) fused: one primary ray per pixel,
+ * closest hit, Lambert shade into img[y * width + x]; hits (optional) gets (primId, t). */
+BVHGB_API int bvhgb_trace_image(const bvhgb_node *nodes, uint32_t numNodes, uint32_t root, const float *vert,
+                                const uint32_t *faces, const bvhgb_camera *cam, const bvhgb_trace_config *cfg,
+                                bvhgb_pixel *img, bvhgb_hit *hits, bvhgb_stream stream);
+/* Closest hit for arbitrary rays: org/dir are float3[n] (dir need not be normalised). */
+BVHGB_API int bvhgb_trace_rays(const bvhgb_node *nodes, uint32_t numNodes, uint32_t root, const float *vert,
+                               const uint32_t *faces, const float *org, const float *dir, uint32_t n,
+                               const bvhgb_trace_config *cfg, bvhgb_hit *hits, bvhgb_stream stream);
+
+/* Device-side traversal error bits seen since the last reset (2 = stack overflow, 4 = bad child
+ * index); synchronous. */
+BVHGB_API int bvhgb_trace_read_errors(uint32_t *flags, int reset);
+
+/* ---- transfer (lib/cuda/cudaFN.hpp:27-33) --------------------------------------------------- */
+
+/* copyMeshToGPU (cudaFN.cu:76-109): allocates and fills out->vert/norm/faces. */
+BVHGB_API int bvhgb_copy_mesh_to_gpu(const float *vert, uint32_t numVert, const float *norm, uint32_t numNorm,
+                                     const uint32_t *faces, uint32_t numFaces, bvhgb_mesh_raw *out);
+/* copyMeshToHost (cudaFN.cu:149-182): copies back and frees the device mesh. */
+BVHGB_API int bvhgb_copy_mesh_to_host(bvhgb_mesh_raw *mesh, float *vert, float *norm, uint32_t *faces);
+/* copyBVHToGPU (cudaFN.cu:32-74): numNodes == 0 gives null pointers and succeeds. */
+BVHGB_API int bvhgb_copy_bvh_to_gpu(const bvhgb_node *nodes, uint32_t numNodes, uint32_t root, uint16_t maxLevel,
+                                    bvhgb_bvh_pointer *out);
+/* LBVH_allocateBVH (LBVH_CUDA.cu:396-424): fails when out already holds a BVH. */
+BVHGB_API int bvhgb_allocate_bvh(bvhgb_bvh_pointer *out, uint32_t numFaces);
+/* copyBVHToHost (cudaFN.cu:113-146): copies the nodes (numNodes of them) back, reports root
+ * and max level, and frees the device BVH. */
+BVHGB_API int bvhgb_copy_bvh_to_host(bvhgb_bvh_pointer *ptr, bvhgb_node *nodes, uint32_t capacity, uint32_t *root,
+                                     uint16_t *maxLevel);
+BVHGB_API int bvhgb_free_bvh(bvhgb_bvh_pointer *ptr);
+BVHGB_API int bvhgb_free_mesh(bvhgb_mesh_raw *mesh);
+/* BVH::fixLevels (BVH.cpp:39-70) on a host copy; returns the max level in *maxLevel. */
+BVHGB_API int bvhgb_fix_levels_host(bvhgb_node *nodes, uint32_t numNodes, uint32_t root, uint16_t *maxLevel);
+/* cudaDeviceSynchronize (LBVH_doCUDASyc, doCudaDevSync, tracerDoCudaSync). */
+BVHGB_API int bvhgb_device_sync(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,598 @@
+/*
+ * Oracle (test infrastructure only): Bittner et al. 2013 reinsertion optimizer.
+ *  - orc_bittner_seq:     the sequential CPU optimizer, lib/builder/Bittner13.cpp:71-312.
+ *  - orc_bittner_chunked: the chunked parallel GPU algorithm, lib/builder/Bittner13CUDA.cu:141-772
+ *                         with lib/base/BVHPatch.hpp:87-335, items of a chunk evaluated against
+ *                         the chunk-start tree, conflicts resolved by batch rank.
+ * Parity unpinned: see oracle.h.
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define NNODE 10
+#define P_GRAND_PARENT 0
+#define P_1ST_ROOT 1
+#define P_1ST_BEST 2
+#define P_NODE 3
+#define P_1ST_INSERT 4
+#define P_2ND_ROOT 5
+#define P_2ND_BEST 6
+#define P_2ND_INSERT 7
+#define P_SIBLING 8
+#define P_PARENT 9
+#define NONE 0xFFFFFFFFu
+
+static void merge_into(orc_aabb *a, const orc_aabb *b) {
+  for (int k = 0; k < 3; ++k) {
+    a->mn[k] = a->mn[k] < b->mn[k] ? a->mn[k] : b->mn[k];
+    a->mx[k] = a->mx[k] > b->mx[k] ? a->mx[k] : b->mx[k];
+  }
+}
+
+/* kCalcCost (Bittner13CUDA.cu:480-500): (SA^3 * 2) / ((SA_L + SA_R) * min(SA_L, SA_R)). */
+float orc_inefficiency(const orc_node *nodes, uint32_t i) {
+  const orc_node *nd = &nodes[i];
+  if (nd->isLeafFlag) return 0.0f;
+  float sa = nd->surfaceArea;
+  float l = nodes[nd->left].surfaceArea;
+  float r = nodes[nd->right].surfaceArea;
+  float num = sa * sa;
+  num = num * sa;
+  num = num * 2.0f;
+  float den = l + r;
+  den = den * (l < r ? l : r);
+  return num / den;
+}
+
+/* ---- binary heap with the hole-based sift of the C++ standard library heap algorithms,
+ *      restated from lib/builder/CUDAHeap.hpp:33-112. "less(a, b)" is a.cost > b.cost, so the
+ *      front of the heap holds the smallest cost. ------------------------------------------- */
+typedef struct hitem {
+  uint32_t node;
+  float cost;
+} hitem;
+
+static int hless(const hitem *a, const hitem *b) { return a->cost > b->cost; }
+
+static void sift_up(hitem *h, long hole, long top, hitem v) {
+  long parent = (hole - 1) / 2;
+  while (hole > top && hless(&h[parent], &v)) {
+    h[hole] = h[parent];
+    hole = parent;
+    parent = (hole - 1) / 2;
+  }
+  h[hole] = v;
+}
+
+static void heap_push(hitem *h, long len_after) { sift_up(h, len_after - 1, 0, h[len_after - 1]); }
+
+static void heap_pop(hitem *h, long len) {
+  if (len <= 1) return;
+  long last = len - 1;
+  hitem v = h[last];
+  h[last] = h[0];
+  long n = last, hole = 0, top = 0, second = 0;
+  while (second < (n - 1) / 2) {
+    second = 2 * (second + 1);
+    if (hless(&h[second], &h[second - 1])) second--;
+    h[hole] = h[second];
+    hole = second;
+  }
+  if ((n & 1) == 0 && second == (n - 2) / 2) {
+    second = 2 * (second + 1);
+    h[hole] = h[second - 1];
+    hole = second - 1;
+  }
+  sift_up(h, hole, top, v);
+}
+
+/* ================================ sequential (Bittner13.cpp) ================================ */
+
+/* findNodeForReinsertion (Bittner13.cpp:71-113). */
+static uint32_t seq_find_node(const orc_node *t, uint32_t root, uint32_t n, hitem *pq, uint32_t cap) {
+  float best_cost = INFINITY;
+  uint32_t best = 0;
+  const orc_node *nd = &t[n];
+  float sarea = nd->surfaceArea;
+  long size = 1;
+  pq[0].node = root;
+  pq[0].cost = 0.0f;
+  while (size > 0) {
+    hitem cur = pq[0];
+    const orc_node *cn = &t[cur.node];
+    heap_pop(pq, size);
+    size--;
+    if (cur.cost + sarea >= best_cost) break;
+    orc_aabb m = nd->bbox; /* directCost: node's box merged with the candidate's */
+    merge_into(&m, &cn->bbox);
+    float direct = orc_surface_area(&m);
+    float total = cur.cost + direct;
+    if (total < best_cost) {
+      best_cost = total;
+      best = cur.node;
+    }
+    float induced = total - cn->surfaceArea;
+    if (induced + sarea < best_cost && !cn->isLeafFlag) {
+      if ((uint32_t)size + 2 <= cap) {
+        pq[size].node = cn->left; pq[size].cost = induced;
+        pq[size + 1].node = cn->right; pq[size + 1].cost = induced;
+        heap_push(pq, size + 1);
+        heap_push(pq, size + 2);
+        size += 2;
+      }
+    }
+  }
+  return best;
+}
+
+/* fixTree (Bittner13.cpp:198-220). */
+static void seq_fix_tree(orc_node *t, uint32_t root, uint32_t x) {
+  int last_left = 1;
+  orc_aabb b = t[t[x].left].bbox;
+  for (;;) {
+    uint32_t sib = last_left ? t[x].right : t[x].left;
+    merge_into(&b, &t[sib].bbox);
+    t[x].bbox = b;
+    t[x].surfaceArea = orc_surface_area(&b);
+    if (x == root) return;
+    last_left = t[x].isLeft != 0;
+    x = t[x].parent;
+  }
+}
+
+static uint32_t sibling_of(const orc_node *t, uint32_t x) {
+  const orc_node *p = &t[t[x].parent];
+  return t[x].isLeft ? p->right : p->left;
+}
+
+/* removeNode (Bittner13.cpp:115-158). */
+static int seq_remove(orc_node *t, uint32_t root, uint32_t x, uint32_t ins[2], uint32_t unused[2]) {
+  if (t[x].isLeafFlag || x == root) return 0;
+  uint32_t s = sibling_of(t, x);
+  uint32_t p = t[x].parent;
+  uint32_t g = t[p].parent;
+  float lsa = t[t[x].left].surfaceArea, rsa = t[t[x].right].surfaceArea;
+  if (p == root) return 0;
+  if (t[p].isLeft) {
+    t[g].left = s;
+    t[s].isLeft = 1;
+  } else {
+    t[g].right = s;
+    t[s].isLeft = 0;
+  }
+  t[s].parent = g;
+  seq_fix_tree(t, root, g);
+  if (lsa > rsa) { ins[0] = t[x].left; ins[1] = t[x].right; }
+  else { ins[0] = t[x].right; ins[1] = t[x].left; }
+  unused[0] = x;
+  unused[1] = p;
+  return 1;
+}
+
+/* reinsert (Bittner13.cpp:161-196). */
+static void seq_reinsert(orc_node *t, uint32_t *root, uint32_t x, uint32_t u, hitem *pq, uint32_t cap) {
+  uint32_t best = seq_find_node(t, *root, x, pq, cap);
+  uint32_t r = t[best].parent;
+  if (best == *root) {
+    *root = u;
+    r = u;
+  } else {
+    if (t[best].isLeft) { t[r].left = u; t[u].isLeft = 1; }
+    else { t[r].right = u; t[u].isLeft = 0; }
+  }
+  t[u].parent = r;
+  t[u].left = best;
+  t[u].right = x;
+  t[best].parent = u;
+  t[best].isLeft = 1;
+  t[x].parent = u;
+  t[x].isLeft = 0;
+  seq_fix_tree(t, *root, u);
+}
+
+typedef struct cost_item {
+  float cost;
+  uint32_t idx;
+} cost_item;
+
+static int cmp_cost_desc(const void *a, const void *b) {
+  const cost_item *x = a, *y = b;
+  if (x->cost > y->cost) return -1;
+  if (x->cost < y->cost) return 1;
+  return x->idx < y->idx ? -1 : (x->idx > y->idx);
+}
+
+int orc_bittner_seq(orc_node *t, uint32_t n_nodes, uint32_t *root, uint32_t iters, float batch_percent,
+                    double *sah_trace) {
+  if (batch_percent <= 0.01f) batch_percent = 0.01f;
+  if (batch_percent >= 75.0f) batch_percent = 75.0f;
+  uint32_t k = (uint32_t)((batch_percent / 100.0f) * (float)n_nodes);
+  const uint32_t cap = 16384; /* Bittner13::QUEUE_SIZE */
+  hitem *pq = malloc(sizeof(hitem) * cap);
+  cost_item *todo = malloc(sizeof(cost_item) * n_nodes);
+  if (sah_trace) sah_trace[0] = orc_sah(t, n_nodes, *root);
+  for (uint32_t it = 0; it < iters; ++it) {
+#pragma omp parallel for schedule(static)
+    for (int64_t j = 0; j < (int64_t)n_nodes; ++j) {
+      todo[j].idx = (uint32_t)j;
+      todo[j].cost = orc_inefficiency(t, (uint32_t)j);
+    }
+    /* nth_element + sort of the first k (Bittner13.cpp:282-283); ties broken by index. */
+    qsort(todo, n_nodes, sizeof(cost_item), cmp_cost_desc);
+    for (uint32_t j = 0; j < k && j < n_nodes; ++j) {
+      uint32_t ins[2], un[2];
+      if (!seq_remove(t, *root, todo[j].idx, ins, un)) continue;
+      seq_reinsert(t, root, ins[0], un[0], pq, cap);
+      seq_reinsert(t, root, ins[1], un[1], pq, cap);
+    }
+    if (sah_trace) sah_trace[it + 1] = orc_sah(t, n_nodes, *root);
+  }
+  free(pq);
+  free(todo);
+  return 0;
+}
+
+/* ============================ chunked GPU algorithm (Bittner13CUDA.cu) ========================= */
+
+typedef struct npatch {
+  uint32_t parent, left, right;
+  uint16_t isLeafFlag, isLeft;
+} npatch;
+
+/* BVHPatch (BVHPatch.hpp:87-335), ENABLE_AABB_PATH = 0 variant. */
+typedef struct bpatch {
+  npatch nd[NNODE];
+  uint32_t idx[NNODE];
+  uint32_t apath[4];
+  orc_aabb abox[4];
+  const orc_node *t;
+  uint32_t root;
+} bpatch;
+
+static npatch to_patch(const orc_node *n) {
+  npatch p = {n->parent, n->left, n->right, n->isLeafFlag, n->isLeft};
+  return p;
+}
+static void bp_clear(bpatch *p) {
+  for (int i = 0; i < NNODE; ++i) p->idx[i] = NONE;
+  for (int i = 0; i < 4; ++i) p->apath[i] = NONE;
+}
+static uint32_t bp_index_subset(const bpatch *p, uint32_t x) {
+  if (p->idx[0] == x) return 0;
+  if (p->idx[1] == NONE) return NONE;
+  if (p->idx[1] == x) return 1;
+  if (p->idx[2] == x) return 2;
+  if (p->idx[3] == x) return 3;
+  return NONE;
+}
+static uint32_t bp_index(const bpatch *p, uint32_t x) {
+  for (uint32_t i = 0; i < NNODE; ++i)
+    if (p->idx[i] == x) return i;
+  return NONE;
+}
+static npatch bp_get(const bpatch *p, uint32_t x) {
+  uint32_t i = bp_index(p, x);
+  return i == NONE ? to_patch(&p->t[x]) : p->nd[i];
+}
+static npatch bp_get_subset(const bpatch *p, uint32_t x) {
+  uint32_t i = bp_index_subset(p, x);
+  return i == NONE ? to_patch(&p->t[x]) : p->nd[i];
+}
+static npatch *bp_patch_node(bpatch *p, uint32_t x, uint32_t slot) {
+  p->idx[slot] = x;
+  p->nd[slot] = to_patch(&p->t[x]);
+  return &p->nd[slot];
+}
+static npatch *bp_move(bpatch *p, uint32_t from, uint32_t to) {
+  p->idx[to] = p->idx[from];
+  p->idx[from] = NONE;
+  p->nd[to] = p->nd[from];
+  return &p->nd[to];
+}
+static uint32_t bp_sibling(const bpatch *p, const npatch *n) {
+  npatch par = bp_get(p, n->parent);
+  return n->isLeft == 0 ? par.left : par.right;
+}
+static orc_aabb bp_get_aabb(const bpatch *p, uint32_t x) {
+  for (int i = 0; i < 4; ++i)
+    if (p->apath[i] == x) return p->abox[i];
+  return p->t[x].bbox;
+}
+/* patchAABBFrom (BVHPatch.hpp:293-316): two levels of temporary boxes from x upwards. */
+static void bp_patch_aabb_from(bpatch *p, uint32_t x, uint32_t pidx) {
+  uint32_t ni = x;
+  npatch nd = bp_get_subset(p, ni);
+  orc_aabb b = bp_get_aabb(p, nd.left);
+  int last_left = 1;
+  for (uint32_t i = 0; i < 2; ++i) {
+    uint32_t sib = last_left ? nd.right : nd.left;
+    orc_aabb sb = bp_get_aabb(p, sib);
+    merge_into(&b, &sb);
+    p->abox[pidx * 2 + i] = b;
+    p->apath[pidx * 2 + i] = ni;
+    last_left = nd.isLeft != 0;
+    if (ni == p->root) break;
+    ni = nd.parent;
+    nd = bp_get_subset(p, ni);
+  }
+}
+
+/* findNode1 (Bittner13CUDA.cu:141-191). */
+static uint32_t gpu_find_node(const bpatch *p, uint32_t n, hitem *pq, uint32_t cap, uint64_t *overflow) {
+  float best_cost = INFINITY;
+  uint32_t best = 0;
+  const orc_node *nd = &p->t[n];
+  orc_aabb nbox = nd->bbox;
+  float sarea = nd->surfaceArea;
+  long size = 1;
+  pq[0].node = p->root;
+  pq[0].cost = 0.0f;
+  while (size > 0) {
+    hitem cur = pq[0];
+    if (cur.cost + sarea >= best_cost) break;
+    heap_pop(pq, size);
+    size--;
+    npatch cn = bp_get_subset(p, cur.node);
+    orc_aabb b = bp_get_aabb(p, cur.node);
+    float induced = -1.0f * orc_surface_area(&b);
+    merge_into(&b, &nbox);
+    float direct = orc_surface_area(&b);
+    float total = cur.cost + direct;
+    if (total < best_cost) {
+      best_cost = total;
+      best = cur.node;
+    }
+    induced = induced + total;
+    if (induced + sarea < best_cost && !cn.isLeafFlag) {
+      if ((uint32_t)size + 2 <= cap) {
+        pq[size].node = cn.left; pq[size].cost = induced;
+        pq[size + 1].node = cn.right; pq[size + 1].cost = induced;
+        heap_push(pq, size + 1);
+        heap_push(pq, size + 2);
+        size += 2;
+      } else {
+        (*overflow)++;
+      }
+    }
+  }
+  return best;
+}
+
+/* removeNode (Bittner13CUDA.cu:267-305). out: ins[2], unused[2], grand parent. */
+static int gpu_remove(bpatch *p, uint32_t x, uint32_t ins[2], uint32_t un[2], uint32_t *g_out) {
+  if (p->t[x].isLeafFlag || x == p->root) return 0;
+  npatch *nn = bp_patch_node(p, x, P_NODE);
+  uint32_t s = bp_sibling(p, nn);
+  uint32_t pi = nn->parent;
+  if (pi == p->root) return 0;
+  npatch *sp = bp_patch_node(p, s, P_SIBLING);
+  npatch *pp = bp_patch_node(p, pi, P_PARENT);
+  uint32_t gi = pp->parent;
+  npatch *gp = bp_patch_node(p, gi, P_GRAND_PARENT);
+  if (pp->isLeft) {
+    gp->left = s;
+    sp->isLeft = 1;
+  } else {
+    gp->right = s;
+    sp->isLeft = 0;
+  }
+  sp->parent = gi;
+  bp_patch_aabb_from(p, gi, 0);
+  if (p->t[nn->left].surfaceArea > p->t[nn->right].surfaceArea) { ins[0] = nn->left; ins[1] = nn->right; }
+  else { ins[0] = nn->right; ins[1] = nn->left; }
+  un[0] = x;
+  un[1] = pi;
+  *g_out = gi;
+  return 1;
+}
+
+/* reinsert (Bittner13CUDA.cu:308-358). */
+static int gpu_reinsert(bpatch *p, uint32_t x, uint32_t unused, int update, hitem *pq, uint32_t cap,
+                        uint64_t *overflow) {
+  uint32_t best = gpu_find_node(p, x, pq, cap, overflow);
+  if (best == p->root) return 0;
+  uint32_t bpi = bp_index(p, best);
+  npatch *b;
+  if (bpi == NONE) b = bp_patch_node(p, best, update ? P_1ST_BEST : P_2ND_BEST);
+  else if (bpi == P_GRAND_PARENT) b = &p->nd[P_GRAND_PARENT];
+  else b = bp_move(p, bpi, update ? P_1ST_BEST : P_2ND_BEST);
+  npatch *nn = bp_patch_node(p, x, update ? P_1ST_INSERT : P_2ND_INSERT);
+  npatch *u = &p->nd[update ? P_NODE : P_PARENT];
+  uint32_t ri = b->parent;
+  uint32_t rpi = bp_index(p, ri);
+  npatch *r = rpi == NONE ? bp_patch_node(p, ri, update ? P_1ST_ROOT : P_2ND_ROOT)
+                          : bp_move(p, rpi, update ? P_1ST_ROOT : P_2ND_ROOT);
+  if (b->isLeft) {
+    r->left = unused;
+    u->isLeft = 1;
+  } else {
+    r->right = unused;
+    u->isLeft = 0;
+  }
+  u->parent = ri;
+  u->left = best;
+  u->right = x;
+  b->parent = unused;
+  b->isLeft = 1;
+  nn->parent = unused;
+  nn->isLeft = 0;
+  if (update) bp_patch_aabb_from(p, unused, 1);
+  return 1;
+}
+
+static int cmp_u32(const void *a, const void *b) {
+  uint32_t x = *(const uint32_t *)a, y = *(const uint32_t *)b;
+  return x < y ? -1 : x > y;
+}
+
+typedef struct dnode {
+  uint32_t depth, idx;
+} dnode;
+static int cmp_depth_desc(const void *a, const void *b) {
+  const dnode *x = a, *y = b;
+  if (x->depth != y->depth) return x->depth > y->depth ? -1 : 1;
+  return x->idx < y->idx ? -1 : (x->idx > y->idx);
+}
+
+/* kFixTree3_1/3_2 (Bittner13CUDA.cu:407-467): refit every node on a path from a fix node to
+ * the root, children first. Same boxes as the full refit of kFixTree1. */
+static void refit_paths(orc_node *t, uint32_t root, const uint32_t *fix, uint32_t nfix, uint8_t *mark,
+                        dnode *buf) {
+  uint32_t nd = 0;
+  for (uint32_t i = 0; i < nfix; ++i) {
+    uint32_t x = fix[i];
+    if (x == NONE) continue;
+    for (;;) {
+      if (mark[x]) break;
+      mark[x] = 1;
+      buf[nd].idx = x;
+      buf[nd].depth = 0;
+      nd++;
+      if (x == root || t[x].parent == x) break;
+      x = t[x].parent;
+    }
+  }
+  for (uint32_t i = 0; i < nd; ++i) {
+    uint32_t x = buf[i].idx, d = 0;
+    while (x != root && t[x].parent != x) { x = t[x].parent; d++; }
+    buf[i].depth = d;
+  }
+  qsort(buf, nd, sizeof(dnode), cmp_depth_desc);
+  for (uint32_t i = 0; i < nd; ++i) {
+    orc_node *x = &t[buf[i].idx];
+    mark[buf[i].idx] = 0;
+    if (x->isLeafFlag) continue;
+    orc_aabb b = t[x->left].bbox;
+    merge_into(&b, &t[x->right].bbox);
+    x->bbox = b;
+    x->surfaceArea = orc_surface_area(&b);
+  }
+}
+
+int orc_bittner_chunked(orc_node *t, uint32_t n_nodes, uint32_t root, uint32_t iters,
+                        const orc_bn13_cfg *cfg, double *sah_trace, orc_bn13_stats *stats) {
+  float bp = cfg->batch_percent;
+  if (bp <= 0.01f) bp = 0.01f;
+  if (bp >= 75.0f) bp = 75.0f;
+  uint32_t numc = cfg->num_chunks ? cfg->num_chunks : 1;
+  uint32_t lnum = (uint32_t)((bp / 100.0f) * (float)n_nodes);
+  uint32_t csize = lnum / numc;
+  uint32_t cap = cfg->heap_cap ? cfg->heap_cap : 4096;
+  orc_bn13_stats st;
+  memset(&st, 0, sizeof(st));
+
+  /* initData (Bittner13CUDA.cu:939-987): the inner-node list in ascending index order. */
+  uint32_t n_inner = 0;
+  for (uint32_t i = 0; i < n_nodes; ++i) n_inner += t[i].isLeafFlag == 0;
+  uint32_t *inner = malloc(sizeof(uint32_t) * (n_inner ? n_inner : 1));
+  for (uint32_t i = 0, j = 0; i < n_nodes; ++i) if (!t[i].isLeafFlag) inner[j++] = i;
+
+  cost_item *todo = malloc(sizeof(cost_item) * (n_inner ? n_inner : 1));
+  bpatch *patches = malloc(sizeof(bpatch) * (csize ? csize : 1));
+  uint8_t *valid = malloc(csize ? csize : 1);
+  uint32_t *fix = malloc(sizeof(uint32_t) * 3 * (csize ? csize : 1));
+  uint32_t *owner = malloc(sizeof(uint32_t) * n_nodes);
+  uint8_t *mark = calloc(n_nodes, 1);
+  dnode *dbuf = malloc(sizeof(dnode) * n_nodes);
+  for (uint32_t i = 0; i < n_nodes; ++i) owner[i] = NONE;
+  uint32_t nthreads = (uint32_t)orc_num_threads();
+  hitem *pqs = malloc(sizeof(hitem) * cap * nthreads);
+  uint64_t *ovf = calloc(nthreads, sizeof(uint64_t));
+
+  if (sah_trace) sah_trace[0] = orc_sah(t, n_nodes, root);
+  for (uint32_t it = 0; it < iters; ++it) {
+    /* bn13_selectNodes (:659-726): kCalcCost + stable descending sort of (cost, node). */
+    for (uint32_t j = 0; j < n_inner; ++j) {
+      todo[j].idx = inner[j];
+      todo[j].cost = orc_inefficiency(t, inner[j]);
+    }
+    qsort(todo, n_inner, sizeof(cost_item), cmp_cost_desc);
+
+    for (uint32_t c = 0; c < numc; ++c) {
+      /* kRemoveAndReinsert (:504-564) against the chunk-start tree. */
+#pragma omp parallel for schedule(dynamic, 4)
+      for (int64_t kk = 0; kk < (int64_t)csize; ++kk) {
+        uint32_t k = (uint32_t)kk;
+#ifdef _OPENMP
+        int tid = omp_get_thread_num();
+#else
+        int tid = 0;
+#endif
+        hitem *pq = pqs + (size_t)cap * tid;
+        uint32_t pos = cfg->offset_access ? k * numc + c : c * csize + k;
+        uint32_t node = pos < n_inner ? todo[pos].idx : NONE;
+        bpatch *p = &patches[k];
+        p->t = t;
+        p->root = root;
+        bp_clear(p);
+        valid[k] = 0;
+        fix[3 * k] = fix[3 * k + 1] = fix[3 * k + 2] = NONE;
+        if (node == NONE) continue;
+        uint32_t ins[2], un[2], g;
+        if (!gpu_remove(p, node, ins, un, &g)) continue;
+        if (!gpu_reinsert(p, ins[0], un[0], 1, pq, cap, &ovf[tid])) continue;
+        if (!gpu_reinsert(p, ins[1], un[1], 0, pq, cap, &ovf[tid])) continue;
+        valid[k] = 1;
+        fix[3 * k] = g;
+        fix[3 * k + 1] = un[0];
+        fix[3 * k + 2] = un[1];
+      }
+      /* Conflict rule: claim every patched node with the item's rank; lowest rank wins. */
+      for (uint32_t k = 0; k < csize; ++k) {
+        if (!valid[k]) continue;
+        for (int s = 0; s < NNODE; ++s) {
+          uint32_t x = patches[k].idx[s];
+          if (x != NONE && k < owner[x]) owner[x] = k;
+        }
+      }
+      uint32_t nwin = 0;
+      for (uint32_t k = 0; k < csize; ++k) {
+        st.items++;
+        if (!valid[k]) { st.skipped_invalid++; continue; }
+        int ok = 1;
+        for (int s = 0; s < NNODE; ++s) {
+          uint32_t x = patches[k].idx[s];
+          if (x != NONE && owner[x] != k) ok = 0;
+        }
+        if (!ok) {
+          st.skipped_conflict++;
+          valid[k] = 0;
+          fix[3 * k] = fix[3 * k + 1] = fix[3 * k + 2] = NONE;
+          continue;
+        }
+        nwin++;
+      }
+      /* kApplyPatches (:612-627) for the winners, then release every claim. */
+      for (uint32_t k = 0; k < csize; ++k) {
+        for (int s = 0; s < NNODE; ++s) {
+          uint32_t x = patches[k].idx[s];
+          if (x == NONE) continue;
+          if (valid[k]) {
+            t[x].parent = patches[k].nd[s].parent;
+            t[x].left = patches[k].nd[s].left;
+            t[x].right = patches[k].nd[s].right;
+            t[x].isLeft = patches[k].nd[s].isLeft;
+          }
+        }
+      }
+      for (uint32_t k = 0; k < csize; ++k)
+        for (int s = 0; s < NNODE; ++s)
+          if (patches[k].idx[s] != NONE) owner[patches[k].idx[s]] = NONE;
+      st.applied += nwin;
+      refit_paths(t, root, fix, 3 * csize, mark, dbuf);
+    }
+    if (sah_trace) sah_trace[it + 1] = orc_sah(t, n_nodes, root);
+  }
+  for (uint32_t i = 0; i < nthreads; ++i) st.heap_overflow += ovf[i];
+  if (stats) *stats = st;
+  free(inner); free(todo); free(patches); free(valid); free(fix); free(owner); free(mark);
+  free(dbuf); free(pqs); free(ovf);
+  (void)cmp_u32;
+  return 0;
+}

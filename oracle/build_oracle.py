@@ -1,0 +1,39 @@
+"""Build recipe for the CPU oracle (test infrastructure only): gcc -> oracle/_build/liborc.so.
+
+-ffp-contract=off keeps every a*b+c as two rounded operations on both x86-64 and aarch64, which
+is the convention the GPU kernels follow with explicit __fmul_rn/__fadd_rn.
+"""
+from __future__ import annotations
+
+import hashlib
+import subprocess
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+OUT = HERE / "_build"
+SOURCES = ["lbvh.c", "bittner.c", "tracer.c"]
+FLAGS = ["-O2", "-std=gnu11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
+         "-Wall", "-Wno-unused-function"]
+
+
+def build(force: bool = False) -> Path:
+    OUT.mkdir(exist_ok=True)
+    lib = OUT / "liborc.so"
+    h = hashlib.sha256()
+    for s in SOURCES + ["oracle.h"]:
+        h.update((HERE / s).read_bytes())
+    h.update(" ".join(FLAGS).encode())
+    stamp = OUT / "stamp"
+    if not force and lib.exists() and stamp.exists() and stamp.read_text() == h.hexdigest():
+        return lib
+    cmd = ["gcc", *FLAGS, *[str(HERE / s) for s in SOURCES], "-o", str(lib) + ".tmp", "-lm"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + res.stdout + res.stderr)
+    Path(str(lib) + ".tmp").replace(lib)
+    stamp.write_text(h.hexdigest())
+    return lib
+
+
+if __name__ == "__main__":
+    print(build(force=True))

@@ -1,0 +1,67 @@
+"""CPU checks of the C ABI: the library loads and exports every symbol include/*.h declares;
+struct layouts match the reference's (lib/base/BVH.hpp). No compute calls (no GPU here)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _declared():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = h.read_text()
+        names |= set(re.findall(r"BVHGB_API\s+[\w\s\*]+?\b(bvhgb_\w+)\s*\(", text))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    from bvhtest_gb300 import native
+    lib = native.load()
+    declared = _declared()
+    assert len(declared) > 30
+    missing = [n for n in sorted(declared) if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(native.PROTOS) <= declared | {"bvhgb_trace_read_errors"}
+
+
+def test_version_and_status_strings():
+    from bvhtest_gb300 import native
+    lib = native.load()
+    assert b"sm_103a" in lib.bvhgb_version()
+    assert lib.bvhgb_status_string(6) == b"CUDA_ERROR"
+    assert lib.bvhgb_status_string(9) == b"DEVICE_TIMEOUT"
+
+
+def test_argument_errors_without_gpu():
+    """Invalid arguments are rejected on the host before any CUDA call."""
+    from bvhtest_gb300 import native
+    lib = native.load()
+    assert lib.bvhgb_lbvh_create(10, None, None) == 8
+    cfg = native.LbvhConfig(31, 0)
+    ws = C.c_void_p()
+    assert lib.bvhgb_lbvh_create(10, C.byref(cfg), C.byref(ws)) == 8
+    cfg = native.LbvhConfig(30, 0)
+    assert lib.bvhgb_lbvh_create(1 << 30, C.byref(cfg), C.byref(ws)) == 11
+    need = C.c_size_t(0)
+    assert lib.bvhgb_radix_sort_pairs(None, C.byref(need), None, None, None, None, 10, 3, 0, 8, None) == 8
+    assert lib.bvhgb_trace_rays(None, 0, 0, None, None, None, None, 0, None, None, None) == 8
+    assert lib.bvhgb_bn13_create(None, 0, 0, None, None, None) == 8
+
+
+def test_struct_layouts():
+    from bvhtest_gb300 import native
+    assert native.NODE_DTYPE.itemsize == 48
+    assert C.sizeof(native.Camera) == 48
+    assert C.sizeof(native.MeshRaw) == 40
+    assert C.sizeof(native.BvhPointer) == 24
+    assert native.PIXEL_DTYPE.itemsize == 4
+
+
+@pytest.mark.parametrize("field,off", [("parent", 24), ("left", 28), ("right", 32), ("isLeafFlag", 36),
+                                       ("isLeft", 38), ("level", 40), ("surfaceArea", 44)])
+def test_node_offsets(field, off):
+    from bvhtest_gb300 import native
+    assert native.NODE_DTYPE.fields[field][1] == off
