@@ -1,0 +1,369 @@
+#!/usr/bin/env python
+"""Benchmark of the GPU BVH pipeline on one GB300: LBVH build -> Bittner13 optimizer -> closest hit.
+
+Workload (the large single scene): 4,194,304 fp32 triangles (a 64-component Gaussian mixture plus a
+724 x 724 two-triangle-per-cell ground grid, seeded), 63-bit Morton codes, LBVH (karras topology),
+200 parallel Bittner13 iterations at 1%, then 1920 x 1080 primary rays plus one cosine-weighted
+diffuse bounce per hit. Synthetic inputs stand in for the reference's mesh files.
+
+One step = build + optimize + trace. `value` is the build + optimize time in ms (inputs already in
+HBM); `e2e` is the same metric through the C ABI with the mesh copied from pinned host memory
+and the optimised node array copied back inside the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload large|small]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "build+optimize ms at equal SAH (learned vs plain); Mrays/s closest-hit; HBM GB/s"
+NODE_BYTES = 48
+
+
+def workload(name: str):
+    from bvhtest_gb300 import scenes
+    if name == "large":
+        vert, faces = scenes.large_scene()
+        return dict(name="large", vert=vert, faces=faces, bits=63, topo="karras", iters=200,
+                    camera=dict(pos=(5.0, 4.0, -9.0), lookAt=(5.0, 2.0, 5.0), up=(0.0, 1.0, 0.0), fov=60.0,
+                                width=1920, height=1080),
+                    desc=("large single scene: 4,194,304 triangles (64-component Gaussian mixture + 724x724 "
+                          "ground grid), 63-bit Morton, karras LBVH, 200 Bittner13 iterations at 1% (32 chunks), "
+                          "1920x1080 primary rays + 1 cosine-weighted bounce per hit"))
+    vert, faces = scenes.uniform_soup(65536, seed=1)
+    return dict(name="small", vert=vert, faces=faces, bits=30, topo="refCompat", iters=100,
+                camera=scenes.camera_default(),
+                desc=("plain small scene: 65,536 triangles, 30-bit Morton, refCompat LBVH, 100 Bittner13 "
+                      "iterations at 1%, 512x512 primary rays + 1 bounce"))
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (read-only queries)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            parts = [p.strip() for p in l.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() in ("active", "1"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(gpus: int):
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------------------------
+# CPU baseline: the oracle restatement of the reference's CPU paths on the host cores
+# ---------------------------------------------------------------------------------------------
+
+def cpu_sample(w, bittner_sample_iters=1, rays_sample=65536):
+    from oracle import pyoracle as orc
+    vert, faces = w["vert"], w["faces"]
+    t0 = time.perf_counter()
+    nodes, _, _ = orc.lbvh_build(vert, faces, w["bits"], 1 if w["topo"] == "karras" else 0)
+    build_ms = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    opt, root, _ = orc.bittner_seq(nodes, bittner_sample_iters)
+    bn_ms = (time.perf_counter() - t0) * 1e3
+    cam = w["camera"]
+    org, dirs = orc.camera_rays(cam["pos"], cam["lookAt"], cam["up"], cam["fov"], cam["width"], cam["height"])
+    sel = np.linspace(0, org.shape[0] - 1, rays_sample).astype(np.int64)
+    t0 = time.perf_counter()
+    orc.trace_cpu_reference(org[sel], dirs[sel], opt, vert, faces, root=root)
+    tr_s = time.perf_counter() - t0
+    value = build_ms + bn_ms * (w["iters"] / bittner_sample_iters)
+    return dict(value=value, build_ms=build_ms, bittner_ms_per_iter=bn_ms / bittner_sample_iters,
+                trace_mrays_per_s=rays_sample / tr_s / 1e6, cores=orc.num_threads(),
+                sample=(f"full CPU LBVH build + {bittner_sample_iters} sequential Bittner13 iteration(s) "
+                        f"scaled to {w['iters']}; stackless CPU tracer on {rays_sample} of the primary rays"))
+
+
+def run_reference(args, w, rank, world):
+    """--impl reference: the oracle port of the reference's CPU builder/optimizer on all host cores."""
+    if rank != 0:
+        return
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(w, bittner_sample_iters=1, rays_sample=16384)
+        if i >= args.warmup:
+            vals.append(r["value"])
+    v = statistics.mean(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": "ms", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(v, 3), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": w["desc"], "triangles": int(w["faces"].shape[0])},
+            "cpu_baseline": {"value": round(v, 3), "unit": "ms", "cores": r["cores"], "kind": "port",
+                             "sample": r["sample"]},
+            "e2e": {"value": round(v, 3), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------------------------
+
+def run_ours(args, w, rank, world, local):
+    import torch
+    from bvhtest_gb300 import api, native
+
+    lib = native.load()
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream()
+    vert_h, faces_h = w["vert"], w["faces"]
+    n = int(faces_h.shape[0])
+    n_nodes = 2 * n - 1
+    vert = torch.from_numpy(vert_h).to(dev)
+    faces = torch.from_numpy(faces_h.view(np.int32)).to(dev)
+    nodes = api.empty_nodes(n_nodes)
+    lbvh = api.LBVH(n, w["bits"], w["topo"])
+    lbvh.build(vert, faces, nodes)
+    torch.cuda.synchronize()
+    opt = api.Bittner13GPU(nodes, num_nodes=n_nodes, profile=True)
+    cam = w["camera"]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+
+    def ev():
+        e = torch.cuda.Event(enable_timing=True)
+        e.record(stream)
+        return e
+
+    def step():
+        marks = [ev()]
+        lbvh.init_tri_data(vert, faces)
+        marks.append(ev())
+        lbvh.calc_morton(vert, faces)
+        marks.append(ev())
+        lbvh.sort(n)
+        marks.append(ev())
+        lbvh.build_tree(vert, faces, nodes)
+        marks.append(ev())
+        opt.run(w["iters"])
+        marks.append(ev())
+        img, hits = api.trace_image(nodes, vert, faces, cam, num_nodes=n_nodes)
+        bounce, _, _ = api.trace_bounce(nodes, vert, faces, cam, hits, seed=17, num_nodes=n_nodes)
+        marks.append(ev())
+        return marks, hits, bounce
+
+    launches0 = lib.bvhgb_launch_count()
+    for _ in range(args.warmup):
+        flush.fill_(1)
+        step()
+    torch.cuda.synchronize()
+    st0 = opt.stats()
+    phases = {"bounds": [], "morton": [], "sort": [], "topology_refit": [], "optimize": [], "trace": []}
+    step_ms, hits_n = [], []
+    c0 = lib.bvhgb_launch_count()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            barrier(world)
+            marks, hits, bounce = step()
+            torch.cuda.synchronize()
+            t = [marks[i].elapsed_time(marks[i + 1]) for i in range(len(marks) - 1)]
+            for k, v in zip(phases, t):
+                phases[k].append(v)
+            step_ms.append(marks[0].elapsed_time(marks[-1]))
+            h = api.hits_to_numpy(hits)
+            b = api.hits_to_numpy(bounce)
+            hits_n.append((h.shape[0], int((h["prim"] != 0xFFFFFFFF).sum()), int((b["prim"] != 0xFFFFFFFF).sum())))
+    c1 = lib.bvhgb_launch_count()
+    st1 = opt.stats()
+    search_ms, search_launches = opt.search_time()
+    sah = api.calc_sah(nodes, 0, n_nodes)
+    mean = {k: statistics.mean(v) for k, v in phases.items()}
+    build_ms = mean["bounds"] + mean["morton"] + mean["sort"] + mean["topology_refit"]
+    value = allmax(build_ms + mean["optimize"], world)
+    ms_step = allmax(statistics.mean(step_ms), world)
+    rays = hits_n[-1][0] + hits_n[-1][1]  # primary rays + one bounce per primary hit
+    mrays = rays / (mean["trace"] * 1e-3) / 1e6
+    launches = (c1 - c0) + opt.launches_per_iteration * w["iters"] * args.steps
+    gpu_launches = int(launches / args.steps)
+
+    # Build-phase algorithmic bytes per triangle (key bytes K, value bytes 4, P digit passes).
+    K = 8 if w["bits"] == 63 else 4
+    P = (w["bits"] + 7) // 8
+    alg = {"bounds": 48 * n, "morton": 48 * n + (K + 4) * n + 4 * n, "sort": K * n + P * 2 * (K + 4) * n,
+           "topology_refit": 4 * n + 48 * n + (K * n if w["topo"] == "karras" else 0) + NODE_BYTES * n_nodes
+           + 24 * (n - 1) + 8 * (n - 1)}
+    peak, peak_kind = measured_peaks()
+    build_bytes = sum(alg.values())
+    build_gbs = build_bytes / (build_ms * 1e-3) / 1e9
+    # Dominant kernel: the reinsertion search (bn13 patch), timed with CUDA events in the graph.
+    visits = st1["nodesVisited"] - st0["nodesVisited"]
+    launches_search = args.steps * w["iters"] * max(1, search_launches)
+    per_launch_bytes = visits * NODE_BYTES / launches_search
+    per_launch_ms = search_ms / max(1, search_launches)
+    ach = per_launch_bytes / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else 0.0
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get(w["name"], {}).get("bn13_patch")
+    clocks = clk.summary()
+    if rank != 0:
+        return
+    cpu = cpu_sample(w)
+
+    # e2e through the C ABI: pinned host mesh -> device, build, optimize, node array -> pinned host.
+    vh = torch.from_numpy(vert_h).pin_memory()
+    fh = torch.from_numpy(faces_h.view(np.int32)).pin_memory()
+    nh = torch.empty((n_nodes, 12), dtype=torch.int32).pin_memory()
+    vd = torch.empty_like(vert)
+    fd = torch.empty_like(faces)
+    e2e = []
+    for i in range(args.warmup + args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        e0 = ev()
+        vd.copy_(vh, non_blocking=True)
+        fd.copy_(fh, non_blocking=True)
+        lbvh.build(vd, fd, nodes)
+        opt.run(w["iters"])
+        nh.copy_(nodes[:n_nodes], non_blocking=True)
+        e1 = ev()
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e.append(e0.elapsed_time(e1))
+    e2e_ms = statistics.mean(e2e)
+
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": w["desc"], "triangles": n, "nodes": n_nodes, "iterations": w["iters"],
+                   "batch_per_iteration": opt.batch_size, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "256 MB buffer written between steps; inputs (201 MB) and nodes (403 MB) exceed L2"},
+        "build_ms": round(build_ms, 3), "optimize_ms": round(mean["optimize"], 3),
+        "optimize_ms_per_iteration": round(mean["optimize"] / w["iters"], 4),
+        "trace_ms": round(mean["trace"], 3), "mrays_per_s": round(mrays, 1), "rays_per_step": rays,
+        "build_phase_ms": {k: round(mean[k], 4) for k in alg},
+        "build_hbm_gbs": round(build_gbs, 1),
+        "build_roofline": {"bound": "hbm", "achieved": round(build_gbs, 1), "peak": peak, "unit": "GB/s",
+                           "frac": round(build_gbs / peak, 4), "peak_kind": peak_kind,
+                           "bytes_per_triangle": round(build_bytes / n, 1)},
+        "sah": round(sah, 4),
+        "bittner": {"applied": st1["applied"] - st0["applied"], "items": st1["items"] - st0["items"],
+                    "skipped_conflict": st1["skippedConflict"] - st0["skippedConflict"],
+                    "heap_overflow": st1["heapOverflow"] - st0["heapOverflow"]},
+        "roofline": {"kernel": "bn13 patch (reinsertion search)", "bound": "hbm", "achieved": round(ach, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 5), "traffic": traffic,
+                     "peak_kind": peak_kind, "ms_per_launch": round(per_launch_ms, 4),
+                     "algorithmic_bytes_per_launch": int(per_launch_bytes)},
+        "cpu_baseline": {"value": round(cpu["value"], 1), "unit": "ms", "cores": cpu["cores"], "kind": "port",
+                         "sample": cpu["sample"], "trace_mrays_per_s": round(cpu["trace_mrays_per_s"], 3)},
+        "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": int(vert_h.nbytes + faces_h.nbytes),
+                "d2h_bytes_per_step": int(n_nodes * NODE_BYTES)},
+        "gpu_launches": gpu_launches,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["large", "small"], default="large")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = dist_setup(args.gpus)
+    w = workload(args.workload)
+    if args.impl == "reference":
+        run_reference(args, w, rank, world)
+    else:
+        run_ours(args, w, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -139,9 +139,9 @@ class Bittner13GPU:
     """The `bittner13GPU` command (lib/builder/Bittner13GPU.cpp:78-133)."""
 
     def __init__(self, nodes: torch.Tensor, root: int = 0, num_chunks=32, block_size=128, batch_percent=1.0,
-                 offset_access=False, heap_capacity=4096, num_nodes=None, stream=None):
+                 offset_access=False, heap_capacity=4096, num_nodes=None, profile=False, stream=None):
         self.lib = load()
-        self.cfg = Bn13Config(num_chunks, block_size, batch_percent, int(offset_access), heap_capacity)
+        self.cfg = Bn13Config(num_chunks, block_size, batch_percent, int(offset_access), heap_capacity, int(profile))
         ws = C.c_void_p()
         n = nodes.shape[0] if num_nodes is None else num_nodes
         check(self.lib.bvhgb_bn13_create(_ptr(nodes), n, root, C.byref(self.cfg), C.byref(ws), _stream(stream)),
@@ -163,6 +163,17 @@ class Bittner13GPU:
     @property
     def batch_size(self) -> int:
         return self.lib.bvhgb_bn13_batch_size(self.ws)
+
+    @property
+    def launches_per_iteration(self) -> int:
+        return self.lib.bvhgb_bn13_launches_per_iteration(self.ws)
+
+    def search_time(self):
+        """(ms, launches) of the reinsertion-search kernel in the last iteration (profile=True)."""
+        ms = C.c_float()
+        n = C.c_uint32()
+        check(self.lib.bvhgb_bn13_search_time(self.ws, C.byref(ms), C.byref(n)), "bvhgb_bn13_search_time")
+        return ms.value, n.value
 
     def step(self, stream=None):
         check(self.lib.bvhgb_bn13_step(self.ws, _ptr(self.nodes), _stream(stream)), "bvhgb_bn13_step")
@@ -208,6 +219,22 @@ def trace_rays(nodes, vert, faces, org, dirs, root=0, tmin=0.0, tmax=float("inf"
     check(load().bvhgb_trace_rays(_ptr(nodes), n, root, _ptr(vert), _ptr(faces), _ptr(o), _ptr(d), o.shape[0],
                                   C.byref(cfg), _ptr(hits), _stream(stream)), "bvhgb_trace_rays")
     return hits
+
+
+def trace_bounce(nodes, vert, faces, camera: dict, primary_hits, seed=1, offset=1e-4, root=0, with_rays=False,
+                 num_nodes=None, stream=None):
+    """One cosine-weighted bounce per primary hit; returns (hits int64 [h*w], org, dir | None)."""
+    cam = make_camera(**camera)
+    cfg = make_trace_config()
+    npx = cam.width * cam.height
+    out = torch.empty(npx, dtype=torch.int64, device="cuda")
+    org = torch.empty((npx, 3), dtype=torch.float32, device="cuda") if with_rays else None
+    dirs = torch.empty((npx, 3), dtype=torch.float32, device="cuda") if with_rays else None
+    n = nodes.shape[0] if num_nodes is None else num_nodes
+    check(load().bvhgb_trace_bounce(_ptr(nodes), n, root, _ptr(vert), _ptr(faces), C.byref(cam), C.byref(cfg), seed,
+                                    offset, _ptr(primary_hits), _ptr(out), _ptr(org), _ptr(dirs), _stream(stream)),
+          "bvhgb_trace_bounce")
+    return out, org, dirs
 
 
 def trace_errors(reset=True) -> int:

@@ -28,7 +28,12 @@ enum : uint32_t {
   P_GRAND_PARENT = 0, P_1ST_ROOT = 1, P_1ST_BEST = 2, P_NODE = 3, P_1ST_INSERT = 4,
   P_2ND_ROOT = 5, P_2ND_BEST = 6, P_2ND_INSERT = 7, P_SIBLING = 8, P_PARENT = 9
 };
-enum StatIdx { S_ITEMS = 0, S_APPLIED = 1, S_CONFLICT = 2, S_INVALID = 3, S_OVERFLOW = 4, S_COUNT = 5 };
+enum StatIdx { S_ITEMS = 0, S_APPLIED = 1, S_CONFLICT = 2, S_INVALID = 3, S_OVERFLOW = 4, S_VISITS = 5, S_COUNT = 6 };
+
+struct SearchCounters {
+  uint32_t overflow;  // queue pushes dropped at capacity
+  uint32_t visits;    // nodes evaluated by the branch and bound
+};
 
 struct NodeP {
   uint32_t parent, left, right;
@@ -181,7 +186,7 @@ __device__ __forceinline__ void heap_pop(HeapItem *h, long len) {
 }
 
 // findNode1 (Bittner13CUDA.cu:141-191).
-__device__ uint32_t find_node(const Patch &p, uint32_t n, HeapItem *pq, uint32_t cap, uint32_t &overflow) {
+__device__ uint32_t find_node(const Patch &p, uint32_t n, HeapItem *pq, uint32_t cap, SearchCounters &ctr) {
   float best_cost = __int_as_float(0x7f800000);
   uint32_t best = 0;
   const Box nbox = tree_box(p.t, n);
@@ -194,6 +199,7 @@ __device__ uint32_t find_node(const Patch &p, uint32_t n, HeapItem *pq, uint32_t
     if (fadd(cur.cost, sarea) >= best_cost) break;
     heap_pop(pq, size);
     size--;
+    ctr.visits++;
     const NodeP cn = p.get_subset(cur.node);
     Box b = p.get_aabb(cur.node);
     float induced = fmul(-1.0f, surface_area(b));
@@ -215,7 +221,7 @@ __device__ uint32_t find_node(const Patch &p, uint32_t n, HeapItem *pq, uint32_t
         heap_push(pq, size + 2);
         size += 2;
       } else {
-        overflow++;
+        ctr.overflow++;
       }
     }
   }
@@ -253,8 +259,8 @@ __device__ bool remove_node(Patch &p, uint32_t x, uint32_t ins[2], uint32_t un[2
 
 // reinsert (Bittner13CUDA.cu:308-358).
 __device__ bool reinsert(Patch &p, uint32_t x, uint32_t unused, bool update, HeapItem *pq, uint32_t cap,
-                         uint32_t &overflow) {
-  const uint32_t best = find_node(p, x, pq, cap, overflow);
+                         SearchCounters &ctr) {
+  const uint32_t best = find_node(p, x, pq, cap, ctr);
   if (best == p.root) return false;
   const uint32_t bpi = p.index(best);
   uint32_t sb;
@@ -319,14 +325,14 @@ __global__ void patch_kernel(const bvhgb_node *__restrict__ t, uint32_t root, co
   p.t = t;
   p.root = root;
   p.clear();
-  uint32_t overflow = 0;
+  SearchCounters ctr = {0u, 0u};
   uint32_t ins[2], un[2], g = kNone;
   bool ok = pos < numTodo;
   const uint32_t node = ok ? __ldg(todo + pos) : kNone;
   HeapItem *pq = heaps + (size_t)k * cap;
   ok = ok && remove_node(p, node, ins, un, g);
-  ok = ok && reinsert(p, ins[0], un[0], true, pq, cap, overflow);
-  ok = ok && reinsert(p, ins[1], un[1], false, pq, cap, overflow);
+  ok = ok && reinsert(p, ins[0], un[0], true, pq, cap, ctr);
+  ok = ok && reinsert(p, ins[1], un[1], false, pq, cap, ctr);
   valid[k] = ok ? 1u : 0u;
   toFix[3 * k + 0] = ok ? g : kNone;
   toFix[3 * k + 1] = ok ? un[0] : kNone;
@@ -338,7 +344,8 @@ __global__ void patch_kernel(const bvhgb_node *__restrict__ t, uint32_t root, co
     if (ok && p.idx[s] != kNone) atomicMin(&owner[p.idx[s]], k);
   }
   if (!ok) atomicAdd(&stats[S_INVALID], 1ull);
-  if (overflow) atomicAdd(&stats[S_OVERFLOW], (unsigned long long)overflow);
+  if (ctr.overflow) atomicAdd(&stats[S_OVERFLOW], (unsigned long long)ctr.overflow);
+  atomicAdd(&stats[S_VISITS], (unsigned long long)ctr.visits);
   atomicAdd(&stats[S_ITEMS], 1ull);
 }
 
@@ -449,6 +456,8 @@ struct bvhgb_bn13_workspace {
   unsigned long long *stats = nullptr;
   cudaGraphExec_t graph = nullptr;
   bvhgb_node *graphNodes = nullptr;
+  uint32_t launchesPerIteration = 0;
+  std::vector<cudaEvent_t> evStart, evStop;  // per chunk, profileKernels only
 };
 
 namespace {
@@ -466,10 +475,13 @@ int run_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t c, cudaStrea
   if (cs == 0) return BVHGB_OK;
   const uint32_t bs = ws->cfg.blockSize ? ws->cfg.blockSize : 128;
   const uint32_t grid = ceil_div(cs, bs);
+  const bool prof = !ws->evStart.empty();
+  if (prof) BVHGB_CUDA_TRY(cudaEventRecordWithFlags(ws->evStart[c], s, cudaEventRecordExternal));
   patch_kernel<<<grid, bs, 0, s>>>(nodes, ws->root, ws->todo, ws->numInner, c, ws->numChunks, cs, ws->cfg.offsetAccess,
                                    ws->patches, ws->valid, ws->toFix, ws->owner, ws->heaps, ws->cfg.heapCapacity,
                                    ws->stats);
   BVHGB_LAUNCH_CHECK("bn13 patch");
+  if (prof) BVHGB_CUDA_TRY(cudaEventRecordWithFlags(ws->evStop[c], s, cudaEventRecordExternal));
   apply_kernel<<<grid, bs, 0, s>>>(nodes, ws->patches, ws->valid, ws->toFix, ws->owner, cs, ws->stats);
   BVHGB_LAUNCH_CHECK("bn13 apply");
   count_kernel<<<grid, bs, 0, s>>>(nodes, ws->root, ws->patches, ws->toFix, ws->owner, ws->counter, cs, ws->numNodes,
@@ -496,7 +508,7 @@ extern "C" BVHGB_API int bvhgb_bn13_create(const bvhgb_node *nodes, uint32_t num
   if (!out || !nodes || numNodes == 0 || root >= numNodes) return BVHGB_INVALID_ARGUMENT;
   *out = nullptr;
   auto *ws = new bvhgb_bn13_workspace();
-  ws->cfg = cfg ? *cfg : bvhgb_bn13_config{32u, 128u, 1.0f, 0u, 4096u};
+  ws->cfg = cfg ? *cfg : bvhgb_bn13_config{32u, 128u, 1.0f, 0u, 4096u, 0u};
   if (ws->cfg.numChunks == 0) ws->cfg.numChunks = 1;
   if (ws->cfg.heapCapacity < 4) ws->cfg.heapCapacity = 4096;
   if (ws->cfg.blockSize == 0 || ws->cfg.blockSize > 1024) ws->cfg.blockSize = 128;
@@ -557,6 +569,14 @@ extern "C" BVHGB_API int bvhgb_bn13_create(const bvhgb_node *nodes, uint32_t num
   if (e == cudaSuccess) e = cudaMemsetAsync(ws->err, 0, 4, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ws->stats, 0, sizeof(unsigned long long) * S_COUNT, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess && ws->cfg.profileKernels) {
+    ws->evStart.assign(ws->numChunks, nullptr);
+    ws->evStop.assign(ws->numChunks, nullptr);
+    for (uint32_t c = 0; c < ws->numChunks && e == cudaSuccess; ++c) {
+      e = cudaEventCreate(&ws->evStart[c]);
+      if (e == cudaSuccess) e = cudaEventCreate(&ws->evStop[c]);
+    }
+  }
   if (e != cudaSuccess) {
     set_last_error("bvhgb_bn13_create", e);
     bvhgb_bn13_destroy(ws);
@@ -569,6 +589,10 @@ extern "C" BVHGB_API int bvhgb_bn13_create(const bvhgb_node *nodes, uint32_t num
 extern "C" BVHGB_API int bvhgb_bn13_destroy(bvhgb_bn13_workspace *ws) {
   if (!ws) return BVHGB_OK;
   if (ws->graph) cudaGraphExecDestroy(ws->graph);
+  for (cudaEvent_t ev : ws->evStart)
+    if (ev) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : ws->evStop)
+    if (ev) cudaEventDestroy(ev);
   cudaFree(ws->inner);
   cudaFree(ws->keys);
   cudaFree(ws->vals);
@@ -584,6 +608,27 @@ extern "C" BVHGB_API int bvhgb_bn13_destroy(bvhgb_bn13_workspace *ws) {
   cudaFree(ws->heaps);
   cudaFree(ws->stats);
   delete ws;
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API uint32_t bvhgb_bn13_launches_per_iteration(const bvhgb_bn13_workspace *ws) {
+  return ws ? ws->launchesPerIteration : 0;
+}
+
+extern "C" BVHGB_API int bvhgb_bn13_search_time(bvhgb_bn13_workspace *ws, float *ms, uint32_t *launches) {
+  if (!ws || !ms) return BVHGB_INVALID_ARGUMENT;
+  *ms = 0.0f;
+  if (launches) *launches = 0;
+  if (ws->evStart.empty()) return BVHGB_INVALID_ARGUMENT;
+  float total = 0.0f;
+  for (uint32_t c = 0; c < ws->numChunks; ++c) {
+    BVHGB_CUDA_TRY(cudaEventSynchronize(ws->evStop[c]));
+    float t = 0.0f;
+    BVHGB_CUDA_TRY(cudaEventElapsedTime(&t, ws->evStart[c], ws->evStop[c]));
+    total += t;
+  }
+  *ms = total;
+  if (launches) *launches = ws->numChunks;
   return BVHGB_OK;
 }
 
@@ -624,10 +669,12 @@ extern "C" BVHGB_API int bvhgb_bn13_run(bvhgb_bn13_workspace *ws, bvhgb_node *no
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     int st = BVHGB_OK;
+    const uint64_t before = bvhgb_launch_count();
     if (e == cudaSuccess) {
       st = do_step(ws, nodes, cap);
       e = cudaStreamEndCapture(cap, &g);
     }
+    ws->launchesPerIteration = (uint32_t)(bvhgb_launch_count() - before);
     if (e == cudaSuccess && st == BVHGB_OK) e = cudaGraphInstantiate(&ws->graph, g, 0);
     if (g) cudaGraphDestroy(g);
     cudaStreamDestroy(cap);
@@ -658,5 +705,6 @@ extern "C" BVHGB_API int bvhgb_bn13_get_stats(bvhgb_bn13_workspace *ws, bvhgb_bn
   stats->skippedConflict = h[S_CONFLICT];
   stats->skippedInvalid = h[S_INVALID];
   stats->heapOverflow = h[S_OVERFLOW];
+  stats->nodesVisited = h[S_VISITS];
   return err ? BVHGB_BVH_ERROR : BVHGB_OK;
 }

@@ -248,6 +248,106 @@ struct TraceParams {
   uint32_t cull;
 };
 
+// Camera::genRays (Camera.cpp:67-88): pixel coordinates in double, the rest in float.
+__device__ __forceinline__ void camera_ray(const CamParams &cam, uint32_t x, uint32_t y, RayPre &r) {
+  const double qx = __ddiv_rn(__dadd_rn((double)x, 0.5), (double)cam.w);
+  const double qy = __ddiv_rn(__dadd_rn((double)y, 0.5), (double)cam.h);
+  const float px = (float)__dmul_rn(__dmul_rn(__dsub_rn(__dmul_rn(2.0, qx), 1.0), (double)cam.scale), (double)cam.ratio);
+  const float py = (float)__dmul_rn(__dsub_rn(1.0, __dmul_rn(2.0, qy)), (double)cam.scale);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    r.o[k] = cam.pos[k];
+    r.d[k] = fadd(fadd(fmul(cam.s[k], px), fmul(cam.u[k], py)), cam.f[k]);
+  }
+  normalize3(r.d);
+  setup_ray(r);
+}
+
+// Counter-based uniform floats in [0, 1): SplitMix64 finaliser of (seed, index, lane).
+__device__ __forceinline__ float uniform01(uint64_t seed, uint64_t idx, uint32_t lane) {
+  uint64_t z = seed + 0x9E3779B97F4A7C15ull * (2 * idx + lane + 1);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (float)(z >> 40) * (1.0f / 16777216.0f);
+}
+
+// One cosine-weighted diffuse bounce from every primary hit (an addition: the reference traces
+// primary rays only). The bounce starts on the hit point, offset along the normal that faces the
+// incoming ray; the direction follows Malley's method around that normal in the orthonormal basis
+// of Duff et al. (JCGT 2017).
+__global__ void __launch_bounds__(128) trace_bounce_kernel(const bvhgb_node *__restrict__ nodes, uint32_t numNodes,
+                                                           uint32_t root, const float *__restrict__ vert,
+                                                           const uint32_t *__restrict__ faces, CamParams cam,
+                                                           TraceParams tp, uint64_t seed, float offset,
+                                                           const bvhgb_hit *__restrict__ primary,
+                                                           bvhgb_hit *__restrict__ out, float *__restrict__ rayOrg,
+                                                           float *__restrict__ rayDir) {
+  const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= cam.w || y >= cam.h) return;
+  const size_t pix = (size_t)y * cam.w + x;
+  const bvhgb_hit ph = primary[pix];
+  bvhgb_hit o;
+  o.primId = kNone;
+  o.t = __int_as_float(0x7f800000);
+  if (ph.primId == kNone) {
+    out[pix] = o;
+    if (rayOrg) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) rayOrg[3 * pix + k] = rayDir[3 * pix + k] = 0.0f;
+    }
+    return;
+  }
+  RayPre cr;
+  camera_ray(cam, x, y, cr);
+  float v0[3], v1[3], v2[3];
+  load_tri(vert, faces, ph.primId, v0, v1, v2);
+  float e1[3], e2[3], n[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    e1[k] = fsub(v1[k], v0[k]);
+    e2[k] = fsub(v2[k], v0[k]);
+  }
+  n[0] = fsub(fmul(e1[1], e2[2]), fmul(e1[2], e2[1]));
+  n[1] = fsub(fmul(e1[2], e2[0]), fmul(e1[0], e2[2]));
+  n[2] = fsub(fmul(e1[0], e2[1]), fmul(e1[1], e2[0]));
+  normalize3(n);
+  const float dn = fadd(fadd(fmul(n[0], cr.d[0]), fmul(n[1], cr.d[1])), fmul(n[2], cr.d[2]));
+  if (dn > 0.0f) { n[0] = -n[0]; n[1] = -n[1]; n[2] = -n[2]; }
+  // Orthonormal basis (t, b, n).
+  const float sgn = copysignf(1.0f, n[2]);
+  const float a = -1.0f / (sgn + n[2]);
+  const float bb = n[0] * n[1] * a;
+  const float tv[3] = {1.0f + sgn * n[0] * n[0] * a, sgn * bb, -sgn * n[0]};
+  const float bv[3] = {bb, sgn + n[1] * n[1] * a, -n[1]};
+  const float u1 = uniform01(seed, pix, 0), u2 = uniform01(seed, pix, 1);
+  const float rr = sqrtf(u1), phi = 6.28318530717958647692f * u2;
+  float sn, cs;
+  sincosf(phi, &sn, &cs);
+  const float lx = rr * cs, ly = rr * sn, lz = sqrtf(fmaxf(0.0f, 1.0f - u1));
+  RayPre r;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float hp = fadd(cr.o[k], fmul(ph.t, cr.d[k]));
+    r.o[k] = hp + offset * n[k];
+    r.d[k] = lx * tv[k] + ly * bv[k] + lz * n[k];
+  }
+  if (rayOrg) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      rayOrg[3 * pix + k] = r.o[k];
+      rayDir[3 * pix + k] = r.d[k];
+    }
+  }
+  setup_ray(r);
+  Hit h;
+  traverse(r, nodes, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h);
+  o.primId = h.prim;
+  o.t = h.prim == kNone ? __int_as_float(0x7f800000) : h.t;
+  out[pix] = o;
+}
+
 __global__ void __launch_bounds__(128) trace_image_kernel(const bvhgb_node *__restrict__ nodes, uint32_t numNodes,
                                                           uint32_t root, const float *__restrict__ vert,
                                                           const uint32_t *__restrict__ faces, CamParams cam,
@@ -256,19 +356,8 @@ __global__ void __launch_bounds__(128) trace_image_kernel(const bvhgb_node *__re
   const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= cam.w || y >= cam.h) return;
-  // Camera::genRays (Camera.cpp:67-88): pixel coordinates in double, the rest in float.
-  const double qx = __ddiv_rn(__dadd_rn((double)x, 0.5), (double)cam.w);
-  const double qy = __ddiv_rn(__dadd_rn((double)y, 0.5), (double)cam.h);
-  const float px = (float)__dmul_rn(__dmul_rn(__dsub_rn(__dmul_rn(2.0, qx), 1.0), (double)cam.scale), (double)cam.ratio);
-  const float py = (float)__dmul_rn(__dsub_rn(1.0, __dmul_rn(2.0, qy)), (double)cam.scale);
   RayPre r;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    r.o[k] = cam.pos[k];
-    r.d[k] = fadd(fadd(fmul(cam.s[k], px), fmul(cam.u[k], py)), cam.f[k]);
-  }
-  normalize3(r.d);
-  setup_ray(r);
+  camera_ray(cam, x, y, r);
   Hit h;
   const uint32_t visits = traverse(r, nodes, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h);
   bvhgb_pixel px_out;
@@ -335,6 +424,29 @@ void h_cross(const float *a, const float *b, float *o) {
   o[2] = z0 - z1;
 }
 
+// Camera basis of inverse(lookAtRH(pos, lookAt, up)) (CUDAKernels.cu:389-391), host side.
+CamParams make_cam_params(const bvhgb_camera *cam) {
+  CamParams cp;
+  float f[3] = {cam->lookAt[0] - cam->pos[0], cam->lookAt[1] - cam->pos[1], cam->lookAt[2] - cam->pos[2]};
+  h_normalize(f);
+  float s[3];
+  h_cross(f, cam->up, s);
+  h_normalize(s);
+  float u[3];
+  h_cross(s, f, u);
+  for (int k = 0; k < 3; ++k) {
+    cp.pos[k] = cam->pos[k];
+    cp.s[k] = s[k];
+    cp.u[k] = u[k];
+    cp.f[k] = f[k];
+  }
+  cp.scale = (float)std::tan(0.5 * (double)cam->fov * 0.01745329251994329576923690768489);
+  cp.ratio = (float)cam->width / (float)cam->height;
+  cp.w = cam->width;
+  cp.h = cam->height;
+  return cp;
+}
+
 TraceParams make_trace_params(const bvhgb_trace_config *cfg) {
   TraceParams tp;
   if (cfg) {
@@ -361,25 +473,7 @@ extern "C" BVHGB_API int bvhgb_trace_image(const bvhgb_node *nodes, uint32_t num
                                            bvhgb_pixel *img, bvhgb_hit *hits, bvhgb_stream stream) {
   if (!nodes || !vert || !faces || !cam || !img || numNodes == 0 || root >= numNodes) return BVHGB_INVALID_ARGUMENT;
   if (cam->width == 0 || cam->height == 0) return BVHGB_OK;
-  // Camera basis of inverse(lookAtRH(pos, lookAt, up)) (CUDAKernels.cu:389-391).
-  CamParams cp;
-  float f[3] = {cam->lookAt[0] - cam->pos[0], cam->lookAt[1] - cam->pos[1], cam->lookAt[2] - cam->pos[2]};
-  h_normalize(f);
-  float s[3];
-  h_cross(f, cam->up, s);
-  h_normalize(s);
-  float u[3];
-  h_cross(s, f, u);
-  for (int k = 0; k < 3; ++k) {
-    cp.pos[k] = cam->pos[k];
-    cp.s[k] = s[k];
-    cp.u[k] = u[k];
-    cp.f[k] = f[k];
-  }
-  cp.scale = (float)std::tan(0.5 * (double)cam->fov * 0.01745329251994329576923690768489);
-  cp.ratio = (float)cam->width / (float)cam->height;
-  cp.w = cam->width;
-  cp.h = cam->height;
+  const CamParams cp = make_cam_params(cam);
   dim3 block(16, 8);
   dim3 grid(ceil_div(cam->width, 16), ceil_div(cam->height, 8));
   trace_image_kernel<<<grid, block, 0, as_stream(stream)>>>(nodes, numNodes, root, vert, faces, cp, make_trace_params(cfg),
@@ -397,6 +491,24 @@ extern "C" BVHGB_API int bvhgb_trace_rays(const bvhgb_node *nodes, uint32_t numN
   trace_rays_kernel<<<ceil_div(n, 128), 128, 0, as_stream(stream)>>>(nodes, numNodes, root, vert, faces, org, dir, n,
                                                                      make_trace_params(cfg), hits);
   BVHGB_LAUNCH_CHECK("trace rays");
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_trace_bounce(const bvhgb_node *nodes, uint32_t numNodes, uint32_t root, const float *vert,
+                                            const uint32_t *faces, const bvhgb_camera *cam, const bvhgb_trace_config *cfg,
+                                            uint64_t seed, float offset, const bvhgb_hit *primary, bvhgb_hit *bounce,
+                                            float *rayOrg, float *rayDir, bvhgb_stream stream) {
+  if (!nodes || !vert || !faces || !cam || !primary || !bounce || numNodes == 0 || root >= numNodes)
+    return BVHGB_INVALID_ARGUMENT;
+  if ((rayOrg == nullptr) != (rayDir == nullptr)) return BVHGB_INVALID_ARGUMENT;
+  if (cam->width == 0 || cam->height == 0) return BVHGB_OK;
+  const CamParams cp = make_cam_params(cam);
+  dim3 block(16, 8);
+  dim3 grid(ceil_div(cam->width, 16), ceil_div(cam->height, 8));
+  trace_bounce_kernel<<<grid, block, 0, as_stream(stream)>>>(nodes, numNodes, root, vert, faces, cp,
+                                                             make_trace_params(cfg), seed, offset, primary, bounce,
+                                                             rayOrg, rayDir);
+  BVHGB_LAUNCH_CHECK("trace bounce");
   return BVHGB_OK;
 }
 

@@ -41,12 +41,12 @@ class LbvhConfig(C.Structure):
 
 class Bn13Config(C.Structure):
     _fields_ = [("numChunks", C.c_uint32), ("blockSize", C.c_uint32), ("batchPercent", C.c_float),
-                ("offsetAccess", C.c_uint32), ("heapCapacity", C.c_uint32)]
+                ("offsetAccess", C.c_uint32), ("heapCapacity", C.c_uint32), ("profileKernels", C.c_uint32)]
 
 
 class Bn13Stats(C.Structure):
     _fields_ = [("items", C.c_uint64), ("applied", C.c_uint64), ("skippedConflict", C.c_uint64),
-                ("skippedInvalid", C.c_uint64), ("heapOverflow", C.c_uint64)]
+                ("skippedInvalid", C.c_uint64), ("heapOverflow", C.c_uint64), ("nodesVisited", C.c_uint64)]
 
 
 class Camera(C.Structure):
@@ -92,8 +92,12 @@ PROTOS = {
     "bvhgb_bn13_chunk": (I32, [VP, VP, U32, VP]),
     "bvhgb_bn13_get_stats": (I32, [VP, C.POINTER(Bn13Stats), VP]),
     "bvhgb_bn13_batch_size": (U32, [VP]),
+    "bvhgb_bn13_launches_per_iteration": (U32, [VP]),
+    "bvhgb_bn13_search_time": (I32, [VP, C.POINTER(F32), C.POINTER(U32)]),
     "bvhgb_trace_image": (I32, [VP, U32, U32, VP, VP, C.POINTER(Camera), C.POINTER(TraceConfig), VP, VP, VP]),
     "bvhgb_trace_rays": (I32, [VP, U32, U32, VP, VP, VP, VP, U32, C.POINTER(TraceConfig), VP, VP]),
+    "bvhgb_trace_bounce": (I32, [VP, U32, U32, VP, VP, C.POINTER(Camera), C.POINTER(TraceConfig), U64, F32, VP, VP,
+                                 VP, VP, VP]),
     "bvhgb_trace_read_errors": (I32, [C.POINTER(U32), I32]),
     "bvhgb_copy_mesh_to_gpu": (I32, [VP, U32, VP, U32, VP, U32, C.POINTER(MeshRaw)]),
     "bvhgb_copy_mesh_to_host": (I32, [C.POINTER(MeshRaw), VP, VP, VP]),

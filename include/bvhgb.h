@@ -175,6 +175,7 @@ typedef struct bvhgb_bn13_config {
   float batchPercent;    /* batchPercent = 1.0, clamped to [0.01, 75] */
   uint32_t offsetAccess; /* offsetAccess = false */
   uint32_t heapCapacity; /* branch-and-bound queue entries per item (reference: 4096) */
+  uint32_t profileKernels; /* 1: bracket every reinsertion-search launch with CUDA events */
 } bvhgb_bn13_config;
 
 typedef struct bvhgb_bn13_stats {
@@ -183,6 +184,7 @@ typedef struct bvhgb_bn13_stats {
   uint64_t skippedConflict;  /* lost the conflict check (numSkipped in the reference) */
   uint64_t skippedInvalid;   /* removeNode refused or best position == root */
   uint64_t heapOverflow;     /* queue pushes dropped at heapCapacity */
+  uint64_t nodesVisited;     /* nodes evaluated by the reinsertion searches */
 } bvhgb_bn13_stats;
 
 typedef struct bvhgb_bn13_workspace bvhgb_bn13_workspace;
@@ -202,6 +204,11 @@ BVHGB_API int bvhgb_bn13_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint
 BVHGB_API int bvhgb_bn13_get_stats(bvhgb_bn13_workspace *ws, bvhgb_bn13_stats *stats, bvhgb_stream stream);
 /* Number of items per iteration (numChunks * chunkSize, Bittner13GPU.cpp:90-92). */
 BVHGB_API uint32_t bvhgb_bn13_batch_size(const bvhgb_bn13_workspace *ws);
+/* Kernels one iteration launches (the nodes of the captured graph). */
+BVHGB_API uint32_t bvhgb_bn13_launches_per_iteration(const bvhgb_bn13_workspace *ws);
+/* With profileKernels = 1: total milliseconds of the reinsertion-search kernel over the chunks of
+ * the most recent iteration, and the number of launches that covers (synchronous). */
+BVHGB_API int bvhgb_bn13_search_time(bvhgb_bn13_workspace *ws, float *ms, uint32_t *launches);
 
 /* ---- tracer (lib/tracer/CUDAKernels.hpp:39-77, CUDATracer.cpp:86-118) ------------------------ */
 
@@ -231,6 +238,15 @@ BVHGB_API int bvhgb_trace_rays(const bvhgb_node *nodes, uint32_t numNodes, uint3
                                const uint32_t *faces, const float *org, const float *dir, uint32_t n,
                                const bvhgb_trace_config *cfg, bvhgb_hit *hits, bvhgb_stream stream);
 
+/* One cosine-weighted diffuse bounce per primary hit (an addition: the reference has no secondary
+ * rays). primary: the hits of bvhgb_trace_image for the same camera. The bounce leaves the hit
+ * point offset by 'offset' along the normal facing the camera ray; its direction is drawn from a
+ * counter-based generator keyed by (seed, pixel). bounce[pixel] gets the closest hit (miss where
+ * the primary ray missed). rayOrg/rayDir (float3 per pixel, optional) receive the bounce rays. */
+BVHGB_API int bvhgb_trace_bounce(const bvhgb_node *nodes, uint32_t numNodes, uint32_t root, const float *vert,
+                                 const uint32_t *faces, const bvhgb_camera *cam, const bvhgb_trace_config *cfg,
+                                 uint64_t seed, float offset, const bvhgb_hit *primary, bvhgb_hit *bounce,
+                                 float *rayOrg, float *rayDir, bvhgb_stream stream);
 /* Device-side traversal error bits seen since the last reset (2 = stack overflow, 4 = bad child
  * index); synchronous. */
 BVHGB_API int bvhgb_trace_read_errors(uint32_t *flags, int reset);
