@@ -103,6 +103,11 @@ class LBVH:
         check(self.lib.bvhgb_lbvh_read_scene_box(self.ws, C.byref(a), _stream(stream)), "read_scene_box")
         return np.array(list(a.mn) + list(a.mx), np.float32)
 
+    def errors(self, stream=None) -> int:
+        v = C.c_uint32()
+        check(self.lib.bvhgb_lbvh_read_errors(self.ws, C.byref(v), _stream(stream)), "read_errors")
+        return v.value
+
     def keys(self, n, sorted_: bool, stream=None):
         k = np.zeros(n, np.uint32 if self.cfg.mortonBits == 30 else np.uint64)
         idx = np.zeros(n, np.uint32)

@@ -82,6 +82,14 @@ struct Patch {
   Box abox[4];
   const bvhgb_node *t;
   uint32_t root;
+  uint32_t numNodes;
+  mutable bool bad;  // an index outside the node array was met (corrupted input); item is dropped
+
+  __device__ uint32_t chk(uint32_t x) const {
+    if (x < numNodes) return x;
+    bad = true;
+    return root;
+  }
 
   __device__ void clear() {
 #pragma unroll
@@ -104,15 +112,15 @@ struct Patch {
   }
   __device__ NodeP get(uint32_t x) const {
     uint32_t i = index(x);
-    return i == kNone ? tree_node(t, x) : nd[i];
+    return i == kNone ? tree_node(t, chk(x)) : nd[i];
   }
   __device__ NodeP get_subset(uint32_t x) const {
     uint32_t i = index_subset(x);
-    return i == kNone ? tree_node(t, x) : nd[i];
+    return i == kNone ? tree_node(t, chk(x)) : nd[i];
   }
   __device__ uint32_t patch_node(uint32_t x, uint32_t slot) {
     idx[slot] = x;
-    nd[slot] = tree_node(t, x);
+    nd[slot] = tree_node(t, chk(x));
     return slot;
   }
   __device__ uint32_t move(uint32_t from, uint32_t to) {
@@ -128,7 +136,7 @@ struct Patch {
   __device__ Box get_aabb(uint32_t x) const {
     for (int i = 0; i < 4; ++i)
       if (apath[i] == x) return abox[i];
-    return tree_box(t, x);
+    return tree_box(t, chk(x));
   }
   // patchAABBFrom (BVHPatch.hpp:293-316)
   __device__ void patch_aabb_from(uint32_t x, uint32_t pidx) {
@@ -189,12 +197,17 @@ __device__ __forceinline__ void heap_pop(HeapItem *h, long len) {
 __device__ uint32_t find_node(const Patch &p, uint32_t n, HeapItem *pq, uint32_t cap, SearchCounters &ctr) {
   float best_cost = __int_as_float(0x7f800000);
   uint32_t best = 0;
-  const Box nbox = tree_box(p.t, n);
-  const float sarea = tree_sa(p.t, n);
+  const Box nbox = tree_box(p.t, p.chk(n));
+  const float sarea = tree_sa(p.t, p.chk(n));
   long size = 1;
   pq[0].node = p.root;
   pq[0].cost = 0.0f;
-  while (size > 0) {
+  // A tree pops each node at most once; the bound only matters for corrupted input.
+  for (uint32_t it = 0; size > 0; ++it) {
+    if (it > p.numNodes) {
+      p.bad = true;
+      break;
+    }
     const HeapItem cur = pq[0];
     if (fadd(cur.cost, sarea) >= best_cost) break;
     heap_pop(pq, size);
@@ -230,7 +243,7 @@ __device__ uint32_t find_node(const Patch &p, uint32_t n, HeapItem *pq, uint32_t
 
 // removeNode (Bittner13CUDA.cu:267-305).
 __device__ bool remove_node(Patch &p, uint32_t x, uint32_t ins[2], uint32_t un[2], uint32_t &g_out) {
-  if (tree_leaf(p.t, x) || x == p.root) return false;
+  if (tree_leaf(p.t, p.chk(x)) || x == p.root) return false;
   const uint32_t sn = p.patch_node(x, P_NODE);
   const uint32_t s = p.sibling(p.nd[sn]);
   const uint32_t pi = p.nd[sn].parent;
@@ -249,7 +262,7 @@ __device__ bool remove_node(Patch &p, uint32_t x, uint32_t ins[2], uint32_t un[2
   p.nd[ss].parent = gi;
   p.patch_aabb_from(gi, 0);
   const uint32_t l = p.nd[sn].left, r = p.nd[sn].right;
-  if (tree_sa(p.t, l) > tree_sa(p.t, r)) { ins[0] = l; ins[1] = r; }
+  if (tree_sa(p.t, p.chk(l)) > tree_sa(p.t, p.chk(r))) { ins[0] = l; ins[1] = r; }
   else { ins[0] = r; ins[1] = l; }
   un[0] = x;
   un[1] = pi;
@@ -317,13 +330,16 @@ __global__ void patch_kernel(const bvhgb_node *__restrict__ t, uint32_t root, co
                              uint32_t numTodo, uint32_t chunk, uint32_t numChunks, uint32_t chunkSize,
                              uint32_t offsetAccess, PatchOut *__restrict__ out, uint32_t *__restrict__ valid,
                              uint32_t *__restrict__ toFix, uint32_t *__restrict__ owner, HeapItem *__restrict__ heaps,
-                             uint32_t cap, unsigned long long *__restrict__ stats) {
+                             uint32_t cap, unsigned long long *__restrict__ stats, uint32_t numNodes,
+                             uint32_t *__restrict__ err) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= chunkSize) return;
   const uint32_t pos = offsetAccess ? k * numChunks + chunk : chunk * chunkSize + k;
   Patch p;
   p.t = t;
   p.root = root;
+  p.numNodes = numNodes;
+  p.bad = false;
   p.clear();
   SearchCounters ctr = {0u, 0u};
   uint32_t ins[2], un[2], g = kNone;
@@ -333,6 +349,10 @@ __global__ void patch_kernel(const bvhgb_node *__restrict__ t, uint32_t root, co
   ok = ok && remove_node(p, node, ins, un, g);
   ok = ok && reinsert(p, ins[0], un[0], true, pq, cap, ctr);
   ok = ok && reinsert(p, ins[1], un[1], false, pq, cap, ctr);
+  if (p.bad) {
+    atomicOr(err, kErrBadIndex);
+    ok = false;
+  }
   valid[k] = ok ? 1u : 0u;
   toFix[3 * k + 0] = ok ? g : kNone;
   toFix[3 * k + 1] = ok ? un[0] : kNone;
@@ -479,7 +499,7 @@ int run_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t c, cudaStrea
   if (prof) BVHGB_CUDA_TRY(cudaEventRecordWithFlags(ws->evStart[c], s, cudaEventRecordExternal));
   patch_kernel<<<grid, bs, 0, s>>>(nodes, ws->root, ws->todo, ws->numInner, c, ws->numChunks, cs, ws->cfg.offsetAccess,
                                    ws->patches, ws->valid, ws->toFix, ws->owner, ws->heaps, ws->cfg.heapCapacity,
-                                   ws->stats);
+                                   ws->stats, ws->numNodes, ws->err);
   BVHGB_LAUNCH_CHECK("bn13 patch");
   if (prof) BVHGB_CUDA_TRY(cudaEventRecordWithFlags(ws->evStop[c], s, cudaEventRecordExternal));
   apply_kernel<<<grid, bs, 0, s>>>(nodes, ws->patches, ws->valid, ws->toFix, ws->owner, cs, ws->stats);

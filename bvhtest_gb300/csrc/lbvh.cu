@@ -26,6 +26,7 @@ struct bvhgb_lbvh_workspace {
   uint32_t *vals = nullptr;
   uint32_t *valsSorted = nullptr;
   uint32_t *slots = nullptr;
+  bool slotsArmed = false;  // slots hold kNone (set by the Morton kernel)
   void *sortTemp = nullptr;
   size_t sortTempBytes = 0;
 };
@@ -204,7 +205,8 @@ __global__ void __launch_bounds__(kBuildThreads) lbvh_build_kernel(const float *
                                                                    const uint32_t *__restrict__ faces,
                                                                    const K *__restrict__ keys,
                                                                    const uint32_t *__restrict__ idx, uint32_t n,
-                                                                   bvhgb_node *nodes, uint32_t *slots) {
+                                                                   bvhgb_node *nodes, uint32_t *slots,
+                                                                   uint32_t *err) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   // Leaf (kGenLeafNodes, LBVH_CUDA.cu:273-292): left = face, right = 1, level = UINT8_MAX.
@@ -220,12 +222,18 @@ __global__ void __launch_bounds__(kBuildThreads) lbvh_build_kernel(const float *
 
   uint32_t l = i, r = i;
   bool right = parent_is_right<MODE, K>(keys, l, r, n);
-  for (;;) {
+  // Each step at least doubles nothing but strictly grows [l, r], so n - 1 steps reach the root;
+  // the bound and the range checks turn corrupted exchange slots into an error, not a hang.
+  for (uint32_t step = 0;; ++step) {
     const uint32_t split = right ? r : l - 1;
     // Meet the sibling: the first thread leaves its far end in the slot and stops.
     const uint32_t other = atom_exch_acq_rel(&slots[split], right ? l : r);
     if (other == kNone) return;
     const uint32_t L = right ? l : other, R = right ? other : r;
+    if (step >= n || L > split || split + 1 > R || R >= n) {
+      atomicOr(err, kErrBadIndex);
+      return;
+    }
     const uint32_t a = (L == split) ? n - 1 + split : split;          // left child  [L, split]
     const uint32_t b = (split + 1 == R) ? n - 1 + split + 1 : split + 1;  // right child [split+1, R]
     const Box sib = load_box_cg(nodes + (right ? b : a));
@@ -249,15 +257,19 @@ __global__ void __launch_bounds__(kBuildThreads) lbvh_build_kernel(const float *
 }
 
 template <int MODE>
-int launch_build(const bvhgb_lbvh_workspace *ws, const float *vert, const uint32_t *faces, uint32_t n,
+int launch_build(bvhgb_lbvh_workspace *ws, const float *vert, const uint32_t *faces, uint32_t n,
                  bvhgb_node *nodes, cudaStream_t s) {
+  // The exchange slots are re-armed by the Morton kernel; a second build from the same sorted keys
+  // re-arms them here.
+  if (!ws->slotsArmed) BVHGB_CUDA_TRY(cudaMemsetAsync(ws->slots, 0xFF, 4ull * n, s));
+  ws->slotsArmed = false;
   dim3 grid(ceil_div(n, kBuildThreads));
   if (ws->keyBytes == 4)
     lbvh_build_kernel<MODE, uint32_t><<<grid, kBuildThreads, 0, s>>>(
-        vert, faces, static_cast<const uint32_t *>(ws->keysSorted), ws->valsSorted, n, nodes, ws->slots);
+        vert, faces, static_cast<const uint32_t *>(ws->keysSorted), ws->valsSorted, n, nodes, ws->slots, ws->scene + 6);
   else
     lbvh_build_kernel<MODE, uint64_t><<<grid, kBuildThreads, 0, s>>>(
-        vert, faces, static_cast<const uint64_t *>(ws->keysSorted), ws->valsSorted, n, nodes, ws->slots);
+        vert, faces, static_cast<const uint64_t *>(ws->keysSorted), ws->valsSorted, n, nodes, ws->slots, ws->scene + 6);
   BVHGB_LAUNCH_CHECK("lbvh build");
   return BVHGB_OK;
 }
@@ -345,6 +357,7 @@ extern "C" BVHGB_API int bvhgb_lbvh_calc_morton(bvhgb_lbvh_workspace *ws, const 
   else
     lbvh_morton_kernel<63><<<grid, kMortonThreads, 0, s>>>(vert, faces, n, ws->scene, ws->keys, ws->vals, ws->slots);
   BVHGB_LAUNCH_CHECK("lbvh morton");
+  ws->slotsArmed = true;
   return BVHGB_OK;
 }
 
@@ -406,5 +419,17 @@ extern "C" BVHGB_API int bvhgb_lbvh_read_keys(bvhgb_lbvh_workspace *ws, int sort
   if (idx_host)
     BVHGB_CUDA_TRY(cudaMemcpyAsync(idx_host, sorted ? ws->valsSorted : ws->vals, 4ull * n, cudaMemcpyDeviceToHost, s));
   BVHGB_CUDA_TRY(cudaStreamSynchronize(s));
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_lbvh_read_errors(bvhgb_lbvh_workspace *ws, uint32_t *flags, bvhgb_stream stream) {
+  if (!ws || !flags) return BVHGB_INVALID_ARGUMENT;
+  uint32_t a = 0, b = 0;
+  cudaStream_t s = as_stream(stream);
+  BVHGB_CUDA_TRY(cudaMemcpyAsync(&a, ws->scene + 6, 4, cudaMemcpyDeviceToHost, s));
+  const uint32_t *se = sort_error_word(ws->sortTemp, ws->maxFaces, ws->keyBytes, 0, ws->cfg.mortonBits);
+  BVHGB_CUDA_TRY(cudaMemcpyAsync(&b, se, 4, cudaMemcpyDeviceToHost, s));
+  BVHGB_CUDA_TRY(cudaStreamSynchronize(s));
+  *flags = a | b;
   return BVHGB_OK;
 }

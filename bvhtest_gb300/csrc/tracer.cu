@@ -150,7 +150,12 @@ __device__ __forceinline__ uint32_t traverse(const RayPre &r, const bvhgb_node *
   if (!box_hit(r, a, b, tmin, tmax, tn)) return 0;
   uint32_t left = __float_as_uint(b.w), right = __float_as_uint(c.x);
   bool leaf = (__float_as_uint(c.y) & 0xFFFFu) != 0;
-  for (;;) {
+  // A tree visits each node at most once; the bound turns a cyclic (corrupted) input into an error.
+  for (uint32_t it = 0;; ++it) {
+    if (it > numNodes) {
+      atomicOr(&g_trace_errors, kErrBadIndex);
+      break;
+    }
     if (leaf) {
       test_leaf(r, vert, faces, left, right, tmin, tmax, cull, h);
     } else {

@@ -151,6 +151,9 @@ BVHGB_API int bvhgb_lbvh_build_tree(bvhgb_lbvh_workspace *ws, const float *vert,
 BVHGB_API int bvhgb_lbvh_read_scene_box(bvhgb_lbvh_workspace *ws, bvhgb_aabb *scene, bvhgb_stream stream);
 BVHGB_API int bvhgb_lbvh_read_keys(bvhgb_lbvh_workspace *ws, int sorted, void *keys_host, uint32_t *idx_host,
                                    uint32_t numFaces, bvhgb_stream stream);
+/* Device error bits of the last build (4 = an inconsistent exchange slot was met and the build
+ * stopped; 1 = the sort's look-back gave up); synchronous on 'stream'. 0 = the build is valid. */
+BVHGB_API int bvhgb_lbvh_read_errors(bvhgb_lbvh_workspace *ws, uint32_t *flags, bvhgb_stream stream);
 
 /* ---- radix sort (used by the build and the optimizer; exposed for tests) --------------------- */
 

@@ -42,6 +42,11 @@ def test_lbvh_bit_exact(gpu, orc, n, bits, topo):
     assert np.array_equal(idx, ref_idx)
     got = gpu.nodes_to_numpy(nodes)[: 2 * n - 1]
     assert np.array_equal(got.view(np.uint8), ref_nodes.view(np.uint8)), _first_diff(got, ref_nodes)
+    assert b.errors() == 0
+    # a second build_tree from the same sorted keys re-arms its exchange slots
+    b.build_tree(v, f, nodes)
+    torch.cuda.synchronize()
+    assert np.array_equal(gpu.nodes_to_numpy(nodes)[: 2 * n - 1].view(np.uint8), ref_nodes.view(np.uint8))
     # whole-command entry point gives the same bytes
     nodes2 = b.build(v, f)
     assert np.array_equal(gpu.nodes_to_numpy(nodes2)[: 2 * n - 1].view(np.uint8), ref_nodes.view(np.uint8))
