@@ -37,7 +37,7 @@ def workload(name: str):
     if name == "large":
         vert, faces = scenes.large_scene()
         return dict(name="large", vert=vert, faces=faces, bits=63, topo="karras", iters=200,
-                    camera=dict(pos=(5.0, 4.0, -9.0), lookAt=(5.0, 2.0, 5.0), up=(0.0, 1.0, 0.0), fov=60.0,
+                    camera=dict(pos=(5.0, 7.0, 5.0), lookAt=(5.0, 0.0, 5.0), up=(0.0, 0.0, 1.0), fov=60.0,
                                 width=1920, height=1080),
                     desc=("large single scene: 4,194,304 triangles (64-component Gaussian mixture + 724x724 "
                           "ground grid), 63-bit Morton, karras LBVH, 200 Bittner13 iterations at 1% (32 chunks), "

@@ -490,18 +490,28 @@ int select_nodes(bvhgb_bn13_workspace *ws, const bvhgb_node *nodes, cudaStream_t
   return sort_pairs(ws->sortTemp, ws->keys, ws->keysSorted, ws->vals, ws->todo, ws->numInner, 4, 0, 32, s);
 }
 
+// Inside a stream capture the record must become an event node of the graph (external record);
+// outside it is an ordinary record.
+cudaError_t record_event(cudaEvent_t ev, cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(s, &cs);
+  if (e != cudaSuccess) return e;
+  return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal)
+                                             : cudaEventRecord(ev, s);
+}
+
 int run_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t c, cudaStream_t s) {
   const uint32_t cs = ws->chunkSize;
   if (cs == 0) return BVHGB_OK;
   const uint32_t bs = ws->cfg.blockSize ? ws->cfg.blockSize : 128;
   const uint32_t grid = ceil_div(cs, bs);
   const bool prof = !ws->evStart.empty();
-  if (prof) BVHGB_CUDA_TRY(cudaEventRecordWithFlags(ws->evStart[c], s, cudaEventRecordExternal));
+  if (prof) BVHGB_CUDA_TRY(record_event(ws->evStart[c], s));
   patch_kernel<<<grid, bs, 0, s>>>(nodes, ws->root, ws->todo, ws->numInner, c, ws->numChunks, cs, ws->cfg.offsetAccess,
                                    ws->patches, ws->valid, ws->toFix, ws->owner, ws->heaps, ws->cfg.heapCapacity,
                                    ws->stats, ws->numNodes, ws->err);
   BVHGB_LAUNCH_CHECK("bn13 patch");
-  if (prof) BVHGB_CUDA_TRY(cudaEventRecordWithFlags(ws->evStop[c], s, cudaEventRecordExternal));
+  if (prof) BVHGB_CUDA_TRY(record_event(ws->evStop[c], s));
   apply_kernel<<<grid, bs, 0, s>>>(nodes, ws->patches, ws->valid, ws->toFix, ws->owner, cs, ws->stats);
   BVHGB_LAUNCH_CHECK("bn13 apply");
   count_kernel<<<grid, bs, 0, s>>>(nodes, ws->root, ws->patches, ws->toFix, ws->owner, ws->counter, cs, ws->numNodes,
