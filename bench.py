@@ -203,7 +203,7 @@ def run_ours(args, w, rank, world, local):
     lbvh = api.LBVH(n, w["bits"], w["topo"])
     lbvh.build(vert, faces, nodes)
     torch.cuda.synchronize()
-    opt = api.Bittner13GPU(nodes, num_nodes=n_nodes, profile=True)
+    opt = api.Bittner13GPU(nodes, num_nodes=n_nodes, profile=not args.no_kernel_events)
     cam = w["camera"]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
 
@@ -254,7 +254,7 @@ def run_ours(args, w, rank, world, local):
             hits_n.append((h.shape[0], int((h["prim"] != 0xFFFFFFFF).sum()), int((b["prim"] != 0xFFFFFFFF).sum())))
     c1 = lib.bvhgb_launch_count()
     st1 = opt.stats()
-    search_ms, search_launches = opt.search_time()
+    search_ms, search_launches = opt.search_time() if not args.no_kernel_events else (0.0, 0)
     sah = api.calc_sah(nodes, 0, n_nodes)
     mean = {k: statistics.mean(v) for k, v in phases.items()}
     build_ms = mean["bounds"] + mean["morton"] + mean["sort"] + mean["topology_refit"]
@@ -287,7 +287,8 @@ def run_ours(args, w, rank, world, local):
     clocks = clk.summary()
     if rank != 0:
         return
-    cpu = cpu_sample(w)
+    cpu = cpu_sample(w) if not args.no_cpu_baseline else {"value": float("nan"), "cores": 0, "sample": "skipped",
+                                                          "trace_mrays_per_s": float("nan")}
 
     # e2e through the C ABI: pinned host mesh -> device, build, optimize, node array -> pinned host.
     vh = torch.from_numpy(vert_h).pin_memory()
@@ -351,11 +352,19 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["large", "small"], default="large")
+    ap.add_argument("--iters", type=int, default=None,
+                    help="override the Bittner13 iteration count (profiling runs only; the headline uses the default)")
+    ap.add_argument("--no-kernel-events", action="store_true",
+                    help="do not bracket the search kernel with CUDA events (for runs under ncu)")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline sample")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     rank, world, local = dist_setup(args.gpus)
     w = workload(args.workload)
+    if args.iters is not None:
+        w["iters"] = args.iters
+        w["desc"] += f" [profiling run: {args.iters} iterations]"
     if args.impl == "reference":
         run_reference(args, w, rank, world)
     else:

@@ -162,53 +162,73 @@ struct Patch {
 // "less(a, b)" is a.cost > b.cost, so h[0] holds the smallest induced cost.
 __device__ __forceinline__ bool hless(const HeapItem &a, const HeapItem &b) { return a.cost > b.cost; }
 
-__device__ __forceinline__ void sift_up(HeapItem *h, long hole, long top, HeapItem v) {
+// Two-level storage: the first kHeapShared entries of each search live in shared memory,
+// interleaved across the warp's lanes (entry i of lane l at i * 32 + l, conflict-free when lanes
+// touch the same depth); deeper entries spill to the item's global region. The index space and
+// the capacity are unchanged, so the pop order is exactly that of a flat array.
+constexpr int kSearchThreads = 32;
+constexpr int kHeapShared = 128;
+
+struct Heap {
+  HeapItem *sm;  // this lane's entry 0 in shared memory (stride kSearchThreads)
+  HeapItem *gm;  // this item's global region (cap entries)
+  __device__ __forceinline__ HeapItem &at(long i) const { return i < kHeapShared ? sm[i * kSearchThreads] : gm[i]; }
+};
+
+__device__ __forceinline__ void sift_up(const Heap &h, long hole, long top, HeapItem v) {
   long parent = (hole - 1) / 2;
-  while (hole > top && hless(h[parent], v)) {
-    h[hole] = h[parent];
+  while (hole > top && hless(h.at(parent), v)) {
+    h.at(hole) = h.at(parent);
     hole = parent;
     parent = (hole - 1) / 2;
   }
-  h[hole] = v;
+  h.at(hole) = v;
 }
-__device__ __forceinline__ void heap_push(HeapItem *h, long lenAfter) { sift_up(h, lenAfter - 1, 0, h[lenAfter - 1]); }
-__device__ __forceinline__ void heap_pop(HeapItem *h, long len) {
+__device__ __forceinline__ void heap_push(const Heap &h, long lenAfter) { sift_up(h, lenAfter - 1, 0, h.at(lenAfter - 1)); }
+__device__ __forceinline__ void heap_pop(const Heap &h, long len) {
   if (len <= 1) return;
   const long last = len - 1;
-  const HeapItem v = h[last];
-  h[last] = h[0];
+  const HeapItem v = h.at(last);
+  h.at(last) = h.at(0);
   const long n = last;
   long hole = 0, second = 0;
   while (second < (n - 1) / 2) {
     second = 2 * (second + 1);
-    if (hless(h[second], h[second - 1])) second--;
-    h[hole] = h[second];
+    if (hless(h.at(second), h.at(second - 1))) second--;
+    h.at(hole) = h.at(second);
     hole = second;
   }
   if ((n & 1) == 0 && second == (n - 2) / 2) {
     second = 2 * (second + 1);
-    h[hole] = h[second - 1];
+    h.at(hole) = h.at(second - 1);
     hole = second - 1;
   }
   sift_up(h, hole, 0, v);
 }
 
+// Starts fetching a node's 48-byte record into L2 while the search keeps working.
+__device__ __forceinline__ void prefetch_node(const bvhgb_node *t, uint32_t x) {
+  const char *p = reinterpret_cast<const char *>(t + x);
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p + 32));
+}
+
 // findNode1 (Bittner13CUDA.cu:141-191).
-__device__ uint32_t find_node(const Patch &p, uint32_t n, HeapItem *pq, uint32_t cap, SearchCounters &ctr) {
+__device__ uint32_t find_node(const Patch &p, uint32_t n, const Heap &pq, uint32_t cap, SearchCounters &ctr) {
   float best_cost = __int_as_float(0x7f800000);
   uint32_t best = 0;
   const Box nbox = tree_box(p.t, p.chk(n));
   const float sarea = tree_sa(p.t, p.chk(n));
   long size = 1;
-  pq[0].node = p.root;
-  pq[0].cost = 0.0f;
+  pq.at(0).node = p.root;
+  pq.at(0).cost = 0.0f;
   // A tree pops each node at most once; the bound only matters for corrupted input.
   for (uint32_t it = 0; size > 0; ++it) {
     if (it > p.numNodes) {
       p.bad = true;
       break;
     }
-    const HeapItem cur = pq[0];
+    const HeapItem cur = pq.at(0);
     if (fadd(cur.cost, sarea) >= best_cost) break;
     heap_pop(pq, size);
     size--;
@@ -226,10 +246,12 @@ __device__ uint32_t find_node(const Patch &p, uint32_t n, HeapItem *pq, uint32_t
     induced = fadd(induced, total);
     if (fadd(induced, sarea) < best_cost && !cn.isLeafFlag) {
       if ((uint32_t)size + 2 <= cap) {
-        pq[size].node = cn.left;
-        pq[size].cost = induced;
-        pq[size + 1].node = cn.right;
-        pq[size + 1].cost = induced;
+        if (cn.left < p.numNodes) prefetch_node(p.t, cn.left);
+        if (cn.right < p.numNodes) prefetch_node(p.t, cn.right);
+        pq.at(size).node = cn.left;
+        pq.at(size).cost = induced;
+        pq.at(size + 1).node = cn.right;
+        pq.at(size + 1).cost = induced;
         heap_push(pq, size + 1);
         heap_push(pq, size + 2);
         size += 2;
@@ -271,7 +293,7 @@ __device__ bool remove_node(Patch &p, uint32_t x, uint32_t ins[2], uint32_t un[2
 }
 
 // reinsert (Bittner13CUDA.cu:308-358).
-__device__ bool reinsert(Patch &p, uint32_t x, uint32_t unused, bool update, HeapItem *pq, uint32_t cap,
+__device__ bool reinsert(Patch &p, uint32_t x, uint32_t unused, bool update, const Heap &pq, uint32_t cap,
                          SearchCounters &ctr) {
   const uint32_t best = find_node(p, x, pq, cap, ctr);
   if (best == p.root) return false;
@@ -332,6 +354,7 @@ __global__ void patch_kernel(const bvhgb_node *__restrict__ t, uint32_t root, co
                              uint32_t *__restrict__ toFix, uint32_t *__restrict__ owner, HeapItem *__restrict__ heaps,
                              uint32_t cap, unsigned long long *__restrict__ stats, uint32_t numNodes,
                              uint32_t *__restrict__ err) {
+  __shared__ HeapItem heapTop[kHeapShared * kSearchThreads];
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= chunkSize) return;
   const uint32_t pos = offsetAccess ? k * numChunks + chunk : chunk * chunkSize + k;
@@ -345,7 +368,7 @@ __global__ void patch_kernel(const bvhgb_node *__restrict__ t, uint32_t root, co
   uint32_t ins[2], un[2], g = kNone;
   bool ok = pos < numTodo;
   const uint32_t node = ok ? __ldg(todo + pos) : kNone;
-  HeapItem *pq = heaps + (size_t)k * cap;
+  const Heap pq{heapTop + (threadIdx.x & (kSearchThreads - 1)), heaps + (size_t)k * cap};
   ok = ok && remove_node(p, node, ins, un, g);
   ok = ok && reinsert(p, ins[0], un[0], true, pq, cap, ctr);
   ok = ok && reinsert(p, ins[1], un[1], false, pq, cap, ctr);
@@ -507,7 +530,10 @@ int run_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t c, cudaStrea
   const uint32_t grid = ceil_div(cs, bs);
   const bool prof = !ws->evStart.empty();
   if (prof) BVHGB_CUDA_TRY(record_event(ws->evStart[c], s));
-  patch_kernel<<<grid, bs, 0, s>>>(nodes, ws->root, ws->todo, ws->numInner, c, ws->numChunks, cs, ws->cfg.offsetAccess,
+  // One warp per block: the searches are latency-bound, so spreading them over more SMs beats
+  // packing them (CUDABlockSize only sizes the other kernels; results do not depend on it).
+  patch_kernel<<<ceil_div(cs, kSearchThreads), kSearchThreads, 0, s>>>(
+      nodes, ws->root, ws->todo, ws->numInner, c, ws->numChunks, cs, ws->cfg.offsetAccess,
                                    ws->patches, ws->valid, ws->toFix, ws->owner, ws->heaps, ws->cfg.heapCapacity,
                                    ws->stats, ws->numNodes, ws->err);
   BVHGB_LAUNCH_CHECK("bn13 patch");
