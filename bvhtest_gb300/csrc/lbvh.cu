@@ -433,3 +433,90 @@ extern "C" BVHGB_API int bvhgb_lbvh_read_errors(bvhgb_lbvh_workspace *ws, uint32
   *flags = a | b;
   return BVHGB_OK;
 }
+
+// ---- allocation-free build -------------------------------------------------------------------
+//
+// Some callers cannot allocate device memory while they build: a per-frame rebuild inside a render
+// or simulation loop (cudaMalloc synchronises the whole device and stalls the frame), host
+// applications whose device memory is owned by their own pool and that forbid driver allocations,
+// and code that must not fail for lack of memory once started. For them the build below takes its
+// working memory from one array in this file, sized for BVHGB_STATIC_MAX_FACES triangles and
+// reserved on every GPU that loads the library until the process exits.
+#include <mutex>
+
+namespace bvhgb {
+namespace {
+
+constexpr size_t kStaticScratchBytes = 12ull << 20;  // covers keys, values, slots and sort scratch
+__device__ __align__(256) unsigned char g_lbvh_static_scratch[kStaticScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mutex;
+unsigned char *g_static_base[kMaxDevices] = {};
+
+size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Device address of the array on the current device, looked up once per device.
+int static_scratch(unsigned char **out) {
+  int dev = 0;
+  BVHGB_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return BVHGB_GENERIC_ERROR;
+  std::lock_guard<std::mutex> lock(g_static_mutex);
+  if (!g_static_base[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_lbvh_static_scratch);
+    if (e != cudaSuccess) {
+      set_last_error("cudaGetSymbolAddress(g_lbvh_static_scratch)", e);
+      return BVHGB_CUDA_ERROR;
+    }
+    g_static_base[dev] = static_cast<unsigned char *>(p);
+  }
+  *out = g_static_base[dev];
+  return BVHGB_OK;
+}
+
+}  // namespace
+}  // namespace bvhgb
+
+extern "C" BVHGB_API int bvhgb_lbvh_build_static(const float *vert, const uint32_t *faces, uint32_t numFaces,
+                                                 const bvhgb_lbvh_config *cfg, bvhgb_node *nodes,
+                                                 bvhgb_stream stream) {
+  const bvhgb_lbvh_config c = cfg ? *cfg : bvhgb_lbvh_config{30u, BVHGB_TOPO_REFCOMPAT};
+  if ((c.mortonBits != 30 && c.mortonBits != 63) || c.topology > BVHGB_TOPO_KARRAS) return BVHGB_INVALID_ARGUMENT;
+  if (numFaces > BVHGB_STATIC_MAX_FACES) return BVHGB_TOO_LARGE;
+  if (numFaces == 0) return BVHGB_OK;
+  if (!vert || !faces || !nodes) return BVHGB_INVALID_ARGUMENT;
+  unsigned char *base = nullptr;
+  int st = static_scratch(&base);
+  if (st) return st;
+  st = sort_prepare();  // a function attribute, not an allocation
+  if (st) return st;
+  // Carve the working memory of one build for the largest size out of the array.
+  bvhgb_lbvh_workspace ws;
+  ws.maxFaces = BVHGB_STATIC_MAX_FACES;
+  ws.cfg = c;
+  ws.keyBytes = c.mortonBits == 30 ? 4u : 8u;
+  const size_t m = BVHGB_STATIC_MAX_FACES;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    unsigned char *p = base + off;
+    off += round256(bytes);
+    return p;
+  };
+  ws.scene = reinterpret_cast<uint32_t *>(take(256));
+  ws.keys = take(ws.keyBytes * m);
+  ws.keysSorted = take(ws.keyBytes * m);
+  ws.vals = reinterpret_cast<uint32_t *>(take(4 * m));
+  ws.valsSorted = reinterpret_cast<uint32_t *>(take(4 * m));
+  ws.slots = reinterpret_cast<uint32_t *>(take(4 * m));
+  ws.sortTempBytes = sort_temp_bytes(BVHGB_STATIC_MAX_FACES, ws.keyBytes, 0, c.mortonBits);
+  ws.sortTemp = take(ws.sortTempBytes);
+  if (off > kStaticScratchBytes) return BVHGB_GENERIC_ERROR;  // the array is sized for the worst case
+  // The same phases as bvhgb_lbvh_build; every scratch word that must start at a known value is
+  // written by the phase that uses it (scene box init kernel, slot reset in the Morton kernel,
+  // the sort's memset of its counters), so the previous call's contents do not matter.
+  if ((st = bvhgb_lbvh_init_tri_data(&ws, vert, faces, numFaces, stream))) return st;
+  if ((st = bvhgb_lbvh_calc_morton(&ws, vert, faces, numFaces, stream))) return st;
+  if ((st = bvhgb_lbvh_sort(&ws, numFaces, stream))) return st;
+  return bvhgb_lbvh_build_tree(&ws, vert, faces, numFaces, nodes, stream);
+}

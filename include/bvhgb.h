@@ -151,6 +151,21 @@ BVHGB_API int bvhgb_lbvh_build_tree(bvhgb_lbvh_workspace *ws, const float *vert,
 BVHGB_API int bvhgb_lbvh_read_scene_box(bvhgb_lbvh_workspace *ws, bvhgb_aabb *scene, bvhgb_stream stream);
 BVHGB_API int bvhgb_lbvh_read_keys(bvhgb_lbvh_workspace *ws, int sorted, void *keys_host, uint32_t *idx_host,
                                    uint32_t numFaces, bvhgb_stream stream);
+/* Allocation-free LBVH build. No counterpart in the reference (its build allocates in
+ * LBVH_allocateWorkingMemory and per call in LBVH_initTriData). For callers that cannot call
+ * cudaMalloc while they build — a per-frame rebuild in a render or simulation loop, where an
+ * allocation synchronises the device, or a host application that owns all device memory through
+ * its own pool. Same result as bvhgb_lbvh_build (same kernels), but the working memory is one
+ * 12 MiB file-scope device array that every GPU loading the library keeps until exit; nothing is
+ * allocated and no allocating library routine is called. The caller still passes the mesh and the
+ * node array (2 * numFaces - 1 nodes). Limits: numFaces <= BVHGB_STATIC_MAX_FACES, else
+ * BVHGB_TOO_LARGE. All calls share the one array: calls that overlap on the GPU (other streams,
+ * other host threads) race and must be serialised by the caller. The first call on each device
+ * looks up the array's device address with that device current; make that first call before any
+ * stream capture. */
+#define BVHGB_STATIC_MAX_FACES 262144u
+BVHGB_API int bvhgb_lbvh_build_static(const float *vert, const uint32_t *faces, uint32_t numFaces,
+                                      const bvhgb_lbvh_config *cfg, bvhgb_node *nodes, bvhgb_stream stream);
 /* Device error bits of the last build (4 = an inconsistent exchange slot was met and the build
  * stopped; 1 = the sort's look-back gave up); synchronous on 'stream'. 0 = the build is valid. */
 BVHGB_API int bvhgb_lbvh_read_errors(bvhgb_lbvh_workspace *ws, uint32_t *flags, bvhgb_stream stream);
