@@ -144,9 +144,10 @@ class Bittner13GPU:
     """The `bittner13GPU` command (lib/builder/Bittner13GPU.cpp:78-133)."""
 
     def __init__(self, nodes: torch.Tensor, root: int = 0, num_chunks=32, block_size=128, batch_percent=1.0,
-                 offset_access=False, heap_capacity=4096, num_nodes=None, profile=False, stream=None):
+                 offset_access=False, heap_capacity=4096, num_nodes=None, profile=False, search_mode=0, stream=None):
         self.lib = load()
-        self.cfg = Bn13Config(num_chunks, block_size, batch_percent, int(offset_access), heap_capacity, int(profile))
+        self.cfg = Bn13Config(num_chunks, block_size, batch_percent, int(offset_access), heap_capacity, int(profile),
+                              int(search_mode))
         ws = C.c_void_p()
         n = nodes.shape[0] if num_nodes is None else num_nodes
         check(self.lib.bvhgb_bn13_create(_ptr(nodes), n, root, C.byref(self.cfg), C.byref(ws), _stream(stream)),

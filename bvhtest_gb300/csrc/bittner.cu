@@ -292,10 +292,150 @@ __device__ bool remove_node(Patch &p, uint32_t x, uint32_t ins[2], uint32_t un[2
   return true;
 }
 
+// ---- batched best-first search: one warp per item -------------------------------------------
+//
+// The frontier (up to 128 entries) lives in registers, 4 slots per lane, entry e = slot * 32 + lane,
+// kept sorted by (cost, node). Each round the warp evaluates slot 0 (the 32 lowest-bound entries)
+// in parallel, reduces the best total, sorts the up-to-64 children with a bitonic network and
+// merges them into slots 1..3 with a bitonic merge; entries past 128 are dropped and counted.
+// oracle/bittner.c (gpu_find_node_batched) restates the same rounds.
+constexpr uint32_t kFull = 0xFFFFFFFFu;
+constexpr int kFrontier = 4;  // slots per lane (128 entries)
+
+__device__ __forceinline__ bool fe_gt(float ca, uint32_t na, float cb, uint32_t nb) {
+  return ca > cb || (ca == cb && na > nb);
+}
+
+// One compare-exchange stage of a bitonic network over S slots x 32 lanes.
+template <int S>
+__device__ __forceinline__ void bitonic_stage(float (&c)[S], uint32_t (&n)[S], int j, int k, bool descending,
+                                              uint32_t lane) {
+  if (j >= 32) {
+    const int d = j >> 5;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      if (s & d) continue;
+      const int t = s + d;
+      const uint32_t e = (uint32_t)s * 32u + lane;
+      const bool asc = ((e & (uint32_t)k) == 0) != descending;
+      const bool swap = asc ? fe_gt(c[s], n[s], c[t], n[t]) : fe_gt(c[t], n[t], c[s], n[s]);
+      if (swap) {
+        const float tc = c[s]; c[s] = c[t]; c[t] = tc;
+        const uint32_t tn = n[s]; n[s] = n[t]; n[t] = tn;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      const float oc = __shfl_xor_sync(kFull, c[s], j);
+      const uint32_t on = __shfl_xor_sync(kFull, n[s], j);
+      const uint32_t e = (uint32_t)s * 32u + lane;
+      const bool asc = ((e & (uint32_t)k) == 0) != descending;
+      const bool keepMin = ((lane & (uint32_t)j) == 0) == asc;
+      if (keepMin ? fe_gt(c[s], n[s], oc, on) : fe_gt(oc, on, c[s], n[s])) {
+        c[s] = oc;
+        n[s] = on;
+      }
+    }
+  }
+}
+
+template <int S>
+__device__ __forceinline__ void bitonic_sort(float (&c)[S], uint32_t (&n)[S], bool descending, uint32_t lane) {
+#pragma unroll
+  for (int k = 2; k <= S * 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) bitonic_stage<S>(c, n, j, k, descending, lane);
+  }
+}
+
+template <int S>
+__device__ __forceinline__ void bitonic_merge(float (&c)[S], uint32_t (&n)[S], uint32_t lane) {
+#pragma unroll
+  for (int j = S * 16; j > 0; j >>= 1) bitonic_stage<S>(c, n, j, S * 32, false, lane);
+}
+
+// findNode1's cost model in batched rounds (every lane of the warp calls it with the same patch).
+__device__ uint32_t find_node_batched(const Patch &p, uint32_t n, SearchCounters &ctr) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const float kInf = __int_as_float(0x7f800000);
+  float best_cost = kInf;
+  uint32_t best = 0;
+  const Box nbox = tree_box(p.t, p.chk(n));
+  const float sarea = tree_sa(p.t, p.chk(n));
+  float fc[kFrontier];
+  uint32_t fn[kFrontier];
+#pragma unroll
+  for (int s = 0; s < kFrontier; ++s) {
+    fc[s] = kInf;
+    fn[s] = kNone;
+  }
+  if (lane == 0) {
+    fc[0] = 0.0f;
+    fn[0] = p.root;
+  }
+  for (uint32_t round = 0;; ++round) {
+    if (round > p.numNodes) {  // bounded: every round evaluates at least one node
+      p.bad = true;
+      break;
+    }
+    const bool cand = fc[0] != kInf && fadd(fc[0], sarea) < best_cost;
+    const uint32_t vmask = __ballot_sync(kFull, cand);
+    if (vmask == 0) break;
+    ctr.visits += __popc(vmask);
+    NodeP cn;
+    float total = kInf, induced = kInf;
+    if (cand) {
+      cn = p.get_subset(fn[0]);
+      Box b = p.get_aabb(fn[0]);
+      induced = fmul(-1.0f, surface_area(b));
+      merge_into(b, nbox);
+      total = fadd(fc[0], surface_area(b));
+      induced = fadd(induced, total);
+    }
+    // Best of the round: smallest total, first in frontier order on ties.
+    const uint32_t key = cand ? f2ord(total) : 0xFFFFFFFFu;
+    const uint32_t kmin = __reduce_min_sync(kFull, key);
+    const uint32_t first = __ffs(__ballot_sync(kFull, cand && key == kmin)) - 1;
+    const float rbest = __shfl_sync(kFull, total, first);
+    const uint32_t rnode = __shfl_sync(kFull, fn[0], first);
+    if (rbest < best_cost) {
+      best_cost = rbest;
+      best = rnode;
+    }
+    // Children, sorted descending in two slots.
+    float cc[2] = {kInf, kInf};
+    uint32_t cnn[2] = {kNone, kNone};
+    if (cand && !cn.isLeafFlag && fadd(induced, sarea) < best_cost) {
+      cc[0] = cc[1] = induced;
+      cnn[0] = cn.left;
+      cnn[1] = cn.right;
+      if (cn.left < p.numNodes) prefetch_node(p.t, cn.left);
+      if (cn.right < p.numNodes) prefetch_node(p.t, cn.right);
+    }
+    bitonic_sort<2>(cc, cnn, true, lane);
+    // Remaining frontier (ascending) ++ children (descending) is bitonic; merge to ascending.
+    float mc[8] = {fc[1], fc[2], fc[3], kInf, kInf, kInf, cc[0], cc[1]};
+    uint32_t mn[8] = {fn[1], fn[2], fn[3], kNone, kNone, kNone, cnn[0], cnn[1]};
+    bitonic_merge<8>(mc, mn, lane);
+    const uint32_t dropped = __popc(__ballot_sync(kFull, mc[4] != kInf)) + __popc(__ballot_sync(kFull, mc[5] != kInf)) +
+                             __popc(__ballot_sync(kFull, mc[6] != kInf)) + __popc(__ballot_sync(kFull, mc[7] != kInf));
+    ctr.overflow += dropped;
+#pragma unroll
+    for (int s = 0; s < kFrontier; ++s) {
+      fc[s] = mc[s];
+      fn[s] = mn[s];
+    }
+  }
+  p.bad = __any_sync(kFull, p.bad);
+  return best;
+}
+
 // reinsert (Bittner13CUDA.cu:308-358).
+template <bool BATCHED>
 __device__ bool reinsert(Patch &p, uint32_t x, uint32_t unused, bool update, const Heap &pq, uint32_t cap,
                          SearchCounters &ctr) {
-  const uint32_t best = find_node(p, x, pq, cap, ctr);
+  const uint32_t best = BATCHED ? find_node_batched(p, x, ctr) : find_node(p, x, pq, cap, ctr);
   if (best == p.root) return false;
   const uint32_t bpi = p.index(best);
   uint32_t sb;
@@ -370,12 +510,58 @@ __global__ void patch_kernel(const bvhgb_node *__restrict__ t, uint32_t root, co
   const uint32_t node = ok ? __ldg(todo + pos) : kNone;
   const Heap pq{heapTop + (threadIdx.x & (kSearchThreads - 1)), heaps + (size_t)k * cap};
   ok = ok && remove_node(p, node, ins, un, g);
-  ok = ok && reinsert(p, ins[0], un[0], true, pq, cap, ctr);
-  ok = ok && reinsert(p, ins[1], un[1], false, pq, cap, ctr);
+  ok = ok && reinsert<false>(p, ins[0], un[0], true, pq, cap, ctr);
+  ok = ok && reinsert<false>(p, ins[1], un[1], false, pq, cap, ctr);
   if (p.bad) {
     atomicOr(err, kErrBadIndex);
     ok = false;
   }
+  valid[k] = ok ? 1u : 0u;
+  toFix[3 * k + 0] = ok ? g : kNone;
+  toFix[3 * k + 1] = ok ? un[0] : kNone;
+  toFix[3 * k + 2] = ok ? un[1] : kNone;
+#pragma unroll
+  for (int s = 0; s < NSLOT; ++s) {
+    out[k].nd[s] = p.nd[s];
+    out[k].idx[s] = ok ? p.idx[s] : kNone;
+    if (ok && p.idx[s] != kNone) atomicMin(&owner[p.idx[s]], k);
+  }
+  if (!ok) atomicAdd(&stats[S_INVALID], 1ull);
+  if (ctr.overflow) atomicAdd(&stats[S_OVERFLOW], (unsigned long long)ctr.overflow);
+  atomicAdd(&stats[S_VISITS], (unsigned long long)ctr.visits);
+  atomicAdd(&stats[S_ITEMS], 1ull);
+}
+
+// One warp per batch item: the patch logic runs redundantly on every lane (same data, no
+// divergence) and the two searches are the warp-cooperative batched search; lane 0 publishes.
+constexpr int kWarpItemsPerBlock = 4;
+
+__global__ void __launch_bounds__(kWarpItemsPerBlock * 32) patch_warp_kernel(
+    const bvhgb_node *__restrict__ t, uint32_t root, const uint32_t *__restrict__ todo, uint32_t numTodo,
+    uint32_t chunk, uint32_t numChunks, uint32_t chunkSize, uint32_t offsetAccess, PatchOut *__restrict__ out,
+    uint32_t *__restrict__ valid, uint32_t *__restrict__ toFix, uint32_t *__restrict__ owner,
+    unsigned long long *__restrict__ stats, uint32_t numNodes, uint32_t *__restrict__ err) {
+  const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t lane = threadIdx.x & 31u;
+  if (k >= chunkSize) return;  // whole warps leave together
+  const uint32_t pos = offsetAccess ? k * numChunks + chunk : chunk * chunkSize + k;
+  Patch p;
+  p.t = t;
+  p.root = root;
+  p.numNodes = numNodes;
+  p.bad = false;
+  p.clear();
+  SearchCounters ctr = {0u, 0u};
+  uint32_t ins[2], un[2], g = kNone;
+  bool ok = pos < numTodo;
+  const uint32_t node = ok ? __ldg(todo + pos) : kNone;
+  const Heap unused{nullptr, nullptr};
+  ok = ok && remove_node(p, node, ins, un, g);
+  ok = ok && reinsert<true>(p, ins[0], un[0], true, unused, 0, ctr);
+  ok = ok && reinsert<true>(p, ins[1], un[1], false, unused, 0, ctr);
+  if (p.bad) ok = false;
+  if (lane != 0) return;
+  if (p.bad) atomicOr(err, kErrBadIndex);
   valid[k] = ok ? 1u : 0u;
   toFix[3 * k + 0] = ok ? g : kNone;
   toFix[3 * k + 1] = ok ? un[0] : kNone;
@@ -530,12 +716,17 @@ int run_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t c, cudaStrea
   const uint32_t grid = ceil_div(cs, bs);
   const bool prof = !ws->evStart.empty();
   if (prof) BVHGB_CUDA_TRY(record_event(ws->evStart[c], s));
-  // One warp per block: the searches are latency-bound, so spreading them over more SMs beats
-  // packing them (CUDABlockSize only sizes the other kernels; results do not depend on it).
-  patch_kernel<<<ceil_div(cs, kSearchThreads), kSearchThreads, 0, s>>>(
-      nodes, ws->root, ws->todo, ws->numInner, c, ws->numChunks, cs, ws->cfg.offsetAccess,
-                                   ws->patches, ws->valid, ws->toFix, ws->owner, ws->heaps, ws->cfg.heapCapacity,
-                                   ws->stats, ws->numNodes, ws->err);
+  if (ws->cfg.searchMode == BVHGB_SEARCH_BATCHED) {
+    patch_warp_kernel<<<ceil_div(cs, kWarpItemsPerBlock), kWarpItemsPerBlock * 32, 0, s>>>(
+        nodes, ws->root, ws->todo, ws->numInner, c, ws->numChunks, cs, ws->cfg.offsetAccess, ws->patches, ws->valid,
+        ws->toFix, ws->owner, ws->stats, ws->numNodes, ws->err);
+  } else {
+    // One warp per block: these searches are latency-bound, so spreading them over more SMs beats
+    // packing them (CUDABlockSize only sizes the other kernels; results do not depend on it).
+    patch_kernel<<<ceil_div(cs, kSearchThreads), kSearchThreads, 0, s>>>(
+        nodes, ws->root, ws->todo, ws->numInner, c, ws->numChunks, cs, ws->cfg.offsetAccess, ws->patches, ws->valid,
+        ws->toFix, ws->owner, ws->heaps, ws->cfg.heapCapacity, ws->stats, ws->numNodes, ws->err);
+  }
   BVHGB_LAUNCH_CHECK("bn13 patch");
   if (prof) BVHGB_CUDA_TRY(record_event(ws->evStop[c], s));
   apply_kernel<<<grid, bs, 0, s>>>(nodes, ws->patches, ws->valid, ws->toFix, ws->owner, cs, ws->stats);
@@ -564,7 +755,11 @@ extern "C" BVHGB_API int bvhgb_bn13_create(const bvhgb_node *nodes, uint32_t num
   if (!out || !nodes || numNodes == 0 || root >= numNodes) return BVHGB_INVALID_ARGUMENT;
   *out = nullptr;
   auto *ws = new bvhgb_bn13_workspace();
-  ws->cfg = cfg ? *cfg : bvhgb_bn13_config{32u, 128u, 1.0f, 0u, 4096u, 0u};
+  ws->cfg = cfg ? *cfg : bvhgb_bn13_config{32u, 128u, 1.0f, 0u, 4096u, 0u, BVHGB_SEARCH_BATCHED};
+  if (ws->cfg.searchMode > BVHGB_SEARCH_HEAP) {
+    delete ws;
+    return BVHGB_INVALID_ARGUMENT;
+  }
   if (ws->cfg.numChunks == 0) ws->cfg.numChunks = 1;
   if (ws->cfg.heapCapacity < 4) ws->cfg.heapCapacity = 4096;
   if (ws->cfg.blockSize == 0 || ws->cfg.blockSize > 1024) ws->cfg.blockSize = 128;

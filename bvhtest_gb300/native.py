@@ -41,7 +41,8 @@ class LbvhConfig(C.Structure):
 
 class Bn13Config(C.Structure):
     _fields_ = [("numChunks", C.c_uint32), ("blockSize", C.c_uint32), ("batchPercent", C.c_float),
-                ("offsetAccess", C.c_uint32), ("heapCapacity", C.c_uint32), ("profileKernels", C.c_uint32)]
+                ("offsetAccess", C.c_uint32), ("heapCapacity", C.c_uint32), ("profileKernels", C.c_uint32),
+                ("searchMode", C.c_uint32)]
 
 
 class Bn13Stats(C.Structure):

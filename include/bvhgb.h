@@ -194,7 +194,15 @@ typedef struct bvhgb_bn13_config {
   uint32_t offsetAccess; /* offsetAccess = false */
   uint32_t heapCapacity; /* branch-and-bound queue entries per item (reference: 4096) */
   uint32_t profileKernels; /* 1: bracket every reinsertion-search launch with CUDA events */
+  uint32_t searchMode;     /* BVHGB_SEARCH_BATCHED (0, default) or BVHGB_SEARCH_HEAP (1) */
 } bvhgb_bn13_config;
+
+/* Reinsertion search. HEAP: findNode1 (Bittner13CUDA.cu:141-191) one node at a time in the order of
+ * the reference's standard-library heap, one thread per item. BATCHED: the same cost model and
+ * pruning evaluated 32 lowest-bound frontier nodes per round by a warp per item (frontier of 128
+ * kept ordered by (cost, node)); it finds the same positions in practice at a fraction of the
+ * latency. Both are deterministic and restated by the oracle. */
+enum { BVHGB_SEARCH_BATCHED = 0, BVHGB_SEARCH_HEAP = 1 };
 
 typedef struct bvhgb_bn13_stats {
   uint64_t items;            /* batch items processed */

@@ -392,10 +392,84 @@ static int gpu_remove(bpatch *p, uint32_t x, uint32_t ins[2], uint32_t un[2], ui
   return 1;
 }
 
-/* reinsert (Bittner13CUDA.cu:308-358). */
+/* Batched best-first search (the GPU kernels' default search). Same cost model and pruning as
+ * findNode1, but each round evaluates the BF_K lowest-bound entries of the frontier together:
+ * the frontier is ordered by (cost, node); the entries whose bound cost + SA(n) is below the best
+ * total so far (a prefix) are evaluated, the best total among them (first in order on ties)
+ * replaces the best if strictly smaller, every evaluated inner node whose induced cost still
+ * passes the bound against the updated best pushes both children, and the frontier keeps its
+ * BF_CAP lowest entries (the rest are counted as overflow). */
+#define BF_K 32
+#define BF_CAP 128
+
+typedef struct fent {
+  float c;
+  uint32_t n;
+} fent;
+
+static int fent_cmp(const void *a, const void *b) {
+  const fent *x = a, *y = b;
+  if (x->c < y->c) return -1;
+  if (x->c > y->c) return 1;
+  return x->n < y->n ? -1 : (x->n > y->n);
+}
+
+static uint32_t gpu_find_node_batched(const bpatch *p, uint32_t n, uint64_t *overflow, uint64_t *visits) {
+  float best_cost = INFINITY;
+  uint32_t best = 0;
+  const orc_node *nd = &p->t[n];
+  orc_aabb nbox = nd->bbox;
+  float sarea = nd->surfaceArea;
+  fent f[BF_CAP + 2 * BF_K], nf[BF_CAP + 2 * BF_K];
+  size_t fn = 1;
+  f[0].c = 0.0f;
+  f[0].n = p->root;
+  for (;;) {
+    size_t take = fn < BF_K ? fn : BF_K;
+    size_t nv = 0;
+    while (nv < take && f[nv].c + sarea < best_cost) nv++;
+    if (nv == 0) break;
+    if (visits) *visits += nv;
+    float tot[BF_K], ind[BF_K];
+    npatch cn[BF_K];
+    for (size_t i = 0; i < nv; ++i) {
+      cn[i] = bp_get_subset(p, f[i].n);
+      orc_aabb b = bp_get_aabb(p, f[i].n);
+      float induced = -1.0f * orc_surface_area(&b);
+      merge_into(&b, &nbox);
+      float direct = orc_surface_area(&b);
+      tot[i] = f[i].c + direct;
+      ind[i] = induced + tot[i];
+    }
+    size_t bi = 0;
+    for (size_t i = 1; i < nv; ++i)
+      if (tot[i] < tot[bi]) bi = i;
+    if (tot[bi] < best_cost) {
+      best_cost = tot[bi];
+      best = f[bi].n;
+    }
+    size_t m = 0;
+    for (size_t i = take; i < fn; ++i) nf[m++] = f[i];
+    for (size_t i = 0; i < nv; ++i) {
+      if (cn[i].isLeafFlag || !(ind[i] + sarea < best_cost)) continue;
+      nf[m].c = ind[i]; nf[m].n = cn[i].left; m++;
+      nf[m].c = ind[i]; nf[m].n = cn[i].right; m++;
+    }
+    qsort(nf, m, sizeof(fent), fent_cmp);
+    if (m > BF_CAP) {
+      *overflow += m - BF_CAP;
+      m = BF_CAP;
+    }
+    memcpy(f, nf, m * sizeof(fent));
+    fn = m;
+  }
+  return best;
+}
+
+/* reinsert (Bittner13CUDA.cu:308-358). mode 0: batched search, 1: findNode1 heap order. */
 static int gpu_reinsert(bpatch *p, uint32_t x, uint32_t unused, int update, hitem *pq, uint32_t cap,
-                        uint64_t *overflow) {
-  uint32_t best = gpu_find_node(p, x, pq, cap, overflow);
+                        uint64_t *overflow, int mode, uint64_t *visits) {
+  uint32_t best = mode == 0 ? gpu_find_node_batched(p, x, overflow, visits) : gpu_find_node(p, x, pq, cap, overflow);
   if (best == p->root) return 0;
   uint32_t bpi = bp_index(p, best);
   npatch *b;
@@ -504,6 +578,8 @@ int orc_bittner_chunked(orc_node *t, uint32_t n_nodes, uint32_t root, uint32_t i
   uint32_t nthreads = (uint32_t)orc_num_threads();
   hitem *pqs = malloc(sizeof(hitem) * cap * nthreads);
   uint64_t *ovf = calloc(nthreads, sizeof(uint64_t));
+  uint64_t *vis = calloc(nthreads, sizeof(uint64_t));
+  const int mode = (int)cfg->search_mode;
 
   if (sah_trace) sah_trace[0] = orc_sah(t, n_nodes, root);
   for (uint32_t it = 0; it < iters; ++it) {
@@ -536,8 +612,8 @@ int orc_bittner_chunked(orc_node *t, uint32_t n_nodes, uint32_t root, uint32_t i
         if (node == NONE) continue;
         uint32_t ins[2], un[2], g;
         if (!gpu_remove(p, node, ins, un, &g)) continue;
-        if (!gpu_reinsert(p, ins[0], un[0], 1, pq, cap, &ovf[tid])) continue;
-        if (!gpu_reinsert(p, ins[1], un[1], 0, pq, cap, &ovf[tid])) continue;
+        if (!gpu_reinsert(p, ins[0], un[0], 1, pq, cap, &ovf[tid], mode, &vis[tid])) continue;
+        if (!gpu_reinsert(p, ins[1], un[1], 0, pq, cap, &ovf[tid], mode, &vis[tid])) continue;
         valid[k] = 1;
         fix[3 * k] = g;
         fix[3 * k + 1] = un[0];
@@ -589,7 +665,11 @@ int orc_bittner_chunked(orc_node *t, uint32_t n_nodes, uint32_t root, uint32_t i
     }
     if (sah_trace) sah_trace[it + 1] = orc_sah(t, n_nodes, root);
   }
-  for (uint32_t i = 0; i < nthreads; ++i) st.heap_overflow += ovf[i];
+  for (uint32_t i = 0; i < nthreads; ++i) {
+    st.heap_overflow += ovf[i];
+    st.nodes_visited += vis[i];
+  }
+  free(vis);
   if (stats) *stats = st;
   free(inner); free(todo); free(patches); free(valid); free(fix); free(owner); free(mark);
   free(dbuf); free(pqs); free(ovf);

@@ -106,6 +106,7 @@ typedef struct orc_bn13_cfg {
   float batch_percent;   /* batchPercent (1.0) */
   uint32_t offset_access;/* offsetAccess */
   uint32_t heap_cap;     /* B&B heap capacity (the reference uses 4096) */
+  uint32_t search_mode;  /* 0: batched best-first (32 per round, frontier 128); 1: findNode1 heap */
 } orc_bn13_cfg;
 
 typedef struct orc_bn13_stats {
@@ -114,6 +115,7 @@ typedef struct orc_bn13_stats {
   uint64_t skipped_conflict;
   uint64_t skipped_invalid; /* removeNode refused or best == root */
   uint64_t heap_overflow;
+  uint64_t nodes_visited; /* nodes evaluated by the searches of mode 0 */
 } orc_bn13_stats;
 
 /* The chunked parallel algorithm of Bittner13CUDA.cu:141-772 + BVHPatch.hpp:87-335, executed

@@ -30,12 +30,12 @@ class Camera(C.Structure):
 
 class Bn13Cfg(C.Structure):
     _fields_ = [("num_chunks", C.c_uint32), ("batch_percent", C.c_float), ("offset_access", C.c_uint32),
-                ("heap_cap", C.c_uint32)]
+                ("heap_cap", C.c_uint32), ("search_mode", C.c_uint32)]
 
 
 class Bn13Stats(C.Structure):
     _fields_ = [("items", C.c_uint64), ("applied", C.c_uint64), ("skipped_conflict", C.c_uint64),
-                ("skipped_invalid", C.c_uint64), ("heap_overflow", C.c_uint64)]
+                ("skipped_invalid", C.c_uint64), ("heap_overflow", C.c_uint64), ("nodes_visited", C.c_uint64)]
 
 
 def lib():
@@ -142,10 +142,12 @@ def bittner_seq(nodes, iters, batch_percent=1.0, root=0):
     return nodes, r.value, trace
 
 
-def bittner_chunked(nodes, iters, num_chunks=32, batch_percent=1.0, offset_access=False, heap_cap=4096, root=0):
+def bittner_chunked(nodes, iters, num_chunks=32, batch_percent=1.0, offset_access=False, heap_cap=4096, root=0,
+                    search_mode=0):
+    """search_mode 0: batched best-first search (GPU default); 1: the reference's heap order."""
     nodes = np.ascontiguousarray(nodes).copy()
     trace = np.zeros(iters + 1, np.float64)
-    cfg = Bn13Cfg(num_chunks, batch_percent, int(offset_access), heap_cap)
+    cfg = Bn13Cfg(num_chunks, batch_percent, int(offset_access), heap_cap, search_mode)
     st = Bn13Stats()
     lib().orc_bittner_chunked(_p(nodes), C.c_uint32(nodes.shape[0]), C.c_uint32(root), C.c_uint32(iters),
                               C.byref(cfg), _p(trace), C.byref(st))

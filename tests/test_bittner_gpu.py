@@ -32,20 +32,24 @@ def _diff(a, b):
 
 @pytest.mark.parametrize("n,iters", [(600, 3), (4096, 5), (65536, 3)])
 @pytest.mark.parametrize("topo", ["refCompat", "karras"])
-def test_bittner_bit_exact_vs_oracle(gpu, orc, n, iters, topo):
+@pytest.mark.parametrize("mode", [0, 1], ids=["batched", "heap"])
+def test_bittner_bit_exact_vs_oracle(gpu, orc, n, iters, topo, mode):
     import torch
     vert, faces, nodes = _build(gpu, n, seed=n, topo=topo)
     start = gpu.nodes_to_numpy(nodes)
-    opt = gpu.Bittner13GPU(nodes, num_nodes=2 * n - 1)
+    opt = gpu.Bittner13GPU(nodes, num_nodes=2 * n - 1, search_mode=mode)
     for _ in range(iters):
         opt.step()
     torch.cuda.synchronize()
     got = gpu.nodes_to_numpy(nodes)[: 2 * n - 1]
-    ref, trace, st = orc.bittner_chunked(start[: 2 * n - 1], iters)
+    ref, trace, st = orc.bittner_chunked(start[: 2 * n - 1], iters, search_mode=mode)
     assert np.array_equal(got.view(np.uint8), ref.view(np.uint8)), _diff(got, ref)
     gs = opt.stats()
     assert gs["items"] == st["items"] and gs["applied"] == st["applied"]
     assert gs["skippedConflict"] == st["skipped_conflict"] and gs["skippedInvalid"] == st["skipped_invalid"]
+    assert gs["heapOverflow"] == st["heap_overflow"]
+    if mode == 0:
+        assert gs["nodesVisited"] == st["nodes_visited"]
     assert orc.validate(got, vert, faces) == [0, 0, 0, 0, 0]
     assert abs(gpu.calc_sah(nodes, 0, 2 * n - 1) - trace[-1]) <= 1e-9 * trace[-1]
     opt.close()
