@@ -374,6 +374,7 @@ __device__ uint32_t find_node_batched(const Patch &p, uint32_t n, SearchCounters
     fc[0] = 0.0f;
     fn[0] = p.root;
   }
+  uint32_t fsize = 1;  // finite frontier entries (warp-uniform)
   for (uint32_t round = 0;; ++round) {
     if (round > p.numNodes) {  // bounded: every round evaluates at least one node
       p.bad = true;
@@ -403,28 +404,68 @@ __device__ uint32_t find_node_batched(const Patch &p, uint32_t n, SearchCounters
       best_cost = rbest;
       best = rnode;
     }
-    // Children, sorted descending in two slots.
-    float cc[2] = {kInf, kInf};
-    uint32_t cnn[2] = {kNone, kNone};
-    if (cand && !cn.isLeafFlag && fadd(induced, sarea) < best_cost) {
-      cc[0] = cc[1] = induced;
-      cnn[0] = cn.left;
-      cnn[1] = cn.right;
+    const bool kids = cand && !cn.isLeafFlag && fadd(induced, sarea) < best_cost;
+    if (kids) {
       if (cn.left < p.numNodes) prefetch_node(p.t, cn.left);
       if (cn.right < p.numNodes) prefetch_node(p.t, cn.right);
     }
-    bitonic_sort<2>(cc, cnn, true, lane);
-    // Remaining frontier (ascending) ++ children (descending) is bitonic; merge to ascending.
-    float mc[8] = {fc[1], fc[2], fc[3], kInf, kInf, kInf, cc[0], cc[1]};
-    uint32_t mn[8] = {fn[1], fn[2], fn[3], kNone, kNone, kNone, cnn[0], cnn[1]};
-    bitonic_merge<8>(mc, mn, lane);
-    const uint32_t dropped = __popc(__ballot_sync(kFull, mc[4] != kInf)) + __popc(__ballot_sync(kFull, mc[5] != kInf)) +
-                             __popc(__ballot_sync(kFull, mc[6] != kInf)) + __popc(__ballot_sync(kFull, mc[7] != kInf));
-    ctr.overflow += dropped;
+    const uint32_t kmask = __ballot_sync(kFull, kids);
+    const uint32_t m = 2u * __popc(kmask);                 // children this round
+    const uint32_t rest = fsize - min(fsize, 32u);        // frontier entries left in slots 1..3
+    if (m == 0) {
+      // Nothing to insert: the remaining frontier is already in order, shift it down a slot.
 #pragma unroll
-    for (int s = 0; s < kFrontier; ++s) {
-      fc[s] = mc[s];
-      fn[s] = mn[s];
+      for (int s = 0; s + 1 < kFrontier; ++s) {
+        fc[s] = fc[s + 1];
+        fn[s] = fn[s + 1];
+      }
+      fc[kFrontier - 1] = kInf;
+      fn[kFrontier - 1] = kNone;
+      fsize = rest;
+    } else if (m <= 32) {
+      // Common case: gather the children into one slot (lane j takes child j), sort it
+      // descending and merge it with the remaining frontier; at most 128 entries, no overflow.
+      const uint32_t src = lane < m ? __fns(kmask, 0, (lane >> 1) + 1) : lane;
+      const float sc = __shfl_sync(kFull, induced, src);
+      const uint32_t sl = __shfl_sync(kFull, cn.left, src), sr = __shfl_sync(kFull, cn.right, src);
+      float c1[1] = {lane < m ? sc : kInf};
+      uint32_t n1[1] = {lane < m ? ((lane & 1) ? sr : sl) : kNone};
+      bitonic_sort<1>(c1, n1, true, lane);
+      if (rest <= 32) {
+        float mc[2] = {fc[1], c1[0]};
+        uint32_t mn[2] = {fn[1], n1[0]};
+        bitonic_merge<2>(mc, mn, lane);
+        fc[0] = mc[0]; fn[0] = mn[0];
+        fc[1] = mc[1]; fn[1] = mn[1];
+        fc[2] = fc[3] = kInf;
+        fn[2] = fn[3] = kNone;
+      } else {
+        float mc[4] = {fc[1], fc[2], fc[3], c1[0]};
+        uint32_t mn[4] = {fn[1], fn[2], fn[3], n1[0]};
+        bitonic_merge<4>(mc, mn, lane);
+#pragma unroll
+        for (int s = 0; s < kFrontier; ++s) {
+          fc[s] = mc[s];
+          fn[s] = mn[s];
+        }
+      }
+      fsize = rest + m;
+    } else {
+      // Wide round: sort all children (two slots) and merge into 256, keeping the lowest 128.
+      float cc[2] = {kids ? induced : kInf, kids ? induced : kInf};
+      uint32_t cnn[2] = {kids ? cn.left : kNone, kids ? cn.right : kNone};
+      bitonic_sort<2>(cc, cnn, true, lane);
+      float mc[8] = {fc[1], fc[2], fc[3], kInf, kInf, kInf, cc[0], cc[1]};
+      uint32_t mn[8] = {fn[1], fn[2], fn[3], kNone, kNone, kNone, cnn[0], cnn[1]};
+      bitonic_merge<8>(mc, mn, lane);
+#pragma unroll
+      for (int s = 0; s < kFrontier; ++s) {
+        fc[s] = mc[s];
+        fn[s] = mn[s];
+      }
+      const uint32_t total = rest + m;
+      ctr.overflow += total > 128u ? total - 128u : 0u;
+      fsize = min(total, 128u);
     }
   }
   p.bad = __any_sync(kFull, p.bad);
