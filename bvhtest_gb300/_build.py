@@ -47,6 +47,15 @@ def _cuda_lib_dir() -> str:
     return str(root / "lib64")
 
 
+def _cuda_include_dir() -> str:
+    root = Path(_nvcc()).resolve().parent.parent
+    for cand in (root / "include", root / "targets" / "sbsa-linux" / "include",
+                 root / "targets" / "x86_64-linux" / "include"):
+        if (cand / "cuda_runtime.h").exists():
+            return str(cand)
+    return str(root / "include")
+
+
 def _sources():
     cu = sorted(CSRC.glob("*.cu"))
     cpp = sorted(HOST.glob("*.cpp")) if HOST.exists() else []
@@ -90,7 +99,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
             continue
         out = OBJ / ("host_" + src.stem + ".o")
         host_lib_objs.append(out)
-        jobs.append(["g++", *CXX_FLAGS, "-c", str(src), "-o", str(out)])
+        jobs.append(["g++", *CXX_FLAGS, "-I" + _cuda_include_dir(), "-c", str(src), "-o", str(out)])
     with ThreadPoolExecutor(max_workers=max(2, min(len(jobs), os.cpu_count() or 4))) as ex:
         for res in ex.map(_run, jobs):
             if verbose and (res.stdout or res.stderr):

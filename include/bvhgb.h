@@ -300,6 +300,16 @@ BVHGB_API int bvhgb_fix_levels_host(bvhgb_node *nodes, uint32_t numNodes, uint32
 /* cudaDeviceSynchronize (LBVH_doCUDASyc, doCudaDevSync, tracerDoCudaSync). */
 BVHGB_API int bvhgb_device_sync(void);
 
+/* ---- command layer (lib/base/Command.*, Config.*, src/main.cpp) ------------------------------ */
+
+/* `bvhTest run CFG` (src/main.cpp:153-210): parse the JSON config, rewrite it with defaults, run
+ * every command for every input. Commands: load, generate, camImport, BVHExport, BVHImport,
+ * writeImg, writeData, copyToGPU, copyToHost, LBVH, bittner13GPU, CUDATracer, status, validate,
+ * sleep. Returns 0, or the ErrorCode of the command that stopped an input. */
+BVHGB_API int bvhgb_run_config(const char *path);
+/* The bvhTest command line (list | generate FILE CMDs | run CFG). */
+BVHGB_API int bvhgb_cli_main(int argc, char **argv);
+
 #ifdef __cplusplus
 }
 #endif
