@@ -192,6 +192,141 @@ class Bittner13GPU:
         check(self.lib.bvhgb_bn13_get_stats(self.ws, C.byref(st), _stream(stream)), "bvhgb_bn13_get_stats")
         return {k: getattr(st, k) for k, _ in Bn13Stats._fields_}
 
+    @property
+    def num_inner(self) -> int:
+        n = C.c_uint32()
+        check(self.lib.bvhgb_bn13_read_inner(self.ws, None, 0, C.byref(n), None), "bvhgb_bn13_read_inner")
+        return n.value
+
+    def inner_nodes(self, stream=None) -> torch.Tensor:
+        """The ascending inner-node list (int32, device copy)."""
+        n = self.num_inner
+        out = torch.empty(n, dtype=torch.int32, device="cuda")
+        check(self.lib.bvhgb_bn13_read_inner(self.ws, _ptr(out), n, None, _stream(stream)), "bvhgb_bn13_read_inner")
+        return out
+
+    def selection(self, stream=None) -> torch.Tensor:
+        """Node order of the most recent selection (int32, device copy, batch position order)."""
+        out = torch.empty(self.num_inner, dtype=torch.int32, device="cuda")
+        check(self.lib.bvhgb_bn13_read_selection(self.ws, _ptr(out), out.shape[0], _stream(stream)),
+              "bvhgb_bn13_read_selection")
+        return out
+
+    def select(self, stream=None):
+        check(self.lib.bvhgb_bn13_select_nodes(self.ws, _ptr(self.nodes), _stream(stream)), "bvhgb_bn13_select_nodes")
+
+    def chunk(self, c: int, stream=None):
+        check(self.lib.bvhgb_bn13_chunk(self.ws, _ptr(self.nodes), c, _stream(stream)), "bvhgb_bn13_chunk")
+
+    def gains(self, cand: torch.Tensor, with_target=False, stream=None):
+        """Realised SAH reduction of reinserting each candidate alone (and the training target)."""
+        cand = cand.to(device="cuda", dtype=torch.int32).contiguous()
+        gain = torch.empty(cand.shape[0], dtype=torch.float32, device="cuda")
+        tgt = torch.empty_like(gain) if with_target else None
+        check(self.lib.bvhgb_bn13_gains(self.ws, _ptr(self.nodes), _ptr(cand), cand.shape[0], _ptr(gain), _ptr(tgt),
+                                        _stream(stream)), "bvhgb_bn13_gains")
+        return (gain, tgt) if with_target else gain
+
+    def set_scorer(self, scorer: "Mlp | None"):
+        """Learned selection with 'scorer' (kept referenced here), or the plain measure for None."""
+        check(self.lib.bvhgb_bn13_set_scorer(self.ws, scorer.handle if scorer is not None else None),
+              "bvhgb_bn13_set_scorer")
+        self._scorer = scorer
+
+
+MLP_PARAMS = 5825
+LR_FEATURES = 24
+
+
+class Mlp:
+    """The learned reinsertion scorer (bvhgb_mlp_*): 24 -> 64 -> 64 -> 1 GELU, BF16 compute."""
+
+    def __init__(self, seed: int = 0, params=None):
+        self.lib = load()
+        h = C.c_void_p()
+        check(self.lib.bvhgb_mlp_create(seed, C.byref(h)), "bvhgb_mlp_create")
+        self.handle = h
+        if params is not None:
+            self.set_params(params)
+
+    def close(self):
+        if self.handle:
+            self.lib.bvhgb_mlp_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(MLP_PARAMS, np.float32)
+        check(self.lib.bvhgb_mlp_get_params(self.handle, out.ctypes.data_as(C.c_void_p)), "bvhgb_mlp_get_params")
+        return out
+
+    def set_params(self, params):
+        a = np.ascontiguousarray(params, dtype=np.float32)
+        assert a.shape == (MLP_PARAMS,)
+        check(self.lib.bvhgb_mlp_set_params(self.handle, a.ctypes.data_as(C.c_void_p)), "bvhgb_mlp_set_params")
+
+    def forward(self, x: torch.Tensor, stream=None) -> torch.Tensor:
+        """x: [n, 24] bfloat16 device rows -> float32 [n]."""
+        x = x.contiguous()
+        assert x.dtype == torch.bfloat16 and x.shape[1] == LR_FEATURES
+        y = torch.empty(x.shape[0], dtype=torch.float32, device="cuda")
+        check(self.lib.bvhgb_mlp_forward(self.handle, _ptr(x), x.shape[0], _ptr(y), _stream(stream)),
+              "bvhgb_mlp_forward")
+        return y
+
+    def gradient(self, x: torch.Tensor, t: torch.Tensor, stream=None):
+        """(gradient [5825] float32 numpy, loss) of the mean squared error over all rows."""
+        x, t = x.contiguous(), t.to(torch.float32).contiguous()
+        g = np.zeros(MLP_PARAMS, np.float32)
+        loss = C.c_float()
+        check(self.lib.bvhgb_mlp_gradient(self.handle, _ptr(x), _ptr(t), x.shape[0], g.ctypes.data_as(C.c_void_p),
+                                          C.byref(loss), _stream(stream)), "bvhgb_mlp_gradient")
+        return g, loss.value
+
+    def train(self, x: torch.Tensor, t: torch.Tensor, steps: int, batch=8192, lr=1e-3, weight_decay=1e-4, seed=0,
+              stream=None, with_loss=True):
+        x, t = x.contiguous(), t.to(torch.float32).contiguous()
+        hist = np.zeros(max(steps, 1), np.float32) if with_loss else None
+        check(self.lib.bvhgb_mlp_train(self.handle, _ptr(x), _ptr(t), x.shape[0], batch, steps, lr, weight_decay, seed,
+                                       hist.ctypes.data_as(C.c_void_p) if hist is not None else None,
+                                       _stream(stream)), "bvhgb_mlp_train")
+        return hist[:steps] if hist is not None else None
+
+
+class LrFeatures:
+    """Feature rows of the learned scorer (bvhgb_lr_features_*)."""
+
+    def __init__(self, max_nodes: int):
+        self.lib = load()
+        h = C.c_void_p()
+        check(self.lib.bvhgb_lr_features_create(max_nodes, C.byref(h)), "bvhgb_lr_features_create")
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            self.lib.bvhgb_lr_features_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __call__(self, nodes: torch.Tensor, inner: torch.Tensor, root=0, num_nodes=None, stream=None) -> torch.Tensor:
+        n = nodes.shape[0] if num_nodes is None else num_nodes
+        inner = inner.to(device="cuda", dtype=torch.int32).contiguous()
+        x = torch.empty((inner.shape[0], LR_FEATURES), dtype=torch.bfloat16, device="cuda")
+        num_leaves = n - inner.shape[0]
+        check(self.lib.bvhgb_lr_features(self.handle, _ptr(nodes), n, root, _ptr(inner), inner.shape[0], num_leaves,
+                                         _ptr(x), _stream(stream)), "bvhgb_lr_features")
+        return x
+
 
 def make_camera(pos, lookAt, up, fov, width, height) -> Camera:
     return Camera((C.c_float * 3)(*pos), (C.c_float * 3)(*lookAt), (C.c_float * 3)(*up), float(fov), int(width),

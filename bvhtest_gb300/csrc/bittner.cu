@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "learned.cuh"
 #include "sort.cuh"
 
 namespace bvhgb {
@@ -705,6 +706,139 @@ __global__ void refit_kernel(bvhgb_node *t, uint32_t root, const uint32_t *__res
   }
 }
 
+// ---- isolated realised gain of one reinsertion (the learned scorer's training label) -----------
+// The patch changes the children of three nodes: the grand parent (its child becomes the sibling)
+// and the two reused nodes. A box changes iff its node lies on a path from one of them to the root
+// in the patched tree, so the SAH reduction (cInner = 1) is the sum of old minus new surface area
+// over the union of the three paths, over the root's area. Path 1 (first reused node) meets path 0
+// (grand parent) at J1 = lca(s1, s0); path 2 meets path 0 or the private part of path 1 at J2, the
+// deeper of lca(s2, s0) and lca(s2, s1). Boxes are rebuilt bottom-up in the order: private part of
+// path 2, private part of path 1, path 0 through the root; a child's new box is the running box of
+// the walk, the last box of a private part at its join node, or its unchanged box. Sums in double
+// in that order.
+struct GainWalk {
+  uint32_t prev, last1, j1, last2, j2;
+  Box prevbox, box1, box2;
+};
+
+__device__ __forceinline__ uint32_t new_parent(const Patch &p, uint32_t x) { return p.get(x).parent; }
+
+__device__ bool new_depth(const Patch &p, uint32_t x, uint32_t &d) {
+  uint32_t k = 0;
+  while (x != p.root) {
+    if (x >= p.numNodes || k > p.numNodes) return false;
+    x = new_parent(p, x);
+    ++k;
+  }
+  d = k;
+  return true;
+}
+
+__device__ uint32_t new_lca(const Patch &p, uint32_t a, uint32_t da, uint32_t b, uint32_t db, uint32_t &dout) {
+  while (da > db) { a = new_parent(p, a); --da; }
+  while (db > da) { b = new_parent(p, b); --db; }
+  while (a != b && da > 0) { a = new_parent(p, a); b = new_parent(p, b); --da; }
+  dout = da;
+  return a;
+}
+
+__device__ __forceinline__ Box child_box(const Patch &p, const GainWalk &w, uint32_t x, uint32_t c) {
+  if (c == w.prev) return w.prevbox;
+  if (x == w.j1 && c == w.last1) return w.box1;
+  if (x == w.j2 && c == w.last2) return w.box2;
+  return tree_box(p.t, c);
+}
+
+__device__ void gain_walk(const Patch &p, GainWalk &w, uint32_t x, uint32_t stop, double &acc, bool &ok) {
+  w.prev = kNone;
+  for (uint32_t k = 0; x != stop; ++k) {
+    if (x >= p.numNodes || k > p.numNodes) {
+      ok = false;
+      return;
+    }
+    const NodeP n = p.get(x);
+    if (n.left >= p.numNodes || n.right >= p.numNodes) {
+      ok = false;
+      return;
+    }
+    Box b = child_box(p, w, x, n.left);
+    const Box rb = child_box(p, w, x, n.right);
+    merge_into(b, rb);
+    acc = __dadd_rn(acc, __dsub_rn((double)tree_sa(p.t, x), (double)surface_area(b)));
+    w.prev = x;
+    w.prevbox = b;
+    if (x == p.root) return;
+    x = n.parent;
+  }
+}
+
+__device__ float isolated_gain(const Patch &p, uint32_t s0, uint32_t s1, uint32_t s2, bool &ok) {
+  uint32_t d0, d1, d2, dj1, d20, d21;
+  if (!new_depth(p, s0, d0) || !new_depth(p, s1, d1) || !new_depth(p, s2, d2)) {
+    ok = false;
+    return 0.0f;
+  }
+  const uint32_t j1 = new_lca(p, s1, d1, s0, d0, dj1);
+  const uint32_t l20 = new_lca(p, s2, d2, s0, d0, d20);
+  const uint32_t l21 = new_lca(p, s2, d2, s1, d1, d21);
+  const uint32_t j2 = d20 >= d21 ? l20 : l21;
+  GainWalk w;
+  w.last1 = w.j1 = w.last2 = w.j2 = kNone;
+  w.prevbox = w.box1 = w.box2 = Box{};
+  double acc = 0.0;
+  gain_walk(p, w, s2, j2, acc, ok);
+  w.last2 = w.prev;
+  w.box2 = w.prevbox;
+  w.j2 = j2;
+  gain_walk(p, w, s1, j1, acc, ok);
+  w.last1 = w.prev;
+  w.box1 = w.prevbox;
+  w.j1 = j1;
+  gain_walk(p, w, s0, kNone, acc, ok);
+  if (!ok) return 0.0f;
+  return __double2float_rn(__ddiv_rn(acc, (double)tree_sa(p.t, p.root)));
+}
+
+// One warp per candidate: the optimizer's removal and batched reinsertion searches against the
+// unmodified tree, then the isolated gain; lane 0 writes. Nothing is applied.
+__global__ void __launch_bounds__(kWarpItemsPerBlock * 32) gain_warp_kernel(
+    const bvhgb_node *__restrict__ t, uint32_t root, const uint32_t *__restrict__ cand, uint32_t n, uint32_t numNodes,
+    float *__restrict__ gain, float *__restrict__ target, uint32_t *__restrict__ err) {
+  const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t lane = threadIdx.x & 31u;
+  if (k >= n) return;  // whole warps leave together
+  Patch p;
+  p.t = t;
+  p.root = root;
+  p.numNodes = numNodes;
+  p.bad = false;
+  p.clear();
+  SearchCounters ctr = {0u, 0u};
+  uint32_t ins[2], un[2], g = kNone;
+  const uint32_t x = __ldg(cand + k);
+  const Heap unused{nullptr, nullptr};
+  bool ok = x < numNodes;
+  ok = ok && remove_node(p, x, ins, un, g);
+  ok = ok && reinsert<true>(p, ins[0], un[0], true, unused, 0, ctr);
+  ok = ok && reinsert<true>(p, ins[1], un[1], false, unused, 0, ctr);
+  if (p.bad) ok = false;
+  float v = 0.0f;
+  if (ok) v = isolated_gain(p, g, un[0], un[1], ok);
+  if (p.bad) ok = false;
+  if (lane != 0) return;
+  if (p.bad) atomicOr(err, kErrBadIndex);
+  if (!ok) v = 0.0f;
+  gain[k] = v;
+  if (target) {
+    float tv = 0.0f;
+    if (x < numNodes) {
+      const float rel = fdiv(tree_sa(t, x), tree_sa(t, root));
+      if (rel > 0.0f) tv = fminf(fmaxf(fdiv(v, rel), -kTargetClip), kTargetClip);
+    }
+    target[k] = tv;
+  }
+}
+
 __global__ void init_inner_kernel(const bvhgb_node *__restrict__ t, uint32_t n, uint32_t *__restrict__ flag) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     flag[i] = __ldg(&t[i].isLeafFlag) == 0 ? 1u : 0u;
@@ -728,15 +862,24 @@ struct bvhgb_bn13_workspace {
   bvhgb_node *graphNodes = nullptr;
   uint32_t launchesPerIteration = 0;
   std::vector<cudaEvent_t> evStart, evStop;  // per chunk, profileKernels only
+  const bvhgb_mlp *scorer = nullptr;         // learned selection when set
+  LrScratch lr;                              // feature scratch, allocated with the first scorer
 };
 
 namespace {
 
 int select_nodes(bvhgb_bn13_workspace *ws, const bvhgb_node *nodes, cudaStream_t s) {
   if (ws->numInner == 0) return BVHGB_OK;
-  const uint32_t grid = min(ceil_div(ws->numInner, 256), (uint32_t)sm_count() * 8);
-  cost_kernel<<<grid, 256, 0, s>>>(nodes, ws->inner, ws->numInner, ws->keys, ws->vals);
-  BVHGB_LAUNCH_CHECK("bn13 cost");
+  if (ws->scorer) {
+    const uint32_t numLeaves = ws->numNodes - ws->numInner;
+    int st = lr_features(ws->lr, nodes, ws->numNodes, ws->root, ws->inner, ws->numInner, lr_inv_log2_leaves(numLeaves), s);
+    if (!st) st = lr_score_keys(ws->scorer, ws->lr, nodes, ws->root, ws->inner, ws->numInner, ws->keys, ws->vals, s);
+    if (st) return st;
+  } else {
+    const uint32_t grid = min(ceil_div(ws->numInner, 256), (uint32_t)sm_count() * 8);
+    cost_kernel<<<grid, 256, 0, s>>>(nodes, ws->inner, ws->numInner, ws->keys, ws->vals);
+    BVHGB_LAUNCH_CHECK("bn13 cost");
+  }
   return sort_pairs(ws->sortTemp, ws->keys, ws->keysSorted, ws->vals, ws->todo, ws->numInner, 4, 0, 32, s);
 }
 
@@ -899,6 +1042,7 @@ extern "C" BVHGB_API int bvhgb_bn13_destroy(bvhgb_bn13_workspace *ws) {
   cudaFree(ws->err);
   cudaFree(ws->heaps);
   cudaFree(ws->stats);
+  lr_scratch_free(ws->lr);
   delete ws;
   return BVHGB_OK;
 }
@@ -999,4 +1143,49 @@ extern "C" BVHGB_API int bvhgb_bn13_get_stats(bvhgb_bn13_workspace *ws, bvhgb_bn
   stats->heapOverflow = h[S_OVERFLOW];
   stats->nodesVisited = h[S_VISITS];
   return err ? BVHGB_BVH_ERROR : BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_bn13_gains(bvhgb_bn13_workspace *ws, const bvhgb_node *nodes, const uint32_t *cand,
+                                         uint32_t n, float *gain, float *target, bvhgb_stream stream) {
+  if (!ws || !nodes || (n && (!cand || !gain))) return BVHGB_INVALID_ARGUMENT;
+  if (n == 0) return BVHGB_OK;
+  gain_warp_kernel<<<ceil_div(n, kWarpItemsPerBlock), kWarpItemsPerBlock * 32, 0, as_stream(stream)>>>(
+      nodes, ws->root, cand, n, ws->numNodes, gain, target, ws->err);
+  BVHGB_LAUNCH_CHECK("bn13 gains");
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_bn13_read_inner(const bvhgb_bn13_workspace *ws, uint32_t *out, uint32_t capacity,
+                                              uint32_t *numInner, bvhgb_stream stream) {
+  if (!ws) return BVHGB_INVALID_ARGUMENT;
+  if (numInner) *numInner = ws->numInner;
+  if (!out) return BVHGB_OK;
+  if (capacity < ws->numInner) return BVHGB_TOO_LARGE;
+  if (ws->numInner)
+    BVHGB_CUDA_TRY(cudaMemcpyAsync(out, ws->inner, 4ull * ws->numInner, cudaMemcpyDeviceToDevice, as_stream(stream)));
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_bn13_set_scorer(bvhgb_bn13_workspace *ws, const bvhgb_mlp *scorer) {
+  if (!ws) return BVHGB_INVALID_ARGUMENT;
+  if (scorer && ws->lr.numNodes < ws->numNodes) {
+    const int st = lr_scratch_alloc(ws->lr, ws->numNodes);
+    if (st) return st;
+  }
+  if (ws->scorer != scorer && ws->graph) {
+    cudaGraphExecDestroy(ws->graph);
+    ws->graph = nullptr;
+    ws->graphNodes = nullptr;
+  }
+  ws->scorer = scorer;
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_bn13_read_selection(const bvhgb_bn13_workspace *ws, uint32_t *out, uint32_t capacity,
+                                                  bvhgb_stream stream) {
+  if (!ws || !out) return BVHGB_INVALID_ARGUMENT;
+  if (capacity < ws->numInner) return BVHGB_TOO_LARGE;
+  if (ws->numInner)
+    BVHGB_CUDA_TRY(cudaMemcpyAsync(out, ws->todo, 4ull * ws->numInner, cudaMemcpyDeviceToDevice, as_stream(stream)));
+  return BVHGB_OK;
 }

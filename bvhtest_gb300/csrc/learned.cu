@@ -1,0 +1,743 @@
+// Learned reinsertion scorer: node features, the 24 -> 64 -> 64 -> 1 GELU MLP (BF16 weights,
+// inputs and activations, FP32 accumulation) and its training kernels. The reference has no learned
+// part; its node selection is the inefficiency of lib/builder/Bittner13CUDA.cu:480-500, which stays
+// the default (bittner.cu) and judges the scorer through the SAH it reaches.
+//
+// Layout in HBM: feature rows are 24 BF16 values (48 bytes, three 16-byte words) per inner node in
+// the order of the optimizer's ascending inner-node list; parameters are one FP32 master array of
+// 5825 values plus its BF16 copy, AdamW moments beside them.
+//
+// GELU is the tanh approximation of Hendrycks and Gimpel, 0.5 z (1 + tanh(sqrt(2/pi)(z + 0.044715 z^3))).
+// Backward passes the BF16 rounding of weights and activations through as identity.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "learned.cuh"
+
+namespace bvhgb {
+namespace {
+
+constexpr int kIn = kMlpIn, kH = kMlpHidden;
+constexpr int oW1 = 0, oB1 = oW1 + kH * kIn, oW2 = oB1 + kH, oB2 = oW2 + kH * kH, oW3 = oB2 + kH, oB3 = oW3 + kH;
+static_assert(oB3 + 1 == kMlpParams, "parameter layout");
+constexpr int kWPad = (kMlpParams + 3) & ~3;
+
+constexpr float kGeluC = 0.7978845608028654f;  // sqrt(2 / pi)
+constexpr float kGeluA = 0.044715f;
+
+__device__ __forceinline__ float gelu(float z) {
+  const float u = kGeluC * (z + kGeluA * z * z * z);
+  return 0.5f * z * (1.0f + tanhf(u));
+}
+__device__ __forceinline__ float gelu_grad(float z) {
+  const float u = kGeluC * (z + kGeluA * z * z * z);
+  const float t = tanhf(u);
+  return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * kGeluC * (1.0f + 3.0f * kGeluA * z * z);
+}
+__device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+__device__ __forceinline__ void load_row(const uint16_t *__restrict__ x, size_t row, float in[kIn]) {
+  const uint4 *p = reinterpret_cast<const uint4 *>(x + row * kIn);
+#pragma unroll
+  for (int w = 0; w < 3; ++w) {
+    const uint4 v = __ldg(p + w);
+    const uint32_t u[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      in[w * 8 + h * 2 + 0] = __uint_as_float(u[h] << 16);
+      in[w * 8 + h * 2 + 1] = __uint_as_float(u[h] & 0xFFFF0000u);
+    }
+  }
+}
+
+__device__ __forceinline__ void load_weights(const __nv_bfloat16 *__restrict__ w, float *W) {
+  for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) W[i] = __bfloat162float(w[i]);
+}
+
+// One sample through the network with weights W (FP32 copies of the BF16 values) in shared memory.
+__device__ __forceinline__ float mlp_eval(const float *W, const float in[kIn]) {
+  float a1[kH];  // fully unrolled so that it stays in registers
+#pragma unroll
+  for (int j = 0; j < kH; ++j) {
+    float z = W[oB1 + j];
+#pragma unroll
+    for (int k = 0; k < kIn; ++k) z += W[oW1 + j * kIn + k] * in[k];
+    a1[j] = bf16r(gelu(z));
+  }
+  float out = W[oB3];
+  for (int j = 0; j < kH; ++j) {
+    float z = W[oB2 + j];
+#pragma unroll
+    for (int i = 0; i < kH; ++i) z += W[oW2 + j * kH + i] * a1[i];
+    out += W[oW3 + j] * bf16r(gelu(z));
+  }
+  return out;
+}
+
+// Inference; with KEYS the selection keys of the optimizer are written as well.
+template <bool KEYS>
+__global__ void __launch_bounds__(256) mlp_forward_kernel(const __nv_bfloat16 *__restrict__ w,
+                                                          const uint16_t *__restrict__ x, uint32_t n,
+                                                          float *__restrict__ y, const bvhgb_node *__restrict__ t,
+                                                          uint32_t root, const uint32_t *__restrict__ inner,
+                                                          uint32_t *__restrict__ keys, uint32_t *__restrict__ vals) {
+  __shared__ float W[kWPad];
+  load_weights(w, W);
+  __syncthreads();
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    float in[kIn];
+    load_row(x, s, in);
+    const float out = mlp_eval(W, in);
+    y[s] = out;
+    if (KEYS) {
+      const uint32_t node = __ldg(inner + s);
+      const float rel = fdiv(__ldg(&t[node].surfaceArea), __ldg(&t[root].surfaceArea));
+      keys[s] = ~f2ord(fmul(out, rel));
+      vals[s] = node;
+    }
+  }
+}
+
+// Forward + backward of one tile of kTile samples per block (one thread per sample). Gradients of
+// loss = sum (y - t)^2 / scaleN are added to grad (FP32); the tile's loss to loss[slot].
+constexpr int kTile = 128;
+constexpr int kStride = kTile + 1;  // [unit][sample] arrays padded against bank conflicts
+constexpr size_t kTrainSmem = sizeof(float) * (kWPad + kIn * kStride + 3 * kH * kStride + kTile);
+
+__global__ void __launch_bounds__(kTile) mlp_train_kernel(const __nv_bfloat16 *__restrict__ w,
+                                                          const uint16_t *__restrict__ x, const float *__restrict__ tgt,
+                                                          const uint32_t *__restrict__ index, uint32_t n, float scaleN,
+                                                          float *__restrict__ grad, float *__restrict__ lossBase,
+                                                          const uint32_t *__restrict__ stepDev, uint32_t step0,
+                                                          uint32_t lossCap) {
+  extern __shared__ __align__(16) float sm[];
+  float *W = sm;
+  float *X = W + kWPad;
+  float *Z1 = X + kIn * kStride;  // pre-activations of layer 1, later their gradients
+  float *A1 = Z1 + kH * kStride;
+  float *Z2 = A1 + kH * kStride;  // pre-activations of layer 2, later their gradients
+  float *dY = Z2 + kH * kStride;
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const uint32_t s = blockIdx.x * kTile + tid;
+  const bool live = s < n;
+  const uint32_t row = live ? (index ? __ldg(index + s) : s) : 0u;
+  load_weights(w, W);
+  {
+    float in[kIn];
+    if (live) load_row(x, row, in);
+#pragma unroll
+    for (int k = 0; k < kIn; ++k) X[k * kStride + tid] = live ? in[k] : 0.0f;
+  }
+  __syncthreads();
+  // forward, one column per thread
+  for (int j = 0; j < kH; ++j) {
+    float z = W[oB1 + j];
+#pragma unroll
+    for (int k = 0; k < kIn; ++k) z += W[oW1 + j * kIn + k] * X[k * kStride + tid];
+    Z1[j * kStride + tid] = z;
+    A1[j * kStride + tid] = bf16r(gelu(z));
+  }
+  float yv = W[oB3];
+  for (int j = 0; j < kH; ++j) {
+    float z = W[oB2 + j];
+#pragma unroll 16
+    for (int i = 0; i < kH; ++i) z += W[oW2 + j * kH + i] * A1[i * kStride + tid];
+    Z2[j * kStride + tid] = z;
+    yv += W[oW3 + j] * bf16r(gelu(z));
+  }
+  const float diff = live ? yv - __ldg(tgt + row) : 0.0f;
+  const float dy = 2.0f * diff / scaleN;
+  dY[tid] = dy;
+  float l = diff * diff / scaleN;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xFFFFFFFFu, l, o);
+  if (lane == 0) {
+    uint32_t slot = 0;
+    if (stepDev) slot = *stepDev - step0;
+    if (slot < lossCap) atomicAdd(lossBase + slot, l);
+  }
+  __syncthreads();
+  // dW3[j] = sum_q dY[q] A2[j][q], db3 = sum_q dY[q] (warp per output unit, lanes over samples)
+  for (int j = warp; j < kH; j += kTile / 32) {
+    float g = 0.0f;
+    for (int q = lane; q < kTile; q += 32) g += dY[q] * bf16r(gelu(Z2[j * kStride + q]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xFFFFFFFFu, g, o);
+    if (lane == 0) atomicAdd(grad + oW3 + j, g);
+  }
+  if (warp == 0) {
+    float g = 0.0f;
+    for (int q = lane; q < kTile; q += 32) g += dY[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xFFFFFFFFu, g, o);
+    if (lane == 0) atomicAdd(grad + oB3, g);
+  }
+  __syncthreads();
+  // dZ2 = dY W3 gelu'(Z2); dZ1 = (W2^T dZ2) gelu'(Z1), one column per thread
+  for (int j = 0; j < kH; ++j) Z2[j * kStride + tid] = dy * W[oW3 + j] * gelu_grad(Z2[j * kStride + tid]);
+  for (int i = 0; i < kH; ++i) {
+    float da = 0.0f;
+#pragma unroll 16
+    for (int j = 0; j < kH; ++j) da += W[oW2 + j * kH + i] * Z2[j * kStride + tid];
+    Z1[i * kStride + tid] = da * gelu_grad(Z1[i * kStride + tid]);
+  }
+  __syncthreads();
+  // weight gradients reduced over the tile: warp per output unit j, lanes over the inputs
+  for (int j = warp; j < kH; j += kTile / 32) {
+    const float *dz2 = Z2 + j * kStride, *dz1 = Z1 + j * kStride;
+    float g2a = 0.0f, g2b = 0.0f, g1 = 0.0f;
+    const float *a1a = A1 + lane * kStride, *a1b = A1 + (lane + 32) * kStride;
+    const float *xk = X + (lane < (uint32_t)kIn ? lane : 0u) * kStride;
+    for (int q = 0; q < kTile; ++q) {
+      const float d2 = dz2[q], d1 = dz1[q];
+      g2a += d2 * a1a[q];
+      g2b += d2 * a1b[q];
+      g1 += d1 * xk[q];
+    }
+    atomicAdd(grad + oW2 + j * kH + lane, g2a);
+    atomicAdd(grad + oW2 + j * kH + lane + 32, g2b);
+    if (lane < (uint32_t)kIn) atomicAdd(grad + oW1 + j * kIn + lane, g1);
+    float b2 = 0.0f, b1 = 0.0f;
+    for (int q = lane; q < kTile; q += 32) {
+      b2 += dz2[q];
+      b1 += dz1[q];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      b2 += __shfl_xor_sync(0xFFFFFFFFu, b2, o);
+      b1 += __shfl_xor_sync(0xFFFFFFFFu, b1, o);
+    }
+    if (lane == 0) {
+      atomicAdd(grad + oB2 + j, b2);
+      atomicAdd(grad + oB1 + j, b1);
+    }
+  }
+}
+
+// AdamW (Loshchilov and Hutter) on all parameters in one block: moments, bias correction with the
+// step count t = *stepDev + 1, decoupled weight decay on weights only; refreshes the BF16 copy,
+// clears the gradient and advances the device step counter.
+__global__ void __launch_bounds__(1024) adamw_kernel(float *__restrict__ p, __nv_bfloat16 *__restrict__ pb,
+                                                     float *__restrict__ g, float *__restrict__ m,
+                                                     float *__restrict__ v, uint32_t *stepDev, float lr, float wd) {
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  const float t = (float)(*stepDev + 1u);
+  const float c1 = 1.0f - powf(b1, t), c2 = 1.0f - powf(b2, t);
+  for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const bool bias = (i >= oB1 && i < oW2) || (i >= oB2 && i < oW3) || i == oB3;
+    float pi = p[i];
+    if (!bias) pi -= lr * wd * pi;
+    pi -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    p[i] = pi;
+    pb[i] = __float2bfloat16_rn(pi);
+    g[i] = 0.0f;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *stepDev += 1u;
+}
+
+__global__ void to_bf16_kernel(const float *__restrict__ p, __nv_bfloat16 *__restrict__ pb, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) pb[i] = __float2bfloat16_rn(p[i]);
+}
+
+// Batch rows for step t = *stepDev + 1: SplitMix64 of (seed, t, i), reduced modulo numSamples.
+__global__ void batch_index_kernel(uint32_t *__restrict__ idx, uint32_t batch, uint32_t numSamples, uint64_t seed,
+                                   const uint32_t *__restrict__ stepDev) {
+  const uint64_t t = (uint64_t)*stepDev + 1u;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < batch; i += gridDim.x * blockDim.x) {
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull * (t * (uint64_t)batch + i + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    idx[i] = (uint32_t)(z % numSamples);
+  }
+}
+
+// ---- features ----------------------------------------------------------------------------------
+
+__device__ __forceinline__ float clamp64(float v) { return fminf(fmaxf(v, -64.0f), 64.0f); }
+__device__ __forceinline__ float nan0(float v) { return isnan(v) ? 0.0f : v; }
+__device__ __forceinline__ uint32_t rank_bin(float v) { return f2ord(v) >> 16; }
+
+// Depth by pointer jumping: after r rounds anc[x] is the 2^r-th ancestor of x, or the root, and
+// dep[x] the distance to it, so kDepthRounds rounds give min(depth, 2^kDepthRounds) exactly.
+__global__ void depth_init_kernel(const bvhgb_node *__restrict__ t, uint32_t n, uint32_t root, uint32_t *__restrict__ anc,
+                                  uint32_t *__restrict__ dep) {
+  for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
+    const uint32_t p = __ldg(&t[x].parent);
+    anc[x] = (x == root || p >= n) ? root : p;
+    dep[x] = x == root ? 0u : 1u;
+  }
+}
+__global__ void depth_jump_kernel(uint32_t n, uint32_t root, const uint32_t *__restrict__ ancIn,
+                                  const uint32_t *__restrict__ depIn, uint32_t *__restrict__ ancOut,
+                                  uint32_t *__restrict__ depOut) {
+  for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
+    const uint32_t a = ancIn[x];
+    if (a == root) {
+      ancOut[x] = a;
+      depOut[x] = depIn[x];
+    } else {
+      ancOut[x] = ancIn[a];
+      depOut[x] = depIn[x] + depIn[a];
+    }
+  }
+}
+
+// Subtree leaf counts bottom-up: each leaf climbs; at every inner node the second arrival adds the
+// children's counts and continues (acq_rel counters order the counts it reads).
+__global__ void leaf_count_kernel(const bvhgb_node *__restrict__ t, uint32_t n, uint32_t root, uint32_t *cnt,
+                                  uint32_t *arrive, uint32_t *err) {
+  for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
+    if (__ldg(&t[x].isLeafFlag) == 0) continue;
+    __stcg(cnt + x, 1u);
+    if (x == root) continue;
+    uint32_t y = __ldg(&t[x].parent);
+    for (uint32_t steps = 0;; ++steps) {
+      if (y >= n || steps > n) {
+        atomicOr(err, kErrBadIndex);
+        break;
+      }
+      if (atom_add_acq_rel(arrive + y, 1u) == 0u) break;  // first arrival: the sibling's path continues
+      const uint32_t l = __ldg(&t[y].left), r = __ldg(&t[y].right);
+      if (l >= n || r >= n) {
+        atomicOr(err, kErrBadIndex);
+        break;
+      }
+      __stcg(cnt + y, __ldcg(cnt + l) + __ldcg(cnt + r));
+      if (y == root) break;
+      y = __ldg(&t[y].parent);
+    }
+  }
+}
+
+__global__ void features_raw_kernel(const bvhgb_node *__restrict__ t, const uint32_t *__restrict__ inner,
+                                    uint32_t numInner, uint32_t numNodes, uint32_t root,
+                                    const uint32_t *__restrict__ depth, const uint32_t *__restrict__ leafCount,
+                                    float invLog2Leaves, float *__restrict__ raw, float *__restrict__ src,
+                                    uint32_t *__restrict__ hist) {
+  const float sroot = __ldg(&t[root].surfaceArea);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < numInner; i += gridDim.x * blockDim.x) {
+    const uint32_t x = __ldg(inner + i);
+    const float sa = __ldg(&t[x].surfaceArea);
+    const uint32_t l = min(__ldg(&t[x].left), numNodes - 1), r = min(__ldg(&t[x].right), numNodes - 1);
+    const float sl = __ldg(&t[l].surfaceArea), sr = __ldg(&t[r].surfaceArea);
+    const uint32_t p = x == root ? root : min(__ldg(&t[x].parent), numNodes - 1);
+    const uint32_t g = p == root ? root : min(__ldg(&t[p].parent), numNodes - 1);
+    const float mn = sl < sr ? sl : sr;
+    const float sum = fadd(sl, sr);
+    const float cost = fdiv(fmul(fmul(fmul(sa, sa), sa), 2.0f), fmul(sum, mn));  // kCalcCost
+    const uint32_t d = min(depth[x], 1u << kDepthRounds);
+    float f[kMlpRaw];
+    f[0] = log2f(sa);
+    f[1] = fdiv(sa, __ldg(&t[p].surfaceArea));
+    f[2] = fdiv(sa, __ldg(&t[g].surfaceArea));
+    f[3] = fdiv(sa, sum);
+    f[4] = fmul((float)d, invLog2Leaves);
+    f[5] = log2f((float)__ldcg(leafCount + l));
+    f[6] = log2f((float)__ldcg(leafCount + r));
+    f[7] = log2f(fdiv(sa, sroot));
+    f[8] = log2f(fdiv(sa, mn));
+    f[9] = log2f(cost);
+#pragma unroll
+    for (int k = 0; k < kMlpRaw; ++k) raw[(size_t)i * kMlpRaw + k] = clamp64(f[k]);
+    const float s4[4] = {nan0(cost), nan0(fdiv(sa, mn)), nan0(fdiv(sa, sum)), nan0(sa)};
+    *reinterpret_cast<float4 *>(src + (size_t)i * 4) = make_float4(s4[0], s4[1], s4[2], s4[3]);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) atomicAdd(hist + q * kRankBins + rank_bin(s4[q]), 1u);
+  }
+}
+
+// Exclusive prefix of each of the four histograms into the second half (one block each).
+__global__ void __launch_bounds__(1024) hist_scan_kernel(uint32_t *hist) {
+  constexpr uint32_t kPer = kRankBins / 1024;
+  __shared__ uint32_t warpSum[32];
+  const uint32_t *h = hist + blockIdx.x * kRankBins;
+  uint32_t *pre = hist + (4 + blockIdx.x) * kRankBins;
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  uint32_t local = 0;
+  for (uint32_t k = 0; k < kPer; ++k) local += h[tid * kPer + k];
+  uint32_t inc = local;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+    if (lane >= (uint32_t)o) inc += v;
+  }
+  if (lane == 31) warpSum[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t w = warpSum[lane];
+    uint32_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+      if (lane >= (uint32_t)o) wi += v;
+    }
+    warpSum[lane] = wi - w;
+  }
+  __syncthreads();
+  uint32_t run = warpSum[warp] + inc - local;
+  for (uint32_t k = 0; k < kPer; ++k) {
+    pre[tid * kPer + k] = run;
+    run += h[tid * kPer + k];
+  }
+}
+
+__device__ __forceinline__ uint32_t bf16_bits(float v) {
+  return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v));
+}
+
+__global__ void features_pack_kernel(const float *__restrict__ raw, const float *__restrict__ src,
+                                     const uint32_t *__restrict__ hist, uint32_t numInner, uint16_t *__restrict__ x) {
+  const float fn = (float)numInner;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < numInner; i += gridDim.x * blockDim.x) {
+    float f[kIn];
+#pragma unroll
+    for (int k = 0; k < kMlpRaw; ++k) f[k] = raw[(size_t)i * kMlpRaw + k];
+    const float4 s4 = *reinterpret_cast<const float4 *>(src + (size_t)i * 4);
+    const float sv[4] = {s4.x, s4.y, s4.z, s4.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t b = rank_bin(sv[q]);
+      const float below = (float)hist[(4 + q) * kRankBins + b];
+      const float own = (float)hist[q * kRankBins + b];
+      f[kMlpRaw + q] = fdiv(fadd(below, fmul(0.5f, own)), fn);
+    }
+#pragma unroll
+    for (int k = kMlpRaw + 4; k < kIn; ++k) f[k] = 0.0f;
+    uint4 *o = reinterpret_cast<uint4 *>(x + (size_t)i * kIn);
+#pragma unroll
+    for (int w = 0; w < 3; ++w) {
+      uint32_t u[4];
+#pragma unroll
+      for (int h = 0; h < 4; ++h) u[h] = bf16_bits(f[w * 8 + h * 2]) | (bf16_bits(f[w * 8 + h * 2 + 1]) << 16);
+      o[w] = make_uint4(u[0], u[1], u[2], u[3]);
+    }
+  }
+}
+
+uint32_t grid_for(uint32_t n, uint32_t block) {
+  return std::max(1u, std::min(ceil_div(n, block), (uint32_t)sm_count() * 8));
+}
+
+}  // namespace
+
+float lr_inv_log2_leaves(uint32_t numLeaves) { return 1.0f / std::log2((float)std::max(numLeaves, 2u)); }
+
+int lr_scratch_alloc(LrScratch &s, uint32_t numNodes) {
+  lr_scratch_free(s);
+  const size_t n = std::max(numNodes, 1u), ni = n / 2 + 1;
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+    e = cudaMalloc(&s.anc[k], 4 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&s.dep[k], 4 * n);
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&s.leafCount, 4 * n);
+  if (e == cudaSuccess) e = cudaMalloc(&s.arrive, 4 * n + 4);  // last word: error flags
+  if (e == cudaSuccess) e = cudaMalloc(&s.hist, 4ull * kRankBins * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&s.raw, 4 * kMlpRaw * ni);
+  if (e == cudaSuccess) e = cudaMalloc(&s.src, 16 * ni);
+  if (e == cudaSuccess) e = cudaMalloc(&s.x, 2ull * kIn * ni);
+  if (e == cudaSuccess) e = cudaMalloc(&s.y, 4 * ni);
+  if (e == cudaSuccess) e = cudaMemset(s.arrive + n, 0, 4);
+  if (e != cudaSuccess) {
+    set_last_error("lr_scratch_alloc", e);
+    lr_scratch_free(s);
+    return e == cudaErrorMemoryAllocation ? BVHGB_OUT_OF_MEMORY : BVHGB_CUDA_ERROR;
+  }
+  s.numNodes = (uint32_t)n;
+  return BVHGB_OK;
+}
+
+void lr_scratch_free(LrScratch &s) {
+  for (int k = 0; k < 2; ++k) {
+    cudaFree(s.anc[k]);
+    cudaFree(s.dep[k]);
+    s.anc[k] = s.dep[k] = nullptr;
+  }
+  cudaFree(s.leafCount);
+  cudaFree(s.arrive);
+  cudaFree(s.hist);
+  cudaFree(s.raw);
+  cudaFree(s.src);
+  cudaFree(s.x);
+  cudaFree(s.y);
+  s.leafCount = s.arrive = s.hist = nullptr;
+  s.raw = s.src = s.y = nullptr;
+  s.x = nullptr;
+  s.numNodes = 0;
+}
+
+uint32_t *lr_error_word(LrScratch &s) { return s.arrive + s.numNodes; }
+
+int lr_features(LrScratch &s, const bvhgb_node *nodes, uint32_t numNodes, uint32_t root, const uint32_t *inner,
+                uint32_t numInner, float invLog2Leaves, cudaStream_t st) {
+  if (numNodes > s.numNodes || numInner > s.numNodes / 2 + 1) return BVHGB_TOO_LARGE;
+  if (numInner == 0) return BVHGB_OK;
+  const uint32_t g = grid_for(numNodes, 256);
+  depth_init_kernel<<<g, 256, 0, st>>>(nodes, numNodes, root, s.anc[0], s.dep[0]);
+  BVHGB_LAUNCH_CHECK("lr depth init");
+  int cur = 0;
+  for (uint32_t r = 0; r < kDepthRounds; ++r) {
+    depth_jump_kernel<<<g, 256, 0, st>>>(numNodes, root, s.anc[cur], s.dep[cur], s.anc[cur ^ 1], s.dep[cur ^ 1]);
+    BVHGB_LAUNCH_CHECK("lr depth jump");
+    cur ^= 1;
+  }
+  BVHGB_CUDA_TRY(cudaMemsetAsync(s.arrive, 0, 4ull * numNodes, st));
+  leaf_count_kernel<<<g, 256, 0, st>>>(nodes, numNodes, root, s.leafCount, s.arrive, lr_error_word(s));
+  BVHGB_LAUNCH_CHECK("lr leaf count");
+  BVHGB_CUDA_TRY(cudaMemsetAsync(s.hist, 0, 4ull * kRankBins * 4, st));
+  const uint32_t gi = grid_for(numInner, 256);
+  features_raw_kernel<<<gi, 256, 0, st>>>(nodes, inner, numInner, numNodes, root, s.dep[cur], s.leafCount,
+                                          invLog2Leaves, s.raw, s.src, s.hist);
+  BVHGB_LAUNCH_CHECK("lr features");
+  hist_scan_kernel<<<4, 1024, 0, st>>>(s.hist);
+  BVHGB_LAUNCH_CHECK("lr rank scan");
+  features_pack_kernel<<<gi, 256, 0, st>>>(s.raw, s.src, s.hist, numInner, s.x);
+  BVHGB_LAUNCH_CHECK("lr features pack");
+  return BVHGB_OK;
+}
+
+}  // namespace bvhgb
+
+// ---- MLP object and C ABI -----------------------------------------------------------------------
+
+struct bvhgb_mlp {
+  float *p = nullptr, *g = nullptr, *m = nullptr, *v = nullptr, *loss = nullptr;
+  __nv_bfloat16 *pb = nullptr;
+  uint32_t *stepDev = nullptr;
+  uint32_t *idx = nullptr;
+  uint32_t idxCap = 0, lossCap = 0;
+};
+
+struct bvhgb_lr_features_ctx {
+  bvhgb::LrScratch s;
+};
+
+namespace bvhgb {
+
+int lr_score_keys(const bvhgb_mlp *m, LrScratch &s, const bvhgb_node *nodes, uint32_t root, const uint32_t *inner,
+                  uint32_t numInner, uint32_t *keys, uint32_t *vals, cudaStream_t st) {
+  if (numInner == 0) return BVHGB_OK;
+  mlp_forward_kernel<true><<<grid_for(numInner, 256), 256, 0, st>>>(m->pb, s.x, numInner, s.y, nodes, root, inner,
+                                                                      keys, vals);
+  BVHGB_LAUNCH_CHECK("lr score");
+  return BVHGB_OK;
+}
+
+namespace {
+int ensure_train_attr() {
+  static bool done = false;
+  if (!done) {
+    BVHGB_CUDA_TRY(cudaFuncSetAttribute(mlp_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem));
+    done = true;
+  }
+  return BVHGB_OK;
+}
+
+int ensure_loss(bvhgb_mlp *m, uint32_t n) {
+  if (m->lossCap >= n && m->loss) return BVHGB_OK;
+  cudaFree(m->loss);
+  m->loss = nullptr;
+  m->lossCap = 0;
+  BVHGB_CUDA_TRY(cudaMalloc(&m->loss, 4ull * std::max(n, 1u)));
+  m->lossCap = std::max(n, 1u);
+  return BVHGB_OK;
+}
+}  // namespace
+}  // namespace bvhgb
+
+using namespace bvhgb;
+
+extern "C" BVHGB_API int bvhgb_mlp_create(uint64_t seed, bvhgb_mlp **out) {
+  if (!out) return BVHGB_INVALID_ARGUMENT;
+  *out = nullptr;
+  auto *m = new bvhgb_mlp();
+  cudaError_t e = cudaMalloc(&m->p, 4 * kMlpParams);
+  if (e == cudaSuccess) e = cudaMalloc(&m->g, 4 * kMlpParams);
+  if (e == cudaSuccess) e = cudaMalloc(&m->m, 4 * kMlpParams);
+  if (e == cudaSuccess) e = cudaMalloc(&m->v, 4 * kMlpParams);
+  if (e == cudaSuccess) e = cudaMalloc(&m->pb, 2 * kMlpParams);
+  if (e == cudaSuccess) e = cudaMalloc(&m->stepDev, 4);
+  if (e != cudaSuccess) {
+    set_last_error("bvhgb_mlp_create", e);
+    bvhgb_mlp_destroy(m);
+    return e == cudaErrorMemoryAllocation ? BVHGB_OUT_OF_MEMORY : BVHGB_CUDA_ERROR;
+  }
+  std::vector<float> h(kMlpParams, 0.0f);
+  uint64_t state = seed;
+  auto uni = [&]() {  // SplitMix64 -> uniform in [-1, 1)
+    uint64_t z = (state += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (float)((double)(z >> 40) * (1.0 / 16777216.0)) * 2.0f - 1.0f;
+  };
+  for (int i = 0; i < kH * kIn; ++i) h[oW1 + i] = uni() * std::sqrt(6.0f / kIn);
+  for (int i = 0; i < kH * kH; ++i) h[oW2 + i] = uni() * std::sqrt(6.0f / kH);
+  for (int i = 0; i < kH; ++i) h[oW3 + i] = uni() * std::sqrt(6.0f / kH) * 0.1f;
+  const int st = bvhgb_mlp_set_params(m, h.data());
+  if (st) {
+    bvhgb_mlp_destroy(m);
+    return st;
+  }
+  *out = m;
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_mlp_destroy(bvhgb_mlp *m) {
+  if (!m) return BVHGB_OK;
+  cudaFree(m->p);
+  cudaFree(m->g);
+  cudaFree(m->m);
+  cudaFree(m->v);
+  cudaFree(m->loss);
+  cudaFree(m->pb);
+  cudaFree(m->stepDev);
+  cudaFree(m->idx);
+  delete m;
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_mlp_set_params(bvhgb_mlp *m, const float *params) {
+  if (!m || !params) return BVHGB_INVALID_ARGUMENT;
+  BVHGB_CUDA_TRY(cudaMemcpy(m->p, params, 4 * kMlpParams, cudaMemcpyHostToDevice));
+  BVHGB_CUDA_TRY(cudaMemset(m->g, 0, 4 * kMlpParams));
+  BVHGB_CUDA_TRY(cudaMemset(m->m, 0, 4 * kMlpParams));
+  BVHGB_CUDA_TRY(cudaMemset(m->v, 0, 4 * kMlpParams));
+  BVHGB_CUDA_TRY(cudaMemset(m->stepDev, 0, 4));
+  to_bf16_kernel<<<ceil_div(kMlpParams, 256), 256>>>(m->p, m->pb, kMlpParams);
+  BVHGB_LAUNCH_CHECK("mlp bf16 copy");
+  BVHGB_CUDA_TRY(cudaDeviceSynchronize());
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_mlp_get_params(const bvhgb_mlp *m, float *params) {
+  if (!m || !params) return BVHGB_INVALID_ARGUMENT;
+  BVHGB_CUDA_TRY(cudaMemcpy(params, m->p, 4 * kMlpParams, cudaMemcpyDeviceToHost));
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_mlp_forward(const bvhgb_mlp *m, const uint16_t *x, uint32_t n, float *y,
+                                           bvhgb_stream stream) {
+  if (!m || (n && (!x || !y))) return BVHGB_INVALID_ARGUMENT;
+  if (n == 0) return BVHGB_OK;
+  mlp_forward_kernel<false><<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(m->pb, x, n, y, nullptr, 0, nullptr,
+                                                                            nullptr, nullptr);
+  BVHGB_LAUNCH_CHECK("mlp forward");
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_mlp_gradient(bvhgb_mlp *m, const uint16_t *x, const float *t, uint32_t n,
+                                            float *gradHost, float *lossHost, bvhgb_stream stream) {
+  if (!m || !x || !t || n == 0) return BVHGB_INVALID_ARGUMENT;
+  int st = ensure_train_attr();
+  if (!st) st = ensure_loss(m, 1);
+  if (st) return st;
+  cudaStream_t s = as_stream(stream);
+  BVHGB_CUDA_TRY(cudaMemsetAsync(m->g, 0, 4 * kMlpParams, s));
+  BVHGB_CUDA_TRY(cudaMemsetAsync(m->loss, 0, 4, s));
+  mlp_train_kernel<<<ceil_div(n, kTile), kTile, kTrainSmem, s>>>(m->pb, x, t, nullptr, n, (float)n, m->g, m->loss,
+                                                                  nullptr, 0, 1);
+  BVHGB_LAUNCH_CHECK("mlp gradient");
+  if (gradHost) BVHGB_CUDA_TRY(cudaMemcpyAsync(gradHost, m->g, 4 * kMlpParams, cudaMemcpyDeviceToHost, s));
+  if (lossHost) BVHGB_CUDA_TRY(cudaMemcpyAsync(lossHost, m->loss, 4, cudaMemcpyDeviceToHost, s));
+  BVHGB_CUDA_TRY(cudaMemsetAsync(m->g, 0, 4 * kMlpParams, s));
+  BVHGB_CUDA_TRY(cudaStreamSynchronize(s));
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_mlp_train(bvhgb_mlp *m, const uint16_t *x, const float *t, uint32_t numSamples,
+                                         uint32_t batch, uint32_t steps, float lr, float weightDecay, uint64_t seed,
+                                         float *lossHistory, bvhgb_stream stream) {
+  if (!m || !x || !t || numSamples == 0 || batch == 0) return BVHGB_INVALID_ARGUMENT;
+  if (steps == 0) return BVHGB_OK;
+  int st = ensure_train_attr();
+  if (!st) st = ensure_loss(m, steps);
+  if (st) return st;
+  cudaStream_t s = as_stream(stream);
+  if (m->idxCap < batch) {
+    cudaFree(m->idx);
+    m->idx = nullptr;
+    m->idxCap = 0;
+    BVHGB_CUDA_TRY(cudaMalloc(&m->idx, 4ull * batch));
+    m->idxCap = batch;
+  }
+  uint32_t step0 = 0;
+  BVHGB_CUDA_TRY(cudaMemcpyAsync(&step0, m->stepDev, 4, cudaMemcpyDeviceToHost, s));
+  BVHGB_CUDA_TRY(cudaStreamSynchronize(s));
+  BVHGB_CUDA_TRY(cudaMemsetAsync(m->loss, 0, 4ull * steps, s));
+  BVHGB_CUDA_TRY(cudaStreamSynchronize(s));
+  // Capture one step (batch rows, forward + backward, AdamW) and replay it; the kernels read the
+  // step number from device memory so every replay is the next step.
+  cudaStream_t cap = nullptr;
+  BVHGB_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    batch_index_kernel<<<ceil_div(batch, 256), 256, 0, cap>>>(m->idx, batch, numSamples, seed, m->stepDev);
+    mlp_train_kernel<<<ceil_div(batch, kTile), kTile, kTrainSmem, cap>>>(m->pb, x, t, m->idx, batch, (float)batch,
+                                                                          m->g, m->loss, m->stepDev, step0, steps);
+    adamw_kernel<<<1, 1024, 0, cap>>>(m->p, m->pb, m->g, m->m, m->v, m->stepDev, lr, weightDecay);
+    e = cudaStreamEndCapture(cap, &graph);
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  cudaStreamDestroy(cap);
+  if (e != cudaSuccess) {
+    set_last_error("bvhgb_mlp_train capture", e);
+    if (exec) cudaGraphExecDestroy(exec);
+    return BVHGB_CUDA_ERROR;
+  }
+  for (uint32_t k = 0; k < steps && e == cudaSuccess; ++k) e = cudaGraphLaunch(exec, s);
+  count_launch(3u * steps);
+  if (e == cudaSuccess && lossHistory) e = cudaMemcpyAsync(lossHistory, m->loss, 4ull * steps, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaGraphExecDestroy(exec);
+  if (e != cudaSuccess) {
+    set_last_error("bvhgb_mlp_train", e);
+    return BVHGB_CUDA_ERROR;
+  }
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_lr_features_create(uint32_t maxNodes, bvhgb_lr_features_ctx **out) {
+  if (!out || maxNodes == 0) return BVHGB_INVALID_ARGUMENT;
+  *out = nullptr;
+  auto *c = new bvhgb_lr_features_ctx();
+  const int st = lr_scratch_alloc(c->s, maxNodes);
+  if (st) {
+    delete c;
+    return st;
+  }
+  *out = c;
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_lr_features_destroy(bvhgb_lr_features_ctx *ctx) {
+  if (!ctx) return BVHGB_OK;
+  lr_scratch_free(ctx->s);
+  delete ctx;
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_lr_features(bvhgb_lr_features_ctx *ctx, const bvhgb_node *nodes, uint32_t numNodes,
+                                           uint32_t root, const uint32_t *inner, uint32_t numInner, uint32_t numLeaves,
+                                           uint16_t *x, bvhgb_stream stream) {
+  if (!ctx || !nodes || !inner || !x || root >= numNodes) return BVHGB_INVALID_ARGUMENT;
+  cudaStream_t s = as_stream(stream);
+  const int st = lr_features(ctx->s, nodes, numNodes, root, inner, numInner, lr_inv_log2_leaves(numLeaves), s);
+  if (st) return st;
+  if (numInner) BVHGB_CUDA_TRY(cudaMemcpyAsync(x, ctx->s.x, 2ull * kIn * numInner, cudaMemcpyDeviceToDevice, s));
+  return BVHGB_OK;
+}

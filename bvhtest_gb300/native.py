@@ -96,6 +96,20 @@ PROTOS = {
     "bvhgb_bn13_batch_size": (U32, [VP]),
     "bvhgb_bn13_launches_per_iteration": (U32, [VP]),
     "bvhgb_bn13_search_time": (I32, [VP, C.POINTER(F32), C.POINTER(U32)]),
+    "bvhgb_bn13_gains": (I32, [VP, VP, VP, U32, VP, VP, VP]),
+    "bvhgb_bn13_read_inner": (I32, [VP, VP, U32, C.POINTER(U32), VP]),
+    "bvhgb_bn13_set_scorer": (I32, [VP, VP]),
+    "bvhgb_bn13_read_selection": (I32, [VP, VP, U32, VP]),
+    "bvhgb_mlp_create": (I32, [U64, C.POINTER(VP)]),
+    "bvhgb_mlp_destroy": (I32, [VP]),
+    "bvhgb_mlp_set_params": (I32, [VP, VP]),
+    "bvhgb_mlp_get_params": (I32, [VP, VP]),
+    "bvhgb_mlp_forward": (I32, [VP, VP, U32, VP, VP]),
+    "bvhgb_mlp_gradient": (I32, [VP, VP, VP, U32, VP, VP, VP]),
+    "bvhgb_mlp_train": (I32, [VP, VP, VP, U32, U32, U32, F32, F32, U64, VP, VP]),
+    "bvhgb_lr_features_create": (I32, [U32, C.POINTER(VP)]),
+    "bvhgb_lr_features_destroy": (I32, [VP]),
+    "bvhgb_lr_features": (I32, [VP, VP, U32, U32, VP, U32, U32, VP, VP]),
     "bvhgb_trace_image": (I32, [VP, U32, U32, VP, VP, C.POINTER(Camera), C.POINTER(TraceConfig), VP, VP, VP]),
     "bvhgb_trace_rays": (I32, [VP, U32, U32, VP, VP, VP, VP, U32, C.POINTER(TraceConfig), VP, VP]),
     "bvhgb_trace_bounce": (I32, [VP, U32, U32, VP, VP, C.POINTER(Camera), C.POINTER(TraceConfig), U64, F32, VP, VP,

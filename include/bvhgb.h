@@ -236,6 +236,75 @@ BVHGB_API uint32_t bvhgb_bn13_launches_per_iteration(const bvhgb_bn13_workspace 
  * the most recent iteration, and the number of launches that covers (synchronous). */
 BVHGB_API int bvhgb_bn13_search_time(bvhgb_bn13_workspace *ws, float *ms, uint32_t *launches);
 
+/* ---- learned reinsertion scorer ------------------------------------------------------------------
+ * No counterpart in the reference: its selection is the inefficiency of Bittner13CUDA.cu:480-500.
+ * A 24 -> 64 -> 64 -> 1 MLP with GELU (tanh form), BF16 weights, inputs and activations, FP32
+ * accumulation, trained by the library's own forward / backward / AdamW kernels on
+ * (feature row, realised SAH reduction) pairs logged from plain optimizer runs, and used in place
+ * of the inefficiency to pick the batch of each iteration. The plain measure stays the default.
+ *
+ * Feature row of an inner node x (children l, r, parent p, grand parent g, SA = surface area; p and
+ * g are the root where they do not exist; raw values clamped to [-64, 64], NaN -> -64):
+ *   0 log2 SA(x)   1 SA(x)/SA(p)   2 SA(x)/SA(g)   3 SA(x)/(SA(l)+SA(r))   4 min(depth,256)/log2(#leaves)
+ *   5 log2 leaves(l)   6 log2 leaves(r)   7 log2 SA(x)/SA(root)   8 log2 SA(x)/min(SA(l),SA(r))
+ *   9 log2 inefficiency   10..13 ranks (over all inner nodes, 65536-bin histogram) of the
+ *   inefficiency, SA(x)/min(SA(l),SA(r)), SA(x)/(SA(l)+SA(r)) and SA(x)   14..23 zero.
+ * Parameters, FP32, in this order: W1[64][24] b1[64] W2[64][64] b2[64] W3[64] b3[1]. */
+#define BVHGB_LR_FEATURES 24
+#define BVHGB_MLP_PARAMS 5825
+
+typedef struct bvhgb_mlp bvhgb_mlp;
+
+/* Parameters initialised from 'seed' (uniform +-sqrt(6/fan_in), last layer scaled by 0.1, zero
+ * biases) and zero AdamW state. */
+BVHGB_API int bvhgb_mlp_create(uint64_t seed, bvhgb_mlp **out);
+BVHGB_API int bvhgb_mlp_destroy(bvhgb_mlp *m);
+/* Host FP32 arrays of BVHGB_MLP_PARAMS values; set also resets the AdamW state and step. */
+BVHGB_API int bvhgb_mlp_set_params(bvhgb_mlp *m, const float *params);
+BVHGB_API int bvhgb_mlp_get_params(const bvhgb_mlp *m, float *params);
+/* y[i] = MLP(x[i]) for n device rows of BVHGB_LR_FEATURES BF16 values (raw uint16 bit patterns). */
+BVHGB_API int bvhgb_mlp_forward(const bvhgb_mlp *m, const uint16_t *x, uint32_t n, float *y, bvhgb_stream stream);
+/* Gradient of the mean squared error over n device samples (x, target t) without an update:
+ * gradHost receives BVHGB_MLP_PARAMS floats, lossHost the loss (either may be NULL). Synchronous.
+ * The BF16 rounding of weights and activations is passed through as identity. */
+BVHGB_API int bvhgb_mlp_gradient(bvhgb_mlp *m, const uint16_t *x, const float *t, uint32_t n, float *gradHost,
+                                 float *lossHost, bvhgb_stream stream);
+/* 'steps' AdamW steps (beta 0.9 / 0.999, eps 1e-8, decoupled weight decay on the weights) on
+ * batches of 'batch' rows drawn with replacement from numSamples device rows by a counter hash of
+ * (seed, step). One step is captured as a CUDA graph and replayed. lossHistory (host, may be NULL)
+ * receives each step's batch loss; the call is synchronous when it is given. */
+BVHGB_API int bvhgb_mlp_train(bvhgb_mlp *m, const uint16_t *x, const float *t, uint32_t numSamples, uint32_t batch,
+                              uint32_t steps, float lr, float weightDecay, uint64_t seed, float *lossHistory,
+                              bvhgb_stream stream);
+
+typedef struct bvhgb_lr_features_ctx bvhgb_lr_features_ctx;
+/* Device scratch for the features of trees of up to maxNodes nodes. */
+BVHGB_API int bvhgb_lr_features_create(uint32_t maxNodes, bvhgb_lr_features_ctx **out);
+BVHGB_API int bvhgb_lr_features_destroy(bvhgb_lr_features_ctx *ctx);
+/* Feature rows (BF16 bit patterns, numInner x BVHGB_LR_FEATURES, device) of the device inner-node
+ * list 'inner' (numInner ids); numLeaves scales the depth feature. */
+BVHGB_API int bvhgb_lr_features(bvhgb_lr_features_ctx *ctx, const bvhgb_node *nodes, uint32_t numNodes, uint32_t root,
+                                const uint32_t *inner, uint32_t numInner, uint32_t numLeaves, uint16_t *x,
+                                bvhgb_stream stream);
+/* Realised gain of reinserting each candidate alone with the batched search: the exact SAH
+ * reduction (cInner = 1) in units of the root's surface area, 0 where the reinsertion is refused.
+ * target (may be NULL) receives the training target clip(gain / (SA(x) / SA(root)), -4, 4).
+ * Device arrays; the tree is not modified. */
+BVHGB_API int bvhgb_bn13_gains(bvhgb_bn13_workspace *ws, const bvhgb_node *nodes, const uint32_t *cand, uint32_t n,
+                               float *gain, float *target, bvhgb_stream stream);
+/* Number of inner nodes of the workspace's tree; with out != NULL (device, capacity entries) also
+ * copies their ids in ascending order (the optimizer's inner-node list) on 'stream'. */
+BVHGB_API int bvhgb_bn13_read_inner(const bvhgb_bn13_workspace *ws, uint32_t *out, uint32_t capacity,
+                                    uint32_t *numInner, bvhgb_stream stream);
+/* Select each iteration's batch by the scorer's predicted reduction (MLP output times
+ * SA(x)/SA(root), descending, ties by node id) instead of the inefficiency; NULL restores the plain
+ * measure. The workspace keeps the pointer: the scorer must outlive its use. Drops a captured graph. */
+BVHGB_API int bvhgb_bn13_set_scorer(bvhgb_bn13_workspace *ws, const bvhgb_mlp *scorer);
+/* Copies the most recent selection order (numInner node ids, batch position order) into out
+ * (device, capacity entries) on 'stream'. */
+BVHGB_API int bvhgb_bn13_read_selection(const bvhgb_bn13_workspace *ws, uint32_t *out, uint32_t capacity,
+                                        bvhgb_stream stream);
+
 /* ---- tracer (lib/tracer/CUDAKernels.hpp:39-77, CUDATracer.cpp:86-118) ------------------------ */
 
 typedef struct bvhgb_camera {

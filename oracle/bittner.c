@@ -549,15 +549,135 @@ static void refit_paths(orc_node *t, uint32_t root, const uint32_t *fix, uint32_
   }
 }
 
-int orc_bittner_chunked(orc_node *t, uint32_t n_nodes, uint32_t root, uint32_t iters,
-                        const orc_bn13_cfg *cfg, double *sah_trace, orc_bn13_stats *stats) {
+/* One iteration of the chunked algorithm over a given batch order (order[pos] = the node at batch
+ * position pos, as the sorted todo list of bn13_selectNodes). Work buffers live in w. */
+typedef struct chunk_work {
+  bpatch *patches;
+  uint8_t *valid;
+  uint32_t *fix, *owner;
+  uint8_t *mark;
+  dnode *dbuf;
+  hitem *pqs;
+  uint64_t *ovf, *vis;
+  uint32_t nthreads;
+} chunk_work;
+
+static void chunk_work_init(chunk_work *w, uint32_t n_nodes, uint32_t csize, uint32_t cap) {
+  w->patches = malloc(sizeof(bpatch) * (csize ? csize : 1));
+  w->valid = malloc(csize ? csize : 1);
+  w->fix = malloc(sizeof(uint32_t) * 3 * (csize ? csize : 1));
+  w->owner = malloc(sizeof(uint32_t) * (n_nodes ? n_nodes : 1));
+  w->mark = calloc(n_nodes ? n_nodes : 1, 1);
+  w->dbuf = malloc(sizeof(dnode) * (n_nodes ? n_nodes : 1));
+  for (uint32_t i = 0; i < n_nodes; ++i) w->owner[i] = NONE;
+  w->nthreads = (uint32_t)orc_num_threads();
+  w->pqs = malloc(sizeof(hitem) * cap * w->nthreads);
+  w->ovf = calloc(w->nthreads, sizeof(uint64_t));
+  w->vis = calloc(w->nthreads, sizeof(uint64_t));
+}
+
+static void chunk_work_free(chunk_work *w, orc_bn13_stats *st) {
+  for (uint32_t i = 0; i < w->nthreads; ++i) {
+    st->heap_overflow += w->ovf[i];
+    st->nodes_visited += w->vis[i];
+  }
+  free(w->patches); free(w->valid); free(w->fix); free(w->owner); free(w->mark); free(w->dbuf);
+  free(w->pqs); free(w->ovf); free(w->vis);
+}
+
+static uint32_t chunk_size(uint32_t n_nodes, const orc_bn13_cfg *cfg, uint32_t *numc_out) {
   float bp = cfg->batch_percent;
   if (bp <= 0.01f) bp = 0.01f;
   if (bp >= 75.0f) bp = 75.0f;
   uint32_t numc = cfg->num_chunks ? cfg->num_chunks : 1;
   uint32_t lnum = (uint32_t)((bp / 100.0f) * (float)n_nodes);
-  uint32_t csize = lnum / numc;
-  uint32_t cap = cfg->heap_cap ? cfg->heap_cap : 4096;
+  *numc_out = numc;
+  return lnum / numc;
+}
+
+static void run_iteration(orc_node *t, uint32_t root, const uint32_t *order, uint32_t n_order, uint32_t numc,
+                          uint32_t csize, uint32_t cap, const orc_bn13_cfg *cfg, chunk_work *w, orc_bn13_stats *st) {
+  const int mode = (int)cfg->search_mode;
+  for (uint32_t c = 0; c < numc; ++c) {
+    /* kRemoveAndReinsert (:504-564) against the chunk-start tree. */
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int64_t kk = 0; kk < (int64_t)csize; ++kk) {
+      uint32_t k = (uint32_t)kk;
+#ifdef _OPENMP
+      int tid = omp_get_thread_num();
+#else
+      int tid = 0;
+#endif
+      hitem *pq = w->pqs + (size_t)cap * tid;
+      uint32_t pos = cfg->offset_access ? k * numc + c : c * csize + k;
+      uint32_t node = pos < n_order ? order[pos] : NONE;
+      bpatch *p = &w->patches[k];
+      p->t = t;
+      p->root = root;
+      bp_clear(p);
+      w->valid[k] = 0;
+      w->fix[3 * k] = w->fix[3 * k + 1] = w->fix[3 * k + 2] = NONE;
+      if (node == NONE) continue;
+      uint32_t ins[2], un[2], g;
+      if (!gpu_remove(p, node, ins, un, &g)) continue;
+      if (!gpu_reinsert(p, ins[0], un[0], 1, pq, cap, &w->ovf[tid], mode, &w->vis[tid])) continue;
+      if (!gpu_reinsert(p, ins[1], un[1], 0, pq, cap, &w->ovf[tid], mode, &w->vis[tid])) continue;
+      w->valid[k] = 1;
+      w->fix[3 * k] = g;
+      w->fix[3 * k + 1] = un[0];
+      w->fix[3 * k + 2] = un[1];
+    }
+    /* Conflict rule: claim every patched node with the item's rank; lowest rank wins. */
+    for (uint32_t k = 0; k < csize; ++k) {
+      if (!w->valid[k]) continue;
+      for (int s = 0; s < NNODE; ++s) {
+        uint32_t x = w->patches[k].idx[s];
+        if (x != NONE && k < w->owner[x]) w->owner[x] = k;
+      }
+    }
+    uint32_t nwin = 0;
+    for (uint32_t k = 0; k < csize; ++k) {
+      st->items++;
+      if (!w->valid[k]) { st->skipped_invalid++; continue; }
+      int ok = 1;
+      for (int s = 0; s < NNODE; ++s) {
+        uint32_t x = w->patches[k].idx[s];
+        if (x != NONE && w->owner[x] != k) ok = 0;
+      }
+      if (!ok) {
+        st->skipped_conflict++;
+        w->valid[k] = 0;
+        w->fix[3 * k] = w->fix[3 * k + 1] = w->fix[3 * k + 2] = NONE;
+        continue;
+      }
+      nwin++;
+    }
+    /* kApplyPatches (:612-627) for the winners, then release every claim. */
+    for (uint32_t k = 0; k < csize; ++k) {
+      for (int s = 0; s < NNODE; ++s) {
+        uint32_t x = w->patches[k].idx[s];
+        if (x == NONE) continue;
+        if (w->valid[k]) {
+          t[x].parent = w->patches[k].nd[s].parent;
+          t[x].left = w->patches[k].nd[s].left;
+          t[x].right = w->patches[k].nd[s].right;
+          t[x].isLeft = w->patches[k].nd[s].isLeft;
+        }
+      }
+    }
+    for (uint32_t k = 0; k < csize; ++k)
+      for (int s = 0; s < NNODE; ++s)
+        if (w->patches[k].idx[s] != NONE) w->owner[w->patches[k].idx[s]] = NONE;
+    st->applied += nwin;
+    refit_paths(t, root, w->fix, 3 * csize, w->mark, w->dbuf);
+  }
+}
+
+int orc_bittner_chunked(orc_node *t, uint32_t n_nodes, uint32_t root, uint32_t iters,
+                        const orc_bn13_cfg *cfg, double *sah_trace, orc_bn13_stats *stats) {
+  uint32_t numc;
+  const uint32_t csize = chunk_size(n_nodes, cfg, &numc);
+  const uint32_t cap = cfg->heap_cap ? cfg->heap_cap : 4096;
   orc_bn13_stats st;
   memset(&st, 0, sizeof(st));
 
@@ -566,20 +686,10 @@ int orc_bittner_chunked(orc_node *t, uint32_t n_nodes, uint32_t root, uint32_t i
   for (uint32_t i = 0; i < n_nodes; ++i) n_inner += t[i].isLeafFlag == 0;
   uint32_t *inner = malloc(sizeof(uint32_t) * (n_inner ? n_inner : 1));
   for (uint32_t i = 0, j = 0; i < n_nodes; ++i) if (!t[i].isLeafFlag) inner[j++] = i;
-
   cost_item *todo = malloc(sizeof(cost_item) * (n_inner ? n_inner : 1));
-  bpatch *patches = malloc(sizeof(bpatch) * (csize ? csize : 1));
-  uint8_t *valid = malloc(csize ? csize : 1);
-  uint32_t *fix = malloc(sizeof(uint32_t) * 3 * (csize ? csize : 1));
-  uint32_t *owner = malloc(sizeof(uint32_t) * n_nodes);
-  uint8_t *mark = calloc(n_nodes, 1);
-  dnode *dbuf = malloc(sizeof(dnode) * n_nodes);
-  for (uint32_t i = 0; i < n_nodes; ++i) owner[i] = NONE;
-  uint32_t nthreads = (uint32_t)orc_num_threads();
-  hitem *pqs = malloc(sizeof(hitem) * cap * nthreads);
-  uint64_t *ovf = calloc(nthreads, sizeof(uint64_t));
-  uint64_t *vis = calloc(nthreads, sizeof(uint64_t));
-  const int mode = (int)cfg->search_mode;
+  uint32_t *order = malloc(sizeof(uint32_t) * (n_inner ? n_inner : 1));
+  chunk_work w;
+  chunk_work_init(&w, n_nodes, csize, cap);
 
   if (sah_trace) sah_trace[0] = orc_sah(t, n_nodes, root);
   for (uint32_t it = 0; it < iters; ++it) {
@@ -589,90 +699,137 @@ int orc_bittner_chunked(orc_node *t, uint32_t n_nodes, uint32_t root, uint32_t i
       todo[j].cost = orc_inefficiency(t, inner[j]);
     }
     qsort(todo, n_inner, sizeof(cost_item), cmp_cost_desc);
-
-    for (uint32_t c = 0; c < numc; ++c) {
-      /* kRemoveAndReinsert (:504-564) against the chunk-start tree. */
-#pragma omp parallel for schedule(dynamic, 4)
-      for (int64_t kk = 0; kk < (int64_t)csize; ++kk) {
-        uint32_t k = (uint32_t)kk;
-#ifdef _OPENMP
-        int tid = omp_get_thread_num();
-#else
-        int tid = 0;
-#endif
-        hitem *pq = pqs + (size_t)cap * tid;
-        uint32_t pos = cfg->offset_access ? k * numc + c : c * csize + k;
-        uint32_t node = pos < n_inner ? todo[pos].idx : NONE;
-        bpatch *p = &patches[k];
-        p->t = t;
-        p->root = root;
-        bp_clear(p);
-        valid[k] = 0;
-        fix[3 * k] = fix[3 * k + 1] = fix[3 * k + 2] = NONE;
-        if (node == NONE) continue;
-        uint32_t ins[2], un[2], g;
-        if (!gpu_remove(p, node, ins, un, &g)) continue;
-        if (!gpu_reinsert(p, ins[0], un[0], 1, pq, cap, &ovf[tid], mode, &vis[tid])) continue;
-        if (!gpu_reinsert(p, ins[1], un[1], 0, pq, cap, &ovf[tid], mode, &vis[tid])) continue;
-        valid[k] = 1;
-        fix[3 * k] = g;
-        fix[3 * k + 1] = un[0];
-        fix[3 * k + 2] = un[1];
-      }
-      /* Conflict rule: claim every patched node with the item's rank; lowest rank wins. */
-      for (uint32_t k = 0; k < csize; ++k) {
-        if (!valid[k]) continue;
-        for (int s = 0; s < NNODE; ++s) {
-          uint32_t x = patches[k].idx[s];
-          if (x != NONE && k < owner[x]) owner[x] = k;
-        }
-      }
-      uint32_t nwin = 0;
-      for (uint32_t k = 0; k < csize; ++k) {
-        st.items++;
-        if (!valid[k]) { st.skipped_invalid++; continue; }
-        int ok = 1;
-        for (int s = 0; s < NNODE; ++s) {
-          uint32_t x = patches[k].idx[s];
-          if (x != NONE && owner[x] != k) ok = 0;
-        }
-        if (!ok) {
-          st.skipped_conflict++;
-          valid[k] = 0;
-          fix[3 * k] = fix[3 * k + 1] = fix[3 * k + 2] = NONE;
-          continue;
-        }
-        nwin++;
-      }
-      /* kApplyPatches (:612-627) for the winners, then release every claim. */
-      for (uint32_t k = 0; k < csize; ++k) {
-        for (int s = 0; s < NNODE; ++s) {
-          uint32_t x = patches[k].idx[s];
-          if (x == NONE) continue;
-          if (valid[k]) {
-            t[x].parent = patches[k].nd[s].parent;
-            t[x].left = patches[k].nd[s].left;
-            t[x].right = patches[k].nd[s].right;
-            t[x].isLeft = patches[k].nd[s].isLeft;
-          }
-        }
-      }
-      for (uint32_t k = 0; k < csize; ++k)
-        for (int s = 0; s < NNODE; ++s)
-          if (patches[k].idx[s] != NONE) owner[patches[k].idx[s]] = NONE;
-      st.applied += nwin;
-      refit_paths(t, root, fix, 3 * csize, mark, dbuf);
-    }
+    for (uint32_t j = 0; j < n_inner; ++j) order[j] = todo[j].idx;
+    run_iteration(t, root, order, n_inner, numc, csize, cap, cfg, &w, &st);
     if (sah_trace) sah_trace[it + 1] = orc_sah(t, n_nodes, root);
   }
-  for (uint32_t i = 0; i < nthreads; ++i) {
-    st.heap_overflow += ovf[i];
-    st.nodes_visited += vis[i];
-  }
-  free(vis);
+  chunk_work_free(&w, &st);
   if (stats) *stats = st;
-  free(inner); free(todo); free(patches); free(valid); free(fix); free(owner); free(mark);
-  free(dbuf); free(pqs); free(ovf);
+  free(inner); free(todo); free(order);
   (void)cmp_u32;
   return 0;
+}
+
+int orc_bittner_iteration_ordered(orc_node *t, uint32_t n_nodes, uint32_t root, const uint32_t *order,
+                                  uint32_t n_order, const orc_bn13_cfg *cfg, orc_bn13_stats *stats) {
+  uint32_t numc;
+  const uint32_t csize = chunk_size(n_nodes, cfg, &numc);
+  const uint32_t cap = cfg->heap_cap ? cfg->heap_cap : 4096;
+  orc_bn13_stats st;
+  memset(&st, 0, sizeof(st));
+  chunk_work w;
+  chunk_work_init(&w, n_nodes, csize, cap);
+  run_iteration(t, root, order, n_order, numc, csize, cap, cfg, &w, &st);
+  chunk_work_free(&w, &st);
+  if (stats) *stats = st;
+  return 0;
+}
+
+/* ---- isolated realised gain of one reinsertion ---------------------------------------------
+ * The patch changes the children of three nodes only: the grand parent (its child becomes the
+ * sibling) and the two reused nodes (new parents of the reinserted children). A node's box changes
+ * iff it lies on a path from one of these to the root in the patched tree, and only those nodes'
+ * surface areas change, so the SAH reduction (cInner = 1) is the sum of old minus new surface
+ * area over the union of the three paths, divided by the root's area. The union is a tree with at
+ * most two join points: path 1 (from the first reused node) meets path 0 (from the grand parent) at
+ * J1 = lca(s1, s0); path 2 meets path 0 or the private part of path 1 at J2, the deeper of
+ * lca(s2, s0) and lca(s2, s1). New boxes are computed bottom-up in the order: private part of
+ * path 2, private part of path 1, path 0 to the root; a child's new box is the running box of the
+ * walk, the last box of a private part at its join node, or else the child's unchanged box. */
+typedef struct gwalk {
+  uint32_t prev, last1, j1, last2, j2;
+  orc_aabb prevbox, box1, box2;
+} gwalk;
+
+static uint32_t np_parent(const bpatch *p, uint32_t x) { return bp_get(p, x).parent; }
+
+static int new_depth(const bpatch *p, uint32_t x, uint32_t n_nodes, uint32_t *d) {
+  uint32_t k = 0;
+  while (x != p->root) {
+    if (x >= n_nodes || k > n_nodes) return 0;
+    x = np_parent(p, x);
+    k++;
+  }
+  *d = k;
+  return 1;
+}
+
+static uint32_t lca(const bpatch *p, uint32_t a, uint32_t da, uint32_t b, uint32_t db, uint32_t *dout) {
+  while (da > db) { a = np_parent(p, a); da--; }
+  while (db > da) { b = np_parent(p, b); db--; }
+  while (a != b && da > 0) { a = np_parent(p, a); b = np_parent(p, b); da--; }
+  *dout = da;
+  return a;
+}
+
+static orc_aabb child_box(const bpatch *p, const gwalk *w, uint32_t x, uint32_t c) {
+  if (c == w->prev) return w->prevbox;
+  if (x == w->j1 && c == w->last1) return w->box1;
+  if (x == w->j2 && c == w->last2) return w->box2;
+  return p->t[c].bbox;
+}
+
+/* Walk from x up to (not including) stop, or through the root when stop is NONE. */
+static void gain_walk(const bpatch *p, gwalk *w, uint32_t x, uint32_t stop, uint32_t n_nodes, double *acc, int *ok) {
+  w->prev = NONE;
+  for (uint32_t k = 0; x != stop; ++k) {
+    if (x >= n_nodes || k > n_nodes) { *ok = 0; return; }
+    npatch n = bp_get(p, x);
+    if (n.left >= n_nodes || n.right >= n_nodes) { *ok = 0; return; }
+    orc_aabb b = child_box(p, w, x, n.left);
+    orc_aabb rb = child_box(p, w, x, n.right);
+    merge_into(&b, &rb);
+    *acc += (double)p->t[x].surfaceArea - (double)orc_surface_area(&b);
+    w->prev = x;
+    w->prevbox = b;
+    if (x == p->root) return;
+    x = n.parent;
+  }
+}
+
+static float isolated_gain(const bpatch *p, uint32_t s0, uint32_t s1, uint32_t s2, uint32_t n_nodes, int *ok) {
+  uint32_t d0, d1, d2, dj1, d20, d21;
+  if (!new_depth(p, s0, n_nodes, &d0) || !new_depth(p, s1, n_nodes, &d1) || !new_depth(p, s2, n_nodes, &d2)) {
+    *ok = 0;
+    return 0.0f;
+  }
+  const uint32_t j1 = lca(p, s1, d1, s0, d0, &dj1);
+  const uint32_t l20 = lca(p, s2, d2, s0, d0, &d20);
+  const uint32_t l21 = lca(p, s2, d2, s1, d1, &d21);
+  const uint32_t j2 = d20 >= d21 ? l20 : l21;
+  gwalk w;
+  memset(&w, 0, sizeof(w));
+  w.last1 = w.j1 = w.last2 = w.j2 = NONE;
+  double acc = 0.0;
+  gain_walk(p, &w, s2, j2, n_nodes, &acc, ok);
+  w.last2 = w.prev;
+  w.box2 = w.prevbox;
+  w.j2 = j2;
+  gain_walk(p, &w, s1, j1, n_nodes, &acc, ok);
+  w.last1 = w.prev;
+  w.box1 = w.prevbox;
+  w.j1 = j1;
+  gain_walk(p, &w, s0, NONE, n_nodes, &acc, ok);
+  if (!*ok) return 0.0f;
+  return (float)(acc / (double)p->t[p->root].surfaceArea);
+}
+
+void orc_bn13_gains(const orc_node *t, uint32_t n_nodes, uint32_t root, const uint32_t *cand, uint32_t n,
+                    float *gain, uint8_t *ok_out) {
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    bpatch p;
+    p.t = t;
+    p.root = root;
+    bp_clear(&p);
+    uint64_t ovf = 0, vis = 0;
+    uint32_t ins[2], un[2], g;
+    const uint32_t x = cand[i];
+    int ok = x < n_nodes && gpu_remove(&p, x, ins, un, &g) && gpu_reinsert(&p, ins[0], un[0], 1, NULL, 0, &ovf, 0, &vis) &&
+             gpu_reinsert(&p, ins[1], un[1], 0, NULL, 0, &ovf, 0, &vis);
+    float v = 0.0f;
+    if (ok) v = isolated_gain(&p, g, un[0], un[1], n_nodes, &ok);
+    gain[i] = ok ? v : 0.0f;
+    if (ok_out) ok_out[i] = (uint8_t)ok;
+  }
 }

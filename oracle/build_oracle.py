@@ -11,7 +11,7 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_build"
-SOURCES = ["lbvh.c", "bittner.c", "tracer.c"]
+SOURCES = ["lbvh.c", "bittner.c", "tracer.c", "learned.c"]
 FLAGS = ["-O2", "-std=gnu11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
          "-Wall", "-Wno-unused-function"]
 

@@ -124,6 +124,31 @@ typedef struct orc_bn13_stats {
 int orc_bittner_chunked(orc_node *nodes, uint32_t n_nodes, uint32_t root, uint32_t iters,
                         const orc_bn13_cfg *cfg, double *sah_trace, orc_bn13_stats *stats);
 
+/* One iteration of the chunked algorithm with a given batch order: order[pos] is the node at batch
+ * position pos (the role of the sorted todo list). Used to check a GPU iteration whose selection
+ * came from the learned scorer. */
+int orc_bittner_iteration_ordered(orc_node *nodes, uint32_t n_nodes, uint32_t root, const uint32_t *order,
+                                  uint32_t n_order, const orc_bn13_cfg *cfg, orc_bn13_stats *stats);
+
+/* ---- Learned reinsertion scorer (an addition; the reference has no learned part) -------------- */
+
+#define ORC_LR_FEATURES 24
+
+/* 1 / log2(max(#leaves, 2)), the depth feature's scale. */
+float orc_lr_inv_log2_leaves(uint32_t n_leaves);
+
+/* Feature rows of every inner node in ascending node order (definition in learned.c); writes the
+ * node ids to inner (may be NULL) and returns the number of inner nodes. */
+uint32_t orc_lr_features(const orc_node *nodes, uint32_t n_nodes, uint32_t root, float *feat, uint32_t *inner);
+
+/* Realised gain of reinserting each candidate alone: remove the node and its parent, reinsert both
+ * children with the batched search (search mode 0), and take the exact SAH reduction (cInner = 1)
+ * of the resulting tree against the current one, in units of the root's surface area (summed in
+ * double over the changed nodes, then rounded to float). Where the reinsertion is refused
+ * (removeNode or best == root) the gain is 0 and ok[i] = 0. */
+void orc_bn13_gains(const orc_node *nodes, uint32_t n_nodes, uint32_t root, const uint32_t *cand, uint32_t n,
+                    float *gain, uint8_t *ok);
+
 /* ---- Tracer ------------------------------------------------------------------------------ */
 
 typedef struct orc_camera {

@@ -210,3 +210,48 @@ def adler32(data: bytes) -> int:
 
 def num_threads() -> int:
     return lib().orc_num_threads()
+
+
+def _cfg(num_chunks=32, batch_percent=1.0, offset_access=False, heap_cap=4096, search_mode=0):
+    return Bn13Cfg(num_chunks, batch_percent, int(offset_access), heap_cap, search_mode)
+
+
+def bittner_iteration_ordered(nodes, order, root=0, **cfg):
+    """One chunked iteration in place with the given batch order; returns the stats dict."""
+    assert nodes.flags.c_contiguous
+    order = _u32(order)
+    st = Bn13Stats()
+    c = _cfg(**cfg)
+    lib().orc_bittner_iteration_ordered(_p(nodes), C.c_uint32(nodes.shape[0]), C.c_uint32(root), _p(order),
+                                        C.c_uint32(order.shape[0]), C.byref(c), C.byref(st))
+    return {k: getattr(st, k) for k, _ in Bn13Stats._fields_}
+
+
+LR_FEATURES = 24
+
+
+def lr_features(nodes, root=0):
+    """(features [n_inner, 24] float32, inner node ids ascending)."""
+    nodes = np.ascontiguousarray(nodes)
+    n = nodes.shape[0]
+    feat = np.zeros((n, LR_FEATURES), np.float32)
+    inner = np.zeros(n, np.uint32)
+    lib().orc_lr_features.restype = C.c_uint32
+    m = lib().orc_lr_features(_p(nodes), C.c_uint32(n), C.c_uint32(root), _p(feat), _p(inner))
+    return feat[:m].copy(), inner[:m].copy()
+
+
+def lr_inv_log2_leaves(n_leaves):
+    lib().orc_lr_inv_log2_leaves.restype = C.c_float
+    return lib().orc_lr_inv_log2_leaves(C.c_uint32(n_leaves))
+
+
+def bn13_gains(nodes, cand, root=0):
+    """Isolated realised SAH reduction of reinserting each candidate alone (units of root SA)."""
+    nodes = np.ascontiguousarray(nodes)
+    cand = _u32(cand)
+    gain = np.zeros(cand.shape[0], np.float32)
+    ok = np.zeros(cand.shape[0], np.uint8)
+    lib().orc_bn13_gains(_p(nodes), C.c_uint32(nodes.shape[0]), C.c_uint32(root), _p(cand), C.c_uint32(cand.shape[0]),
+                         _p(gain), _p(ok))
+    return gain, ok.astype(bool)
