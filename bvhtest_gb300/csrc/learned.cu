@@ -324,10 +324,19 @@ __global__ void features_raw_kernel(const bvhgb_node *__restrict__ t, const uint
                                     uint32_t numInner, uint32_t numNodes, uint32_t root,
                                     const uint32_t *__restrict__ depth, const uint32_t *__restrict__ leafCount,
                                     float invLog2Leaves, float *__restrict__ raw, float *__restrict__ src,
-                                    uint32_t *__restrict__ hist) {
+                                    uint32_t *__restrict__ hist, uint32_t *__restrict__ err) {
   const float sroot = __ldg(&t[root].surfaceArea);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < numInner; i += gridDim.x * blockDim.x) {
     const uint32_t x = __ldg(inner + i);
+    if (x >= numNodes) {  // not a node: a zero row, flagged
+      atomicOr(err, kErrBadIndex);
+#pragma unroll
+      for (int k = 0; k < kMlpRaw; ++k) raw[(size_t)i * kMlpRaw + k] = 0.0f;
+      *reinterpret_cast<float4 *>(src + (size_t)i * 4) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) atomicAdd(hist + q * kRankBins + rank_bin(0.0f), 1u);
+      continue;
+    }
     const float sa = __ldg(&t[x].surfaceArea);
     const uint32_t l = min(__ldg(&t[x].left), numNodes - 1), r = min(__ldg(&t[x].right), numNodes - 1);
     const float sl = __ldg(&t[l].surfaceArea), sr = __ldg(&t[r].surfaceArea);
@@ -498,7 +507,7 @@ int lr_features(LrScratch &s, const bvhgb_node *nodes, uint32_t numNodes, uint32
   BVHGB_CUDA_TRY(cudaMemsetAsync(s.hist, 0, 4ull * kRankBins * 4, st));
   const uint32_t gi = grid_for(numInner, 256);
   features_raw_kernel<<<gi, 256, 0, st>>>(nodes, inner, numInner, numNodes, root, s.dep[cur], s.leafCount,
-                                          invLog2Leaves, s.raw, s.src, s.hist);
+                                          invLog2Leaves, s.raw, s.src, s.hist, lr_error_word(s));
   BVHGB_LAUNCH_CHECK("lr features");
   hist_scan_kernel<<<4, 1024, 0, st>>>(s.hist);
   BVHGB_LAUNCH_CHECK("lr rank scan");
