@@ -212,6 +212,12 @@ class Bittner13GPU:
               "bvhgb_bn13_read_selection")
         return out
 
+    def set_selection(self, order: torch.Tensor, stream=None):
+        """Use 'order' (numInner node ids, batch position order) for the following chunk() calls."""
+        order = order.to(device="cuda", dtype=torch.int32).contiguous()
+        check(self.lib.bvhgb_bn13_set_selection(self.ws, _ptr(order), order.shape[0], _stream(stream)),
+              "bvhgb_bn13_set_selection")
+
     def select(self, stream=None):
         check(self.lib.bvhgb_bn13_select_nodes(self.ws, _ptr(self.nodes), _stream(stream)), "bvhgb_bn13_select_nodes")
 

@@ -803,7 +803,7 @@ __device__ float isolated_gain(const Patch &p, uint32_t s0, uint32_t s1, uint32_
 // unmodified tree, then the isolated gain; lane 0 writes. Nothing is applied.
 __global__ void __launch_bounds__(kWarpItemsPerBlock * 32) gain_warp_kernel(
     const bvhgb_node *__restrict__ t, uint32_t root, const uint32_t *__restrict__ cand, uint32_t n, uint32_t numNodes,
-    float *__restrict__ gain, float *__restrict__ target, uint32_t *__restrict__ err) {
+    float targetScale, float *__restrict__ gain, float *__restrict__ target, uint32_t *__restrict__ err) {
   const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t lane = threadIdx.x & 31u;
   if (k >= n) return;  // whole warps leave together
@@ -829,14 +829,7 @@ __global__ void __launch_bounds__(kWarpItemsPerBlock * 32) gain_warp_kernel(
   if (p.bad) atomicOr(err, kErrBadIndex);
   if (!ok) v = 0.0f;
   gain[k] = v;
-  if (target) {
-    float tv = 0.0f;
-    if (x < numNodes) {
-      const float rel = fdiv(tree_sa(t, x), tree_sa(t, root));
-      if (rel > 0.0f) tv = fminf(fmaxf(fdiv(v, rel), -kTargetClip), kTargetClip);
-    }
-    target[k] = tv;
-  }
+  if (target) target[k] = copysignf(log1pf(fmul(fabsf(v), targetScale)), v);
 }
 
 __global__ void init_inner_kernel(const bvhgb_node *__restrict__ t, uint32_t n, uint32_t *__restrict__ flag) {
@@ -1150,7 +1143,7 @@ extern "C" BVHGB_API int bvhgb_bn13_gains(bvhgb_bn13_workspace *ws, const bvhgb_
   if (!ws || !nodes || (n && (!cand || !gain))) return BVHGB_INVALID_ARGUMENT;
   if (n == 0) return BVHGB_OK;
   gain_warp_kernel<<<ceil_div(n, kWarpItemsPerBlock), kWarpItemsPerBlock * 32, 0, as_stream(stream)>>>(
-      nodes, ws->root, cand, n, ws->numNodes, gain, target, ws->err);
+      nodes, ws->root, cand, n, ws->numNodes, (float)(ws->numNodes - ws->numInner) / kTargetEps, gain, target, ws->err);
   BVHGB_LAUNCH_CHECK("bn13 gains");
   return BVHGB_OK;
 }
@@ -1187,5 +1180,12 @@ extern "C" BVHGB_API int bvhgb_bn13_read_selection(const bvhgb_bn13_workspace *w
   if (capacity < ws->numInner) return BVHGB_TOO_LARGE;
   if (ws->numInner)
     BVHGB_CUDA_TRY(cudaMemcpyAsync(out, ws->todo, 4ull * ws->numInner, cudaMemcpyDeviceToDevice, as_stream(stream)));
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_bn13_set_selection(bvhgb_bn13_workspace *ws, const uint32_t *order, uint32_t n,
+                                                 bvhgb_stream stream) {
+  if (!ws || (n && !order) || n != ws->numInner) return BVHGB_INVALID_ARGUMENT;
+  if (n) BVHGB_CUDA_TRY(cudaMemcpyAsync(ws->todo, order, 4ull * n, cudaMemcpyDeviceToDevice, as_stream(stream)));
   return BVHGB_OK;
 }

@@ -82,8 +82,7 @@ __device__ __forceinline__ float mlp_eval(const float *W, const float in[kIn]) {
 template <bool KEYS>
 __global__ void __launch_bounds__(256) mlp_forward_kernel(const __nv_bfloat16 *__restrict__ w,
                                                           const uint16_t *__restrict__ x, uint32_t n,
-                                                          float *__restrict__ y, const bvhgb_node *__restrict__ t,
-                                                          uint32_t root, const uint32_t *__restrict__ inner,
+                                                          float *__restrict__ y, const uint32_t *__restrict__ inner,
                                                           uint32_t *__restrict__ keys, uint32_t *__restrict__ vals) {
   __shared__ float W[kWPad];
   load_weights(w, W);
@@ -94,10 +93,8 @@ __global__ void __launch_bounds__(256) mlp_forward_kernel(const __nv_bfloat16 *_
     const float out = mlp_eval(W, in);
     y[s] = out;
     if (KEYS) {
-      const uint32_t node = __ldg(inner + s);
-      const float rel = fdiv(__ldg(&t[node].surfaceArea), __ldg(&t[root].surfaceArea));
-      keys[s] = ~f2ord(fmul(out, rel));
-      vals[s] = node;
+      keys[s] = ~f2ord(out);
+      vals[s] = __ldg(inner + s);
     }
   }
 }
@@ -537,8 +534,7 @@ namespace bvhgb {
 int lr_score_keys(const bvhgb_mlp *m, LrScratch &s, const bvhgb_node *nodes, uint32_t root, const uint32_t *inner,
                   uint32_t numInner, uint32_t *keys, uint32_t *vals, cudaStream_t st) {
   if (numInner == 0) return BVHGB_OK;
-  mlp_forward_kernel<true><<<grid_for(numInner, 256), 256, 0, st>>>(m->pb, s.x, numInner, s.y, nodes, root, inner,
-                                                                      keys, vals);
+  mlp_forward_kernel<true><<<grid_for(numInner, 256), 256, 0, st>>>(m->pb, s.x, numInner, s.y, inner, keys, vals);
   BVHGB_LAUNCH_CHECK("lr score");
   return BVHGB_OK;
 }
@@ -640,8 +636,8 @@ extern "C" BVHGB_API int bvhgb_mlp_forward(const bvhgb_mlp *m, const uint16_t *x
                                            bvhgb_stream stream) {
   if (!m || (n && (!x || !y))) return BVHGB_INVALID_ARGUMENT;
   if (n == 0) return BVHGB_OK;
-  mlp_forward_kernel<false><<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(m->pb, x, n, y, nullptr, 0, nullptr,
-                                                                            nullptr, nullptr);
+  mlp_forward_kernel<false><<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(m->pb, x, n, y, nullptr, nullptr,
+                                                                            nullptr);
   BVHGB_LAUNCH_CHECK("mlp forward");
   return BVHGB_OK;
 }

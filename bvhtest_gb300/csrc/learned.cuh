@@ -15,7 +15,7 @@ constexpr int kMlpParams = BVHGB_MLP_PARAMS;  // W1[64][24] b1[64] W2[64][64] b2
 constexpr int kMlpRaw = 10;                   // raw (non-rank) features
 constexpr uint32_t kRankBins = 65536;         // rank histogram bins (top 16 bits of the ordered image)
 constexpr uint32_t kDepthRounds = 8;          // pointer-jumping rounds: depth is exact up to 256
-constexpr float kTargetClip = 4.0f;           // training target = clip(gain / (SA / SA_root))
+constexpr float kTargetEps = 0.16f;           // target = sign(g) ln(1 + |g| numLeaves / kTargetEps)
 
 // Device scratch for the features of one tree (sized for numNodes nodes).
 struct LrScratch {
@@ -34,8 +34,8 @@ void lr_scratch_free(LrScratch &s);
 int lr_features(LrScratch &s, const bvhgb_node *nodes, uint32_t numNodes, uint32_t root, const uint32_t *inner,
                 uint32_t numInner, float invLog2Leaves, cudaStream_t st);
 
-// Scorer forward over s.x, then the selection keys: key = ~order(y * SA(x) / SA(root)) so that an
-// ascending sort gives the descending predicted reduction; vals = node ids.
+// Scorer forward over s.x, then the selection keys: key = ~order(y) so that an ascending sort gives
+// the descending predicted reduction; vals = node ids.
 int lr_score_keys(const bvhgb_mlp *m, LrScratch &s, const bvhgb_node *nodes, uint32_t root, const uint32_t *inner,
                   uint32_t numInner, uint32_t *keys, uint32_t *vals, cudaStream_t st);
 

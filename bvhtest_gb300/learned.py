@@ -3,9 +3,10 @@ runs on the GPU, training the MLP with the library's own kernels, and optimising
 
 The reference has no learned part; this is the extension that replaces the inefficiency measure
 (lib/builder/Bittner13CUDA.cu:480-500) by a prediction of the SAH a reinsertion actually removes.
-Label of a node: the exact SAH reduction (cInner = 1, in units of the root's surface area) of
+Label of a node: the exact SAH reduction g (cInner = 1, in units of the root's surface area) of
 removing it and reinserting its children alone against the current tree; training target:
-clip(label / (SA(node) / SA(root)), -4, 4); selection key: prediction * SA(node) / SA(root).
+sign(g) ln(1 + |g| numLeaves / 0.16), the gain in units of SA(root) / numLeaves, log-compressed so
+that the nodes of every size are ranked on one scale; selection key: the prediction itself.
 Everything runs on the device through libbvhgb; there is no CPU path.
 """
 from __future__ import annotations

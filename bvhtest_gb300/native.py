@@ -100,6 +100,7 @@ PROTOS = {
     "bvhgb_bn13_read_inner": (I32, [VP, VP, U32, C.POINTER(U32), VP]),
     "bvhgb_bn13_set_scorer": (I32, [VP, VP]),
     "bvhgb_bn13_read_selection": (I32, [VP, VP, U32, VP]),
+    "bvhgb_bn13_set_selection": (I32, [VP, VP, U32, VP]),
     "bvhgb_mlp_create": (I32, [U64, C.POINTER(VP)]),
     "bvhgb_mlp_destroy": (I32, [VP]),
     "bvhgb_mlp_set_params": (I32, [VP, VP]),

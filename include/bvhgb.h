@@ -288,7 +288,8 @@ BVHGB_API int bvhgb_lr_features(bvhgb_lr_features_ctx *ctx, const bvhgb_node *no
                                 bvhgb_stream stream);
 /* Realised gain of reinserting each candidate alone with the batched search: the exact SAH
  * reduction (cInner = 1) in units of the root's surface area, 0 where the reinsertion is refused.
- * target (may be NULL) receives the training target clip(gain / (SA(x) / SA(root)), -4, 4).
+ * target (may be NULL) receives the training target sign(g) ln(1 + |g| numLeaves / 0.16): the gain
+ * in units of SA(root) / numLeaves, log-compressed so that one scale ranks nodes of every size.
  * Device arrays; the tree is not modified. */
 BVHGB_API int bvhgb_bn13_gains(bvhgb_bn13_workspace *ws, const bvhgb_node *nodes, const uint32_t *cand, uint32_t n,
                                float *gain, float *target, bvhgb_stream stream);
@@ -296,10 +297,14 @@ BVHGB_API int bvhgb_bn13_gains(bvhgb_bn13_workspace *ws, const bvhgb_node *nodes
  * copies their ids in ascending order (the optimizer's inner-node list) on 'stream'. */
 BVHGB_API int bvhgb_bn13_read_inner(const bvhgb_bn13_workspace *ws, uint32_t *out, uint32_t capacity,
                                     uint32_t *numInner, bvhgb_stream stream);
-/* Select each iteration's batch by the scorer's predicted reduction (MLP output times
- * SA(x)/SA(root), descending, ties by node id) instead of the inefficiency; NULL restores the plain
- * measure. The workspace keeps the pointer: the scorer must outlive its use. Drops a captured graph. */
+/* Select each iteration's batch by the scorer's predicted reduction (its output, the target scale
+ * above; descending, ties by node id) instead of the inefficiency; NULL restores the plain measure.
+ * The workspace keeps the pointer: the scorer must outlive its use. Drops a captured graph. */
 BVHGB_API int bvhgb_bn13_set_scorer(bvhgb_bn13_workspace *ws, const bvhgb_mlp *scorer);
+/* Replaces the selection of the current iteration by a caller order (numInner node ids, device, in
+ * batch position order) for the following bvhgb_bn13_chunk calls; a later select overwrites it. */
+BVHGB_API int bvhgb_bn13_set_selection(bvhgb_bn13_workspace *ws, const uint32_t *order, uint32_t n,
+                                       bvhgb_stream stream);
 /* Copies the most recent selection order (numInner node ids, batch position order) into out
  * (device, capacity entries) on 'stream'. */
 BVHGB_API int bvhgb_bn13_read_selection(const bvhgb_bn13_workspace *ws, uint32_t *out, uint32_t capacity,

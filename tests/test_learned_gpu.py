@@ -63,10 +63,9 @@ def test_gains_match_oracle_bit_exact(gpu, orc, topo, iters):
     g = gain.cpu().numpy()
     assert np.array_equal(g, ref), f"{np.count_nonzero(g != ref)} gains differ"
     assert ok.mean() > 0.99 and (ref > 0).mean() > 0.3
-    sa = host["surfaceArea"]
-    rel = (sa[inner.cpu().numpy()] / sa[0]).astype(np.float32)
-    want = np.where(rel > 0, np.clip((ref / rel).astype(np.float32), -4, 4), 0).astype(np.float32)
-    assert np.array_equal(tgt.cpu().numpy(), want)
+    leaves = host.shape[0] - inner.shape[0]
+    want = np.sign(ref) * np.log1p(np.abs(ref).astype(np.float64) * np.float32(leaves / 0.16))
+    assert np.allclose(tgt.cpu().numpy(), want, rtol=2e-6, atol=1e-7)
     # the tree is not modified by the evaluation
     assert np.array_equal(gpu.nodes_to_numpy(nodes).view(np.uint8), host.view(np.uint8))
 
@@ -141,13 +140,11 @@ def test_learned_selection_iteration_matches_oracle(gpu, orc):
     opt.set_scorer(m)
     opt.select()
     order = opt.selection().cpu().numpy().view(np.uint32)
-    # the order is the stable descending order of the scorer's own outputs times SA / SA_root
+    # the order is the stable descending order of the scorer's own outputs
     inner = opt.inner_nodes()
     y = m.forward(gpu.LrFeatures(nodes.shape[0])(nodes, inner)).cpu().numpy()
-    sa = start["surfaceArea"]
     inn = inner.cpu().numpy().view(np.uint32)
-    key = (y * (sa[inn] / sa[0]).astype(np.float32)).astype(np.float32)
-    want = inn[np.argsort(-key, kind="stable")]
+    want = inn[np.argsort(-y, kind="stable")]
     assert np.array_equal(order, want)
     for c in range(32):
         opt.chunk(c)
@@ -171,18 +168,24 @@ def test_learned_selection_iteration_matches_oracle(gpu, orc):
 
 def test_trained_scorer_beats_the_plain_measure(gpu):
     """Train on pairs logged from plain runs over 6 scenes, evaluate on 2 unseen ones: the learned
-    selection must reach the plain optimizer's 100-iteration SAH in at most half the iterations."""
+    selection must reach the plain optimizer's 100-iteration SAH in at most 40 iterations, and after
+    100 iterations of its own be at least 3% below it."""
     n = 16384
     trees = (_tree(gpu, n, seed=100 + s)[2] for s in range(6))
     data = learned.log_pairs(trees, iterations=60, every=3)
     assert data.x.shape[0] == 6 * 20 * (n - 1)
     m, hist, _ = learned.train(data, steps=3000, batch=8192, lr=1e-3)
-    assert hist[-100:].mean() < hist[:20].mean()
+    assert hist[-100:].mean() < 0.7 * hist[:20].mean()
     for seed in (7, 8):
         _, _, plain = _tree(gpu, n, seed)
-        _, _, lrn = _tree(gpu, n, seed)
         opt = gpu.Bittner13GPU(plain)
         opt.run(100)
         target = gpu.calc_sah(plain)
+        _, _, lrn = _tree(gpu, n, seed)
         it, trace = learned.optimize_until(lrn, target, 100, scorer=m)
-        assert it is not None and it <= 50, (seed, target, trace[::10])
+        assert it is not None and it <= 40, (seed, target, trace[::10])
+        _, _, full = _tree(gpu, n, seed)
+        lo = gpu.Bittner13GPU(full)
+        lo.set_scorer(m)
+        lo.run(100)
+        assert gpu.calc_sah(full) < 0.97 * target
