@@ -8,7 +8,9 @@ diffuse bounce per hit. Synthetic inputs stand in for the reference's mesh files
 
 One step = build + optimize + trace. `value` is the build + optimize time in ms (inputs already in
 HBM); `e2e` is the same metric through the C ABI with the mesh copied from pinned host memory
-and the optimised node array copied back inside the timed region.
+and the optimised node array copied back inside the timed region. `learned_vs_plain` trains the
+learned reinsertion scorer (32 seeded 65,536-triangle scenes, about 52M logged pairs, 20k AdamW
+steps) and times build + optimisation to equal SAH on an unseen scene, plain against learned.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload large|small]
 """
@@ -344,7 +346,87 @@ def run_ours(args, w, rank, world, local):
         "gpu_launches": gpu_launches,
         "clocks": clocks,
     }
+    if not args.no_learned:
+        line["learned_vs_plain"] = learned_arm(args, dev, flush, stream)
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------------------
+# Learned scorer against the plain measure (uniform 65,536-triangle scenes)
+# ---------------------------------------------------------------------------------------------
+
+LEARNED_N, LEARNED_SCENES, LEARNED_ITERS, LEARNED_EVERY, LEARNED_STEPS = 65536, 32, 100, 4, 20000
+
+
+def learned_arm(args, dev, flush, stream):
+    """Train the scorer on pairs logged from plain runs over 32 seeded scenes, then time LBVH build +
+    optimisation to the plain optimizer's 100-iteration SAH on an unseen scene, plain vs learned."""
+    import torch
+    from bvhtest_gb300 import api, learned, scenes
+
+    n = LEARNED_N
+    builder = api.LBVH(n, 30, "refCompat")
+    trees = (learned.uniform_scene_tree(n, 1000 + s, builder=builder)[2].clone() for s in range(LEARNED_SCENES))
+    data = learned.log_pairs(trees, iterations=LEARNED_ITERS, every=LEARNED_EVERY)
+    pairs, log_s = int(data.x.shape[0]), data.seconds
+    scorer, hist, train_s = learned.train(data, steps=LEARNED_STEPS, batch=8192, lr=1e-3, weight_decay=1e-4)
+    del data
+    torch.cuda.empty_cache()
+
+    vert_h, faces_h = scenes.uniform_soup(n, seed=1)  # the training scenes use seeds 1000..1031
+    vert = torch.from_numpy(vert_h).to(dev)
+    faces = torch.from_numpy(faces_h.view(np.int32)).to(dev)
+    nodes = api.empty_nodes(2 * n - 1)
+    lbvh = api.LBVH(n, 30, "refCompat")
+    plain = api.Bittner13GPU(lbvh.build(vert, faces, nodes))
+    sah0 = api.calc_sah(nodes)
+    plain.run(LEARNED_ITERS)
+    target = api.calc_sah(nodes)
+    lrn = api.Bittner13GPU(lbvh.build(vert, faces, nodes))
+    lrn.set_scorer(scorer)
+    k_learned = None
+    for it in range(1, LEARNED_ITERS + 1):  # calibration (untimed): iterations to reach the target
+        lrn.step()
+        if api.calc_sah(nodes) <= target:
+            k_learned = it
+            break
+    if k_learned is None:
+        return {"workload": "uniform 65,536 triangles", "error": "learned selection did not reach the plain SAH"}
+
+    def timed(opt, iters):
+        out = []
+        for i in range(args.warmup + args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            lbvh.build(vert, faces, nodes)
+            opt.run(iters)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if i >= args.warmup:
+                out.append(e0.elapsed_time(e1))
+        return statistics.mean(out), api.calc_sah(nodes)
+
+    plain_ms, plain_sah = timed(plain, LEARNED_ITERS)
+    learned_ms, learned_sah = timed(lrn, k_learned)
+    lrn_full = api.Bittner13GPU(lbvh.build(vert, faces, nodes))
+    lrn_full.set_scorer(scorer)
+    lrn_full.run(LEARNED_ITERS)
+    sah_learned_full = api.calc_sah(nodes)
+    return {
+        "workload": ("uniform 65,536 triangles (seed 1, unseen in training), 30-bit Morton, refCompat LBVH; "
+                     "target = SAH after 100 plain Bittner13 iterations at 1%"),
+        "sah_start": round(sah0, 4), "sah_target": round(target, 4),
+        "plain": {"iterations": LEARNED_ITERS, "build_optimize_ms": round(plain_ms, 3), "sah": round(plain_sah, 4)},
+        "learned": {"iterations": k_learned, "build_optimize_ms": round(learned_ms, 3), "sah": round(learned_sah, 4),
+                    "sah_after_100": round(sah_learned_full, 4)},
+        "wall_time_ratio": round(learned_ms / plain_ms, 4),
+        "train": {"scenes": LEARNED_SCENES, "pairs": pairs, "log_s": round(log_s, 2), "steps": LEARNED_STEPS,
+                  "batch": 8192, "lr": 1e-3, "weight_decay": 1e-4, "train_s": round(train_s, 2),
+                  "loss_first": round(float(hist[:100].mean()), 4), "loss_last": round(float(hist[-100:].mean()), 4)},
+    }
 
 
 def main():
@@ -359,6 +441,7 @@ def main():
     ap.add_argument("--no-kernel-events", action="store_true",
                     help="do not bracket the search kernel with CUDA events (for runs under ncu)")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-scorer comparison")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
