@@ -266,6 +266,14 @@ class Mlp:
         except Exception:
             pass
 
+    def save(self, path):
+        """Raw little-endian float32 parameters (the `learnedScorer` file of the bittner13GPU command)."""
+        self.params().astype("<f4").tofile(path)
+
+    @classmethod
+    def load(cls, path) -> "Mlp":
+        return cls(params=np.fromfile(path, dtype="<f4"))
+
     def params(self) -> np.ndarray:
         out = np.zeros(MLP_PARAMS, np.float32)
         check(self.lib.bvhgb_mlp_get_params(self.handle, out.ctypes.data_as(C.c_void_p)), "bvhgb_mlp_get_params")

@@ -574,7 +574,9 @@ class Bittner13GPU : public Command {
   bool vSort = true, vOffsetAccess = false, vAltFindNode = false, vAltFixTree = false, vAltSort = false,
        vLocalPatchCPY = false;
   std::string vSearch = "batched";
+  std::string vScorer;  // learned scorer weights (5825 little-endian float32); empty = inefficiency
   bvhgb_bn13_workspace *vWs = nullptr;
+  bvhgb_mlp *vMlp = nullptr;
 
  public:
   std::string name() const override { return "bittner13GPU"; }
@@ -595,6 +597,7 @@ class Bittner13GPU : public Command {
     vAltSort = j.value("altSort", vAltSort);
     vLocalPatchCPY = j.value("localPatchCPY", vLocalPatchCPY);
     vSearch = j.value("searchMode", vSearch);
+    vScorer = j.value("learnedScorer", vScorer);
     if (vBatchPercent <= 0.01f) vBatchPercent = 0.01f;
     if (vBatchPercent >= 75.0f) vBatchPercent = 75.0f;
   }
@@ -613,6 +616,7 @@ class Bittner13GPU : public Command {
     o["altSort"] = vAltSort;
     o["localPatchCPY"] = vLocalPatchCPY;
     o["searchMode"] = vSearch;
+    o["learnedScorer"] = vScorer;
     return o;
   }
 
@@ -630,7 +634,22 @@ class Bittner13GPU : public Command {
     if (vAltFindNode) warn("altFindNode: the reference's approximate 16-slot queue is not built; using the searchMode search");
     bvhgb_bn13_config cfg{vNumChunks, vBlockSize, vBatchPercent, vOffsetAccess ? 1u : 0u, 4096u, 0u,
                           vSearch == "heap" ? (uint32_t)BVHGB_SEARCH_HEAP : (uint32_t)BVHGB_SEARCH_BATCHED};
-    return from_status(bvhgb_bn13_create(s.cudaBVH.nodes, s.cudaBVH.numNodes, s.root, &cfg, &vWs, nullptr));
+    ErrorCode e = from_status(bvhgb_bn13_create(s.cudaBVH.nodes, s.cudaBVH.numNodes, s.root, &cfg, &vWs, nullptr));
+    if (e != ErrorCode::OK || vScorer.empty()) return e;
+    // learned selection: weights relative to the base path unless absolute
+    fs::path wp = fs::path(vScorer);
+    if (wp.is_relative()) wp = fs::path(s.basePath) / wp;
+    std::ifstream in(wp, std::ios::binary);
+    std::vector<float> w(BVHGB_MLP_PARAMS);
+    if (!in.read(reinterpret_cast<char *>(w.data()), (std::streamsize)(w.size() * sizeof(float)))) {
+      error("learnedScorer: cannot read " + std::to_string(BVHGB_MLP_PARAMS) + " floats from " + wp.string());
+      return ErrorCode::IO_ERROR;
+    }
+    int st = bvhgb_mlp_create(0, &vMlp);
+    if (!st) st = bvhgb_mlp_set_params(vMlp, w.data());
+    if (!st) st = bvhgb_bn13_set_scorer(vWs, vMlp);
+    if (!st) info("learned selection with " + wp.string());
+    return from_status(st);
   }
   ErrorCode runImpl(State &s) override {
     using clk = std::chrono::steady_clock;
@@ -657,6 +676,8 @@ class Bittner13GPU : public Command {
     info("Skipped " + std::to_string(st.skippedConflict) + " of " + std::to_string(s.optData.numTotal));
     bvhgb_bn13_destroy(vWs);
     vWs = nullptr;
+    bvhgb_mlp_destroy(vMlp);
+    vMlp = nullptr;
   }
 };
 

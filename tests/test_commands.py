@@ -115,3 +115,31 @@ def test_gpu_pipeline_matches_oracle(tmp_path, orc):
     assert len(sahs) == 5 and np.allclose(sahs, trace, rtol=1e-6)
     assert stats["numTotal"] == 4 * (int(np.float32(0.01) * np.float32(2 * n - 1)) // 32) * 32
     assert (tmp_path / "t_CUDA_cam_0.ppm").stat().st_size > 96 * 64 * 3
+
+
+@pytest.mark.gpu
+def test_learned_scorer_option(tmp_path, gpu):
+    """bittner13GPU{learnedScorer} selects with the scorer read from the file: same tree as the API."""
+    import torch
+    n = 12000
+    vert, faces = scenes.uniform_soup(n, seed=21)
+    meshio.write_mesh_v3(tmp_path / "scene", vert, faces)
+    m = gpu.Mlp(seed=11)
+    m.save(tmp_path / "scorer.f32")
+    cfg = _config(tmp_path, [
+        {"cmd": "load"}, {"cmd": "copyToGPU"}, {"cmd": "LBVH"},
+        {"cmd": "bittner13GPU", "options": {"maxNumStepps": 3, "learnedScorer": "scorer.f32"}},
+        {"cmd": "copyToHost"}, {"cmd": "BVHExport"}])
+    assert _run(cfg) == 0
+    got, _ = meshio.read_bvh_v9(tmp_path / "scene")
+    v = torch.from_numpy(vert).cuda()
+    f = torch.from_numpy(faces.view(np.int32)).cuda()
+    nodes = gpu.LBVH(n).build(v, f)
+    opt = gpu.Bittner13GPU(nodes)
+    opt.set_scorer(gpu.Mlp.load(tmp_path / "scorer.f32"))
+    opt.run(3)
+    want = gpu.nodes_to_numpy(nodes)
+    assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
+    cfg2 = _config(tmp_path, [{"cmd": "load"}, {"cmd": "copyToGPU"}, {"cmd": "LBVH"},
+                              {"cmd": "bittner13GPU", "options": {"maxNumStepps": 1, "learnedScorer": "missing.f32"}}])
+    assert _run(cfg2) == 2  # IO_ERROR stops the input
