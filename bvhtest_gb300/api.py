@@ -233,11 +233,20 @@ class Bittner13GPU:
                                         _stream(stream)), "bvhgb_bn13_gains")
         return (gain, tgt) if with_target else gain
 
-    def set_scorer(self, scorer: "Mlp | None"):
-        """Learned selection with 'scorer' (kept referenced here), or the plain measure for None."""
-        check(self.lib.bvhgb_bn13_set_scorer(self.ws, scorer.handle if scorer is not None else None),
+    def set_scorer(self, scorer: "Mlp | None", plain_every: int = 2):
+        """Learned selection with 'scorer' (kept referenced here); every plain_every-th iteration still
+        selects by the inefficiency (2 = alternate, 0 = scorer only). None restores the plain measure."""
+        check(self.lib.bvhgb_bn13_set_scorer(self.ws, scorer.handle if scorer is not None else None, plain_every),
               "bvhgb_bn13_set_scorer")
         self._scorer = scorer
+
+    @property
+    def iteration(self) -> int:
+        return self.lib.bvhgb_bn13_iteration(self.ws)
+
+    @iteration.setter
+    def iteration(self, it: int):
+        check(self.lib.bvhgb_bn13_set_iteration(self.ws, it), "bvhgb_bn13_set_iteration")
 
 
 MLP_PARAMS = 5825

@@ -28,6 +28,9 @@ int check_launch(const char *what) {
 }
 
 void count_launch(uint32_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+// Launches recorded while a stream was being captured did not run; the capture takes them back and
+// every replay of the graph adds its kernel count instead.
+void uncount_launches(uint64_t n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
 
 int sm_count() {
   int dev = 0, n = 0;

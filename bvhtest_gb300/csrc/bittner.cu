@@ -14,7 +14,9 @@
 //            arrivals on the way to the root (kFixTree3_1);
 //   refit  : the last arrival at a node recomputes its box from its children (kFixTree3_2) with
 //            acq_rel counters, so no box is read before it is final.
-// bvhgb_bn13_run captures one iteration into a CUDA graph and replays it.
+// bvhgb_bn13_run captures one iteration into a CUDA graph and replays it. With a learned scorer
+// set, iteration i selects by the scorer unless plainEvery > 0 and i % plainEvery == plainEvery - 1,
+// in which case it selects by the inefficiency (one graph per kind of iteration).
 #include <vector>
 
 #include "common.cuh"
@@ -851,9 +853,12 @@ struct bvhgb_bn13_workspace {
   uint32_t *valid = nullptr, *toFix = nullptr, *owner = nullptr, *counter = nullptr, *err = nullptr;
   HeapItem *heaps = nullptr;
   unsigned long long *stats = nullptr;
-  cudaGraphExec_t graph = nullptr;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [0] plain iteration, [1] learned iteration
   bvhgb_node *graphNodes = nullptr;
   uint32_t launchesPerIteration = 0;
+  uint32_t launchesKind[2] = {0, 0};  // kernels in each captured graph
+  uint64_t iteration = 0;  // iterations run so far (selects the kind of the next one)
+  uint32_t plainEvery = 0;
   std::vector<cudaEvent_t> evStart, evStop;  // per chunk, profileKernels only
   const bvhgb_mlp *scorer = nullptr;         // learned selection when set
   LrScratch lr;                              // feature scratch, allocated with the first scorer
@@ -861,9 +866,22 @@ struct bvhgb_bn13_workspace {
 
 namespace {
 
-int select_nodes(bvhgb_bn13_workspace *ws, const bvhgb_node *nodes, cudaStream_t s) {
+bool learned_iteration(const bvhgb_bn13_workspace *ws, uint64_t it) {
+  if (!ws->scorer) return false;
+  return ws->plainEvery == 0 || it % ws->plainEvery != ws->plainEvery - 1;
+}
+
+void drop_graphs(bvhgb_bn13_workspace *ws) {
+  for (auto &g : ws->graph) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+  ws->graphNodes = nullptr;
+}
+
+int select_kind(bvhgb_bn13_workspace *ws, const bvhgb_node *nodes, bool learned, cudaStream_t s) {
   if (ws->numInner == 0) return BVHGB_OK;
-  if (ws->scorer) {
+  if (learned) {
     const uint32_t numLeaves = ws->numNodes - ws->numInner;
     int st = lr_features(ws->lr, nodes, ws->numNodes, ws->root, ws->inner, ws->numInner, lr_inv_log2_leaves(numLeaves), s);
     if (!st) st = lr_score_keys(ws->scorer, ws->lr, nodes, ws->root, ws->inner, ws->numInner, ws->keys, ws->vals, s);
@@ -874,6 +892,10 @@ int select_nodes(bvhgb_bn13_workspace *ws, const bvhgb_node *nodes, cudaStream_t
     BVHGB_LAUNCH_CHECK("bn13 cost");
   }
   return sort_pairs(ws->sortTemp, ws->keys, ws->keysSorted, ws->vals, ws->todo, ws->numInner, 4, 0, 32, s);
+}
+
+int select_nodes(bvhgb_bn13_workspace *ws, const bvhgb_node *nodes, cudaStream_t s) {
+  return select_kind(ws, nodes, learned_iteration(ws, ws->iteration), s);
 }
 
 // Inside a stream capture the record must become an event node of the graph (external record);
@@ -916,11 +938,45 @@ int run_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t c, cudaStrea
   return BVHGB_OK;
 }
 
-int do_step(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, cudaStream_t s) {
-  int st = select_nodes(ws, nodes, s);
+int step_kind(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, bool learned, cudaStream_t s) {
+  int st = select_kind(ws, nodes, learned, s);
   if (st) return st;
   for (uint32_t c = 0; c < ws->numChunks; ++c)
     if ((st = run_chunk(ws, nodes, c, s))) return st;
+  return BVHGB_OK;
+}
+
+int do_step(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, cudaStream_t s) {
+  const int st = step_kind(ws, nodes, learned_iteration(ws, ws->iteration), s);
+  if (st == BVHGB_OK) ++ws->iteration;
+  return st;
+}
+
+// One iteration of the given kind captured on a private stream.
+int capture_step(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, bool learned, cudaGraphExec_t *out) {
+  int pst = sort_prepare();
+  if (pst) return pst;
+  cudaStream_t cap = nullptr;
+  BVHGB_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+  int st = BVHGB_OK;
+  const uint64_t before = bvhgb_launch_count();
+  if (e == cudaSuccess) {
+    st = step_kind(ws, nodes, learned, cap);
+    e = cudaStreamEndCapture(cap, &g);
+  }
+  ws->launchesPerIteration = ws->launchesKind[learned ? 1 : 0] = (uint32_t)(bvhgb_launch_count() - before);
+  uncount_launches(ws->launchesPerIteration);
+  if (e == cudaSuccess && st == BVHGB_OK) e = cudaGraphInstantiate(out, g, 0);
+  if (g) cudaGraphDestroy(g);
+  cudaStreamDestroy(cap);
+  if (st) return st;
+  if (e != cudaSuccess) {
+    set_last_error("bvhgb_bn13_run capture", e);
+    *out = nullptr;
+    return BVHGB_CUDA_ERROR;
+  }
   return BVHGB_OK;
 }
 
@@ -1016,7 +1072,7 @@ extern "C" BVHGB_API int bvhgb_bn13_create(const bvhgb_node *nodes, uint32_t num
 
 extern "C" BVHGB_API int bvhgb_bn13_destroy(bvhgb_bn13_workspace *ws) {
   if (!ws) return BVHGB_OK;
-  if (ws->graph) cudaGraphExecDestroy(ws->graph);
+  drop_graphs(ws);
   for (cudaEvent_t ev : ws->evStart)
     if (ev) cudaEventDestroy(ev);
   for (cudaEvent_t ev : ws->evStop)
@@ -1085,38 +1141,18 @@ extern "C" BVHGB_API int bvhgb_bn13_run(bvhgb_bn13_workspace *ws, bvhgb_node *no
   if (!ws || !nodes) return BVHGB_INVALID_ARGUMENT;
   if (iterations == 0) return BVHGB_OK;
   cudaStream_t s = as_stream(stream);
-  // Capture one iteration on a private stream, then replay it on the caller's stream.
-  if (ws->graph && ws->graphNodes != nodes) {
-    cudaGraphExecDestroy(ws->graph);
-    ws->graph = nullptr;
-  }
-  if (!ws->graph) {
-    int pst = sort_prepare();
-    if (pst) return pst;
-    cudaStream_t cap = nullptr;
-    BVHGB_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-    cudaGraph_t g = nullptr;
-    cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-    int st = BVHGB_OK;
-    const uint64_t before = bvhgb_launch_count();
-    if (e == cudaSuccess) {
-      st = do_step(ws, nodes, cap);
-      e = cudaStreamEndCapture(cap, &g);
-    }
-    ws->launchesPerIteration = (uint32_t)(bvhgb_launch_count() - before);
-    if (e == cudaSuccess && st == BVHGB_OK) e = cudaGraphInstantiate(&ws->graph, g, 0);
-    if (g) cudaGraphDestroy(g);
-    cudaStreamDestroy(cap);
-    if (st) return st;
-    if (e != cudaSuccess) {
-      set_last_error("bvhgb_bn13_run capture", e);
-      ws->graph = nullptr;
-      return BVHGB_CUDA_ERROR;
-    }
-    ws->graphNodes = nodes;
-  }
+  // Each kind of iteration is captured once on a private stream, then replayed on the caller's.
+  if (ws->graphNodes != nodes) drop_graphs(ws);
+  ws->graphNodes = nodes;
   for (uint32_t i = 0; i < iterations; ++i) {
-    BVHGB_CUDA_TRY(cudaGraphLaunch(ws->graph, s));
+    const int kind = learned_iteration(ws, ws->iteration) ? 1 : 0;
+    if (!ws->graph[kind]) {
+      const int st = capture_step(ws, nodes, kind == 1, &ws->graph[kind]);
+      if (st) return st;
+    }
+    BVHGB_CUDA_TRY(cudaGraphLaunch(ws->graph[kind], s));
+    count_launch(ws->launchesKind[kind]);
+    ++ws->iteration;
   }
   return BVHGB_OK;
 }
@@ -1159,18 +1195,24 @@ extern "C" BVHGB_API int bvhgb_bn13_read_inner(const bvhgb_bn13_workspace *ws, u
   return BVHGB_OK;
 }
 
-extern "C" BVHGB_API int bvhgb_bn13_set_scorer(bvhgb_bn13_workspace *ws, const bvhgb_mlp *scorer) {
+extern "C" BVHGB_API int bvhgb_bn13_set_scorer(bvhgb_bn13_workspace *ws, const bvhgb_mlp *scorer,
+                                               uint32_t plainEvery) {
   if (!ws) return BVHGB_INVALID_ARGUMENT;
   if (scorer && ws->lr.numNodes < ws->numNodes) {
     const int st = lr_scratch_alloc(ws->lr, ws->numNodes);
     if (st) return st;
   }
-  if (ws->scorer != scorer && ws->graph) {
-    cudaGraphExecDestroy(ws->graph);
-    ws->graph = nullptr;
-    ws->graphNodes = nullptr;
-  }
+  if (ws->scorer != scorer) drop_graphs(ws);
   ws->scorer = scorer;
+  ws->plainEvery = plainEvery;
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API uint64_t bvhgb_bn13_iteration(const bvhgb_bn13_workspace *ws) { return ws ? ws->iteration : 0; }
+
+extern "C" BVHGB_API int bvhgb_bn13_set_iteration(bvhgb_bn13_workspace *ws, uint64_t iteration) {
+  if (!ws) return BVHGB_INVALID_ARGUMENT;
+  ws->iteration = iteration;
   return BVHGB_OK;
 }
 

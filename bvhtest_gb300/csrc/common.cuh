@@ -128,6 +128,7 @@ namespace bvhgb {
 void set_last_error(const char *what, cudaError_t e);
 int check_launch(const char *what);
 void count_launch(uint32_t n = 1);
+void uncount_launches(uint64_t n);
 inline cudaStream_t as_stream(bvhgb_stream s) { return reinterpret_cast<cudaStream_t>(s); }
 inline uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 int sm_count();

@@ -705,7 +705,7 @@ extern "C" BVHGB_API int bvhgb_mlp_train(bvhgb_mlp *m, const uint16_t *x, const 
     return BVHGB_CUDA_ERROR;
   }
   for (uint32_t k = 0; k < steps && e == cudaSuccess; ++k) e = cudaGraphLaunch(exec, s);
-  count_launch(3u * steps);
+  count_launch(3u * steps);  // (the capture itself recorded none: its launches are not counted)
   if (e == cudaSuccess && lossHistory) e = cudaMemcpyAsync(lossHistory, m->loss, 4ull * steps, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   cudaGraphExecDestroy(exec);

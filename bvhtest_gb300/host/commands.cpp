@@ -575,6 +575,7 @@ class Bittner13GPU : public Command {
        vLocalPatchCPY = false;
   std::string vSearch = "batched";
   std::string vScorer;  // learned scorer weights (5825 little-endian float32); empty = inefficiency
+  uint32_t vPlainEvery = 2;  // with a scorer: every k-th iteration selects by the inefficiency
   bvhgb_bn13_workspace *vWs = nullptr;
   bvhgb_mlp *vMlp = nullptr;
 
@@ -598,6 +599,7 @@ class Bittner13GPU : public Command {
     vLocalPatchCPY = j.value("localPatchCPY", vLocalPatchCPY);
     vSearch = j.value("searchMode", vSearch);
     vScorer = j.value("learnedScorer", vScorer);
+    vPlainEvery = j.value("learnedPlainEvery", vPlainEvery);
     if (vBatchPercent <= 0.01f) vBatchPercent = 0.01f;
     if (vBatchPercent >= 75.0f) vBatchPercent = 75.0f;
   }
@@ -617,6 +619,7 @@ class Bittner13GPU : public Command {
     o["localPatchCPY"] = vLocalPatchCPY;
     o["searchMode"] = vSearch;
     o["learnedScorer"] = vScorer;
+    o["learnedPlainEvery"] = vPlainEvery;
     return o;
   }
 
@@ -647,7 +650,7 @@ class Bittner13GPU : public Command {
     }
     int st = bvhgb_mlp_create(0, &vMlp);
     if (!st) st = bvhgb_mlp_set_params(vMlp, w.data());
-    if (!st) st = bvhgb_bn13_set_scorer(vWs, vMlp);
+    if (!st) st = bvhgb_bn13_set_scorer(vWs, vMlp, vPlainEvery);
     if (!st) info("learned selection with " + wp.string());
     return from_status(st);
   }

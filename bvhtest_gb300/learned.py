@@ -39,11 +39,15 @@ def uniform_scene_tree(n: int, seed: int, morton_bits=30, topology="refCompat", 
     return v, f, nodes
 
 
-def log_pairs(trees, iterations=100, every=4, batch_percent=1.0, num_chunks=32, with_sah=False) -> TrainingSet:
+def log_pairs(trees, iterations=100, every=4, batch_percent=1.0, num_chunks=32, with_sah=False, sample=1.0,
+              seed=0) -> TrainingSet:
     """Run the plain optimizer on each node tensor of 'trees' for 'iterations' iterations; before every
-    'every'-th iteration log the feature rows and realised-gain targets of all inner nodes."""
+    'every'-th iteration log the feature rows and realised-gain targets of all inner nodes, or of a
+    random fraction 'sample' of them (drawn on the device from 'seed')."""
     xs, ts, sahs = [], [], []
     feats, feats_cap = None, 0
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
     t0 = time.perf_counter()
     count = 0
     for nodes in trees:
@@ -55,8 +59,13 @@ def log_pairs(trees, iterations=100, every=4, batch_percent=1.0, num_chunks=32, 
         trace = []
         for it in range(iterations):
             if it % every == 0:
-                xs.append(feats(nodes, inner))
-                _, tgt = opt.gains(inner, with_target=True)
+                x = feats(nodes, inner)
+                cand = inner
+                if sample < 1.0:
+                    pick = torch.randperm(inner.shape[0], device="cuda", generator=gen)[: max(1, int(sample * inner.shape[0]))]
+                    x, cand = x[pick], inner[pick]
+                xs.append(x)
+                _, tgt = opt.gains(cand, with_target=True)
                 ts.append(tgt)
             if with_sah:
                 trace.append(api.calc_sah(nodes))

@@ -98,7 +98,9 @@ PROTOS = {
     "bvhgb_bn13_search_time": (I32, [VP, C.POINTER(F32), C.POINTER(U32)]),
     "bvhgb_bn13_gains": (I32, [VP, VP, VP, U32, VP, VP, VP]),
     "bvhgb_bn13_read_inner": (I32, [VP, VP, U32, C.POINTER(U32), VP]),
-    "bvhgb_bn13_set_scorer": (I32, [VP, VP]),
+    "bvhgb_bn13_set_scorer": (I32, [VP, VP, U32]),
+    "bvhgb_bn13_iteration": (U64, [VP]),
+    "bvhgb_bn13_set_iteration": (I32, [VP, U64]),
     "bvhgb_bn13_read_selection": (I32, [VP, VP, U32, VP]),
     "bvhgb_bn13_set_selection": (I32, [VP, VP, U32, VP]),
     "bvhgb_mlp_create": (I32, [U64, C.POINTER(VP)]),

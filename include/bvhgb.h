@@ -110,7 +110,8 @@ BVHGB_API const char *bvhgb_version(void);
 BVHGB_API const char *bvhgb_status_string(int status);
 /* Last CUDA error text seen by this thread (empty if none). */
 BVHGB_API const char *bvhgb_last_error(void);
-/* Number of kernels this library has launched (process-wide, monotonic). */
+/* Number of kernels this library has launched (process-wide, monotonic; a replayed CUDA graph
+ * counts the kernels it holds, a capture counts none). */
 BVHGB_API uint64_t bvhgb_launch_count(void);
 
 /* ---- LBVH build (lib/builder/LBVH_CUDA.hpp:49-59, LBVH.cpp:28-55) ------------------------- */
@@ -297,10 +298,17 @@ BVHGB_API int bvhgb_bn13_gains(bvhgb_bn13_workspace *ws, const bvhgb_node *nodes
  * copies their ids in ascending order (the optimizer's inner-node list) on 'stream'. */
 BVHGB_API int bvhgb_bn13_read_inner(const bvhgb_bn13_workspace *ws, uint32_t *out, uint32_t capacity,
                                     uint32_t *numInner, bvhgb_stream stream);
-/* Select each iteration's batch by the scorer's predicted reduction (its output, the target scale
- * above; descending, ties by node id) instead of the inefficiency; NULL restores the plain measure.
- * The workspace keeps the pointer: the scorer must outlive its use. Drops a captured graph. */
-BVHGB_API int bvhgb_bn13_set_scorer(bvhgb_bn13_workspace *ws, const bvhgb_mlp *scorer);
+/* Select batches by the scorer's predicted reduction (its output, the target scale above;
+ * descending, ties by node id) instead of the inefficiency. With plainEvery = k > 0, every k-th
+ * iteration (iteration i with i % k == k - 1, counted from the workspace's creation) still selects
+ * by the inefficiency: the plain measure stays in the loop and picks the nodes the scorer misses
+ * (k = 2, alternating, is the recommended policy; 0 = scorer only). NULL restores the plain
+ * measure. The workspace keeps the pointer: the scorer must outlive its use. */
+BVHGB_API int bvhgb_bn13_set_scorer(bvhgb_bn13_workspace *ws, const bvhgb_mlp *scorer, uint32_t plainEvery);
+/* Iterations run on this workspace so far (step and run; decides the kind of the next one), and
+ * its reset for a new optimisation of a rebuilt tree of the same mesh. */
+BVHGB_API uint64_t bvhgb_bn13_iteration(const bvhgb_bn13_workspace *ws);
+BVHGB_API int bvhgb_bn13_set_iteration(bvhgb_bn13_workspace *ws, uint64_t iteration);
 /* Replaces the selection of the current iteration by a caller order (numInner node ids, device, in
  * batch position order) for the following bvhgb_bn13_chunk calls; a later select overwrites it. */
 BVHGB_API int bvhgb_bn13_set_selection(bvhgb_bn13_workspace *ws, const uint32_t *order, uint32_t n,

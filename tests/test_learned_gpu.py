@@ -189,3 +189,25 @@ def test_trained_scorer_beats_the_plain_measure(gpu):
         lo.set_scorer(m)
         lo.run(100)
         assert gpu.calc_sah(full) < 0.97 * target
+
+
+def test_policy_alternates_learned_and_plain_iterations(gpu):
+    import torch
+    _, _, nodes = _tree(gpu, 8192, seed=34)
+    m = gpu.Mlp(seed=12)
+    opt = gpu.Bittner13GPU(nodes)
+    opt.set_scorer(m, 2)
+    plain = gpu.Bittner13GPU(nodes)
+    for it in range(4):
+        assert opt.iteration == it
+        opt.select()
+        plain.select()
+        same = torch.equal(opt.selection(), plain.selection())
+        assert same == (it % 2 == 1), it  # odd iterations select by the inefficiency
+        opt.step()
+    opt.iteration = 0
+    assert opt.iteration == 0
+    opt.set_scorer(m, 0)  # scorer only
+    opt.select()
+    plain.select()
+    assert not torch.equal(opt.selection(), plain.selection())
