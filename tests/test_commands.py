@@ -129,7 +129,7 @@ def test_learned_scorer_option(tmp_path, gpu):
     cfg = _config(tmp_path, [
         {"cmd": "load"}, {"cmd": "copyToGPU"}, {"cmd": "LBVH"},
         {"cmd": "bittner13GPU", "options": {"maxNumStepps": 3, "learnedScorer": "scorer.f32"}},
-        {"cmd": "copyToHost"}, {"cmd": "BVHExport"}])
+        {"cmd": "copyToHost", "options": {"fixLevels": False}}, {"cmd": "BVHExport"}])
     assert _run(cfg) == 0
     got, _ = meshio.read_bvh_v9(tmp_path / "scene")
     v = torch.from_numpy(vert).cuda()
