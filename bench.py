@@ -383,28 +383,6 @@ def run_ours(args, w, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
-def scorer_for_large_scene(dev):
-    """The scorer of the large-scene family: trained on pairs logged from plain runs over 8 seeded
-    262,144-triangle scenes of the same generator (a 181 x 181 grid + a 64-component mixture)."""
-    import torch
-    from bvhtest_gb300 import api, learned, scenes
-
-    def trees():
-        b = api.LBVH(262144, 63, "karras")
-        for s in range(8):
-            v_h, f_h = scenes.large_scene(262144, seed=10 + s, grid_cells=181)
-            yield b.build(torch.from_numpy(v_h).to(dev), torch.from_numpy(f_h.view(np.int32)).to(dev))
-
-    data = learned.log_pairs(trees(), iterations=200, every=8)
-    pairs, log_s = int(data.x.shape[0]), data.seconds
-    scorer, hist, train_s = learned.train(data, steps=20000, batch=8192, lr=1e-3, weight_decay=1e-4)
-    del data
-    torch.cuda.empty_cache()
-    return scorer, {"scenes": 8, "triangles_per_scene": 262144, "pairs": pairs, "log_s": round(log_s, 2),
-                    "steps": 20000, "batch": 8192, "lr": 1e-3, "weight_decay": 1e-4, "train_s": round(train_s, 2),
-                    "loss_first": round(float(hist[:100].mean()), 4), "loss_last": round(float(hist[-100:].mean()), 4)}
-
-
 def first_hit(opt, nodes, target, max_iters, rebuild):
     """Untimed calibration: iterations until the SAH first drops to <= target (None if never)."""
     from bvhtest_gb300 import api
@@ -426,7 +404,8 @@ def learned_large(args, w, dev, flush, stream, vert, faces, nodes, lbvh, target,
 
     n = int(w["faces"].shape[0])
     n_nodes = 2 * n - 1
-    scorer, train = scorer_for_large_scene(dev)
+    from bvhtest_gb300 import learned
+    scorer, train = learned.train_family("large")
     rebuild = lambda: lbvh.build(vert, faces, nodes)
     lopt = api.Bittner13GPU(rebuild(), num_nodes=n_nodes)
     lopt.set_scorer(scorer, 2)
@@ -535,13 +514,7 @@ def learned_arm(args, dev, flush, stream):
     from bvhtest_gb300 import api, learned, scenes
 
     n = LEARNED_N
-    builder = api.LBVH(n, 30, "refCompat")
-    trees = (learned.uniform_scene_tree(n, 1000 + s, builder=builder)[2].clone() for s in range(LEARNED_SCENES))
-    data = learned.log_pairs(trees, iterations=LEARNED_ITERS, every=LEARNED_EVERY)
-    pairs, log_s = int(data.x.shape[0]), data.seconds
-    scorer, hist, train_s = learned.train(data, steps=LEARNED_STEPS, batch=8192, lr=1e-3, weight_decay=1e-4)
-    del data
-    torch.cuda.empty_cache()
+    scorer, train = learned.train_family("uniform", steps=LEARNED_STEPS)
 
     vert_h, faces_h = scenes.uniform_soup(n, seed=1)  # the training scenes use seeds 1000..1031
     vert = torch.from_numpy(vert_h).to(dev)
@@ -606,9 +579,7 @@ def learned_arm(args, dev, flush, stream):
                     "policy": "scorer iterations alternating with plain ones (plainEvery 2)"},
         "wall_time_ratio": round(learned_ms / first_ms, 4),
         "wall_time_ratio_vs_100_plain": round(learned_ms / plain_ms, 4),
-        "train": {"scenes": LEARNED_SCENES, "pairs": pairs, "log_s": round(log_s, 2), "steps": LEARNED_STEPS,
-                  "batch": 8192, "lr": 1e-3, "weight_decay": 1e-4, "train_s": round(train_s, 2),
-                  "loss_first": round(float(hist[:100].mean()), 4), "loss_last": round(float(hist[-100:].mean()), 4)},
+        "train": train,
     }
 
 
@@ -624,6 +595,9 @@ def run_phase(args, w):
     lbvh = api.LBVH(n, w["bits"], w["topo"])
     lbvh.build(vert, faces, nodes)
     opt = api.Bittner13GPU(nodes, num_nodes=2 * n - 1) if args.only == "optimize" else None
+    if opt is not None and args.scorer:
+        scorer = api.Mlp.load(args.scorer)
+        opt.set_scorer(scorer, args.plain_every)
     times = []
     for i in range(args.warmup + args.steps):
         torch.cuda.synchronize()
@@ -632,6 +606,8 @@ def run_phase(args, w):
         if args.only == "build":
             lbvh.build(vert, faces, nodes)
         elif args.only == "optimize":
+            lbvh.build(vert, faces, nodes)
+            opt.iteration = 0
             opt.run(w["iters"])
         else:
             img, hits = api.trace_image(nodes, vert, faces, w["camera"], num_nodes=2 * n - 1)
@@ -658,6 +634,8 @@ def main():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-scorer comparison")
     ap.add_argument("--only", choices=["build", "optimize", "trace"], default=None,
                     help="repeat one phase only and print its time (profiling runs; no benchmark record)")
+    ap.add_argument("--scorer", default=None, help="with --only optimize: learned selection with these weights")
+    ap.add_argument("--plain-every", type=int, default=2, help="with --scorer: every k-th iteration is plain")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -103,3 +103,58 @@ def optimize_until(nodes: torch.Tensor, target_sah: float, max_iterations: int, 
         trace.append(api.calc_sah(nodes))
     opt.close()
     return (it if trace[-1] <= target_sah else None), trace
+
+
+# ---- training families -----------------------------------------------------------------------
+
+def uniform_family(n=65536, count=32, seed0=1000):
+    """Config-4 training scenes: uniform soups of n triangles, 30-bit Morton, refCompat LBVH."""
+    builder = api.LBVH(n, 30, "refCompat")
+    for s in range(count):
+        yield uniform_scene_tree(n, seed0 + s, builder=builder)[2].clone()
+
+
+def large_family(n=262144, count=8, seed0=10, grid_cells=181):
+    """Scenes of the large-scene generator at n triangles (a grid_cells^2 ground grid + a 64-component
+    mixture), 63-bit Morton, karras LBVH."""
+    b = api.LBVH(n, 63, "karras")
+    for s in range(count):
+        v_h, f_h = scenes.large_scene(n, seed=seed0 + s, grid_cells=grid_cells)
+        yield b.build(torch.from_numpy(v_h).cuda(), torch.from_numpy(f_h.view(np.int32)).cuda())
+
+
+FAMILIES = {
+    "uniform": dict(trees=uniform_family, count=32, iterations=100, every=4),
+    "large": dict(trees=large_family, count=8, iterations=200, every=8),
+}
+
+
+def train_family(name: str, steps=20000, batch=8192, lr=1e-3, weight_decay=1e-4, seed=0):
+    """Log pairs from plain runs over the family's scenes and train a scorer; returns (mlp, info)."""
+    f = FAMILIES[name]
+    data = log_pairs(f["trees"](count=f["count"]), iterations=f["iterations"], every=f["every"])
+    pairs, log_s = int(data.x.shape[0]), data.seconds
+    m, hist, train_s = train(data, steps=steps, batch=batch, lr=lr, weight_decay=weight_decay, seed=seed)
+    del data
+    torch.cuda.empty_cache()
+    return m, {"family": name, "scenes": f["count"], "pairs": pairs, "log_s": round(log_s, 2),
+               "steps": steps, "batch": batch, "lr": lr, "weight_decay": weight_decay, "train_s": round(train_s, 2),
+               "loss_first": round(float(hist[:100].mean()), 4), "loss_last": round(float(hist[-100:].mean()), 4)}
+
+
+def main(argv=None):
+    import argparse
+    ap = argparse.ArgumentParser(prog="python -m bvhtest_gb300.learned")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    t = sub.add_parser("train", help="log pairs from plain runs of a scene family and train a scorer")
+    t.add_argument("--family", choices=sorted(FAMILIES), required=True)
+    t.add_argument("--out", required=True, help="weights file (5825 little-endian float32)")
+    t.add_argument("--steps", type=int, default=20000)
+    a = ap.parse_args(argv)
+    m, info = train_family(a.family, steps=a.steps)
+    m.save(a.out)
+    print(info, flush=True)
+
+
+if __name__ == "__main__":
+    main()
