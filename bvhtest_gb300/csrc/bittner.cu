@@ -652,34 +652,37 @@ __global__ void apply_kernel(bvhgb_node *t, const PatchOut *__restrict__ in, uin
   atomicAdd(&stats[S_APPLIED], 1ull);
 }
 
-// Release the claims and count, per node, how many dirty paths arrive (kFixTree3_1).
+// Release the claims and count, per node, how many dirty paths arrive (kFixTree3_1). One thread
+// per dirty path (3 per item); the parent link is loaded together with the counter update, so a
+// level costs one round trip.
 __global__ void count_kernel(const bvhgb_node *__restrict__ t, uint32_t root, const PatchOut *__restrict__ in,
                              const uint32_t *__restrict__ toFix, uint32_t *__restrict__ owner,
                              uint32_t *__restrict__ counter, uint32_t chunkSize, uint32_t numNodes,
                              uint32_t *__restrict__ err) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= chunkSize) return;
-#pragma unroll
-  for (int s = 0; s < NSLOT; ++s) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * chunkSize) return;
+  const uint32_t k = i / 3, j = i - 3 * k;
+  for (uint32_t s = j; s < (uint32_t)NSLOT; s += 3) {
     const uint32_t x = in[k].idx[s];
     if (x != kNone) owner[x] = kNone;
   }
-  for (int j = 0; j < 3; ++j) {
-    uint32_t x = toFix[3 * k + j];
-    if (x == kNone) continue;
-    for (uint32_t steps = 0;; ++steps) {
-      if (x >= numNodes || steps > numNodes) {
-        atomicOr(err, kErrBadIndex);
-        break;
-      }
-      if (atomicAdd(&counter[x], 1u) != 0u) break;
-      if (x == root) break;
-      x = t[x].parent;
+  uint32_t x = toFix[i];
+  if (x == kNone) return;
+  for (uint32_t steps = 0;; ++steps) {
+    if (x >= numNodes || steps > numNodes) {
+      atomicOr(err, kErrBadIndex);
+      break;
     }
+    const uint32_t px = t[x].parent;  // issued before the update; the links are final here
+    if (atomicAdd(&counter[x], 1u) != 0u) break;
+    if (x == root) break;
+    x = px;
   }
 }
 
-// The last path to arrive at a node recomputes its box (kFixTree3_2).
+// The last path to arrive at a node recomputes its box (kFixTree3_2). A node's links do not change
+// in this launch, so they are read before its counter; after the acq_rel update only the other
+// child's box is loaded (the box of the child the path came from is still in registers).
 __global__ void refit_kernel(bvhgb_node *t, uint32_t root, const uint32_t *__restrict__ toFix,
                              uint32_t *__restrict__ counter, uint32_t chunkSize, uint32_t numNodes,
                              uint32_t *__restrict__ err) {
@@ -687,24 +690,32 @@ __global__ void refit_kernel(bvhgb_node *t, uint32_t root, const uint32_t *__res
   if (i >= 3 * chunkSize) return;
   uint32_t x = toFix[i];
   if (x == kNone) return;
+  uint32_t from = kNone;  // child the path came from, whose box is 'cur'
+  Box cur;
   for (uint32_t steps = 0;; ++steps) {
     if (x >= numNodes || steps > numNodes) {
       atomicOr(err, kErrBadIndex);
       return;
     }
+    const float4 w1 = __ldcg(reinterpret_cast<const float4 *>(t + x) + 1);  // mx.y mx.z parent left
+    const float4 w2 = __ldcg(reinterpret_cast<const float4 *>(t + x) + 2);  // right flags level sa
     if (atom_add_acq_rel(&counter[x], 0xFFFFFFFFu) != 1u) return;  // not the last arrival
-    const uint32_t l = ld_cg(&t[x].left), r = ld_cg(&t[x].right);
-    if (ld_cg(reinterpret_cast<const uint32_t *>(&t[x].isLeafFlag)) & 0xFFFFu) return;
-    Box b = load_box_cg(t + l);
-    const Box rb = load_box_cg(t + r);
+    const uint32_t parent = __float_as_uint(w1.z), l = __float_as_uint(w1.w), r = __float_as_uint(w2.x);
+    if ((__float_as_uint(w2.y) & 0xFFFFu) || l >= numNodes || r >= numNodes) {
+      if (!(__float_as_uint(w2.y) & 0xFFFFu)) atomicOr(err, kErrBadIndex);
+      return;
+    }
+    Box b = from == l ? cur : load_box_cg(t + l);
+    const Box rb = from == r ? cur : load_box_cg(t + r);
     merge_into(b, rb);
     float4 *p = reinterpret_cast<float4 *>(t + x);
-    const float4 old1 = __ldcg(p + 1);
     p[0] = make_float4(b.mn[0], b.mn[1], b.mn[2], b.mx[0]);
-    p[1] = make_float4(b.mx[1], b.mx[2], old1.z, old1.w);
+    p[1] = make_float4(b.mx[1], b.mx[2], w1.z, w1.w);
     t[x].surfaceArea = surface_area(b);
     if (x == root) return;
-    x = ld_cg(&t[x].parent);
+    from = x;
+    cur = b;
+    x = parent;
   }
 }
 
@@ -930,7 +941,8 @@ int run_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t c, cudaStrea
   if (prof) BVHGB_CUDA_TRY(record_event(ws->evStop[c], s));
   apply_kernel<<<grid, bs, 0, s>>>(nodes, ws->patches, ws->valid, ws->toFix, ws->owner, cs, ws->stats);
   BVHGB_LAUNCH_CHECK("bn13 apply");
-  count_kernel<<<grid, bs, 0, s>>>(nodes, ws->root, ws->patches, ws->toFix, ws->owner, ws->counter, cs, ws->numNodes,
+  count_kernel<<<ceil_div(3ull * cs, bs), bs, 0, s>>>(nodes, ws->root, ws->patches, ws->toFix, ws->owner, ws->counter,
+                                                      cs, ws->numNodes,
                                    ws->err);
   BVHGB_LAUNCH_CHECK("bn13 count");
   refit_kernel<<<ceil_div(3ull * cs, bs), bs, 0, s>>>(nodes, ws->root, ws->toFix, ws->counter, cs, ws->numNodes, ws->err);
