@@ -5,10 +5,13 @@
 //   1. one read of all keys builds the digit histograms of every pass;
 //   2. a tiny scan turns them into global digit offsets;
 //   3. per pass, one kernel: each CTA takes the next tile index from an atomic counter (so the
-//      tiles it looks back on are already running), ranks its 4096 keys stably with warp
-//      match/ballot, publishes per-digit counts, resolves its exclusive prefix by decoupled
-//      look-back (bounded spin), stages the tile in shared memory in digit order and writes it
-//      out in runs, so each digit's run is a contiguous store.
+//      tiles it looks back on are already running), ranks its 8192 keys stably (per item, the lanes
+//      holding the same digit are found with 9 ballots and a warp-private counter per digit is
+//      advanced by one shared-memory atomic of the lowest such lane; the atomics of all items are
+//      issued before any result is used), publishes per-digit counts, resolves its exclusive prefix
+//      by decoupled look-back (four predecessors per round trip, bounded spin), stages the tile in
+//      shared memory in digit order and writes it out in runs, so each digit's run is a contiguous
+//      store.
 #include "common.cuh"
 #include "sort.cuh"
 
@@ -16,9 +19,9 @@ namespace bvhgb {
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;
 constexpr int kItems = 16;
-constexpr int kTile = kThreads * kItems;  // 4096 keys per CTA
+constexpr int kTile = kThreads * kItems;  // 8192 keys per CTA
 constexpr int kWarps = kThreads / 32;
 constexpr int kRadix = 256;
 constexpr int kBins = kRadix + 1;  // + a bin for padding keys of the last tile
@@ -96,13 +99,15 @@ struct OnesweepSmem {
   uint32_t warpHist[kWarps][kBins];
   uint32_t tileStart[kRadix];
   uint32_t globalBase[kRadix];
+  uint32_t scanTot[kRadix / 32];
   uint32_t tileIdx;
   K keys[kTile];
   uint32_t vals[kTile];
 };
+static_assert(kThreads >= kRadix, "one thread per digit in the look-back");
 
 template <typename K>
-__global__ void __launch_bounds__(kThreads) onesweep_kernel(const K *__restrict__ keysIn, K *__restrict__ keysOut,
+__global__ void __launch_bounds__(kThreads, 1) onesweep_kernel(const K *__restrict__ keysIn, K *__restrict__ keysOut,
                                                             const uint32_t *__restrict__ valsIn,
                                                             uint32_t *__restrict__ valsOut, uint32_t n,
                                                             uint32_t shift, uint32_t mask,
@@ -135,25 +140,36 @@ __global__ void __launch_bounds__(kThreads) onesweep_kernel(const K *__restrict_
       dig[j] = kRadix;  // padding bin
     }
   }
-  // Stable rank within the warp: items in order, lanes in order.
+  // Stable rank within the warp: items in order, lanes in order. Peers of an item are the lanes
+  // with the same digit (9 ballots: 8 digit bits + the padding bin); the lowest of them advances
+  // the warp's counter for that digit by their number. All atomics are issued first, in item
+  // order (__syncwarp orders them), and their results are used afterwards.
   const uint32_t ltMask = (1u << lane) - 1u;
+  uint32_t old[kItems], peersOf[kItems];
 #pragma unroll
   for (int j = 0; j < kItems; ++j) {
-    uint32_t peers = __match_any_sync(0xFFFFFFFFu, dig[j]);
-    uint32_t leader = __ffs(peers) - 1u;
-    uint32_t before = 0;
-    if (lane == leader) {
-      before = sm.warpHist[warp][dig[j]];
-      sm.warpHist[warp][dig[j]] = before + __popc(peers);
+    uint32_t peers = 0xFFFFFFFFu;
+#pragma unroll
+    for (int bit = 0; bit < 9; ++bit) {
+      const bool on = (dig[j] >> bit) & 1u;
+      const uint32_t bal = __ballot_sync(0xFFFFFFFFu, on);
+      peers &= on ? bal : ~bal;
     }
-    before = __shfl_sync(peers, before, leader);
-    loc[j] = before + __popc(peers & ltMask);
+    peersOf[j] = peers;
+    old[j] = 0;
+    if ((peers & ltMask) == 0) old[j] = atomicAdd(&sm.warpHist[warp][dig[j]], (uint32_t)__popc(peers));
     __syncwarp();
+  }
+#pragma unroll
+  for (int j = 0; j < kItems; ++j) {
+    const uint32_t leader = __ffs(peersOf[j]) - 1u;
+    loc[j] = __shfl_sync(0xFFFFFFFFu, old[j], leader) + __popc(peersOf[j] & ltMask);
   }
   __syncthreads();
 
-  // Per digit: exclusive over warps, tile count, publish, look back.
-  uint32_t count = 0;
+  // Per digit (one thread each): exclusive over warps, tile count, publish, look back; the tile's
+  // exclusive scan over digits runs at the same time (a warp scan per 32 digits).
+  uint32_t count = 0, incl = 0;
   if (threadIdx.x < kRadix) {
     const uint32_t d = threadIdx.x;
 #pragma unroll
@@ -164,45 +180,56 @@ __global__ void __launch_bounds__(kThreads) onesweep_kernel(const K *__restrict_
     }
     uint32_t *st = status + (size_t)tile * kRadix + d;
     st_release(st, (tile == 0 ? kFlagInc : kFlagAgg) | count);
+    incl = count;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+      if (lane >= (uint32_t)o) incl += y;
+    }
+    if (lane == 31) sm.scanTot[warp] = incl;
     uint32_t excl = 0;
     if (tile > 0) {
-      uint32_t pred = tile - 1;
-      for (;;) {
-        const uint32_t *ps = status + (size_t)pred * kRadix + d;
-        uint32_t v = ld_acquire(ps);
-        uint32_t spins = 0;
-        while ((v & kFlagMask) == 0u) {
-          if (++spins > kSpinLimit) {
-            atomicOr(err, kErrTimeout);
+      int64_t pred = (int64_t)tile - 1;
+      bool done = false;
+      while (!done) {
+        uint32_t v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = pred - q >= 0 ? ld_acquire(status + (size_t)(pred - q) * kRadix + d) : kFlagInc;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          if (done) break;
+          if (pred - q < 0) {
+            done = true;
             break;
           }
-          __nanosleep(32);
-          v = ld_acquire(ps);
+          const uint32_t *ps = status + (size_t)(pred - q) * kRadix + d;
+          uint32_t spins = 0;
+          while ((v[q] & kFlagMask) == 0u) {
+            if (++spins > kSpinLimit) {
+              atomicOr(err, kErrTimeout);
+              break;
+            }
+            __nanosleep(32);
+            v[q] = ld_acquire(ps);
+          }
+          if ((v[q] & kFlagMask) == 0u) {
+            done = true;
+            break;
+          }
+          excl += v[q] & kValMask;
+          if (v[q] & kFlagInc) done = true;
         }
-        excl += v & kValMask;
-        if ((v & kFlagInc) || pred == 0 || (v & kFlagMask) == 0u) break;
-        --pred;
+        pred -= 4;
       }
       st_release(st, kFlagInc | (excl + count));
     }
     sm.globalBase[d] = offsets[d] + excl;
-    sm.tileStart[d] = count;  // scanned below
   }
   __syncthreads();
-  // Exclusive scan of the tile counts over digits (in place, first warp).
-  if (warp == 0) {
-    uint32_t run = 0;
-    for (int c = 0; c < kRadix / 32; ++c) {
-      uint32_t v = sm.tileStart[c * 32 + lane];
-      uint32_t x = v;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-        if (lane >= (unsigned)o) x += y;
-      }
-      sm.tileStart[c * 32 + lane] = run + x - v;
-      run += __shfl_sync(0xFFFFFFFFu, x, 31);
-    }
+  if (threadIdx.x < kRadix) {
+    uint32_t prefix = 0;
+    for (uint32_t w = 0; w < warp; ++w) prefix += sm.scanTot[w];
+    sm.tileStart[threadIdx.x] = prefix + incl - count;
   }
   __syncthreads();
   // Stage the tile in digit order.
