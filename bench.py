@@ -278,12 +278,15 @@ def run_ours(args, w, rank, world, local):
     mrays = rays / (mean["trace"] * 1e-3) / 1e6
     gpu_launches = int((c1 - c0) / args.steps)  # graph replays count the kernels they hold
 
-    # Build-phase algorithmic bytes per triangle (key bytes K, value bytes 4, P digit passes).
+    # Build-phase algorithmic bytes (key bytes K, value bytes V = 4, P 8-bit digit passes), as the
+    # scope's measurement section defines them for the reference's phases: scene reduce + Morton
+    # 2 (12 + 36) N + (K + V) N; sort K N + P 2 (K + V) N; topology K N + 48 (2N - 1); refit
+    # 2 * 48 (N - 1) + 48 (N - 1) + 48 N + 8 (N - 1). The fused build kernel moves less than the
+    # separate topology + refit passes counted here.
     K = 8 if w["bits"] == 63 else 4
     P = (w["bits"] + 7) // 8
-    alg = {"bounds": 48 * n, "morton": 48 * n + (K + 4) * n + 4 * n, "sort": K * n + P * 2 * (K + 4) * n,
-           "topology_refit": 4 * n + 48 * n + (K * n if w["topo"] == "karras" else 0) + NODE_BYTES * n_nodes
-           + 24 * (n - 1) + 8 * (n - 1)}
+    alg = {"bounds": 48 * n, "morton": 48 * n + (K + 4) * n, "sort": K * n + P * 2 * (K + 4) * n,
+           "topology_refit": K * n + NODE_BYTES * n_nodes + 2 * 48 * (n - 1) + 48 * (n - 1) + 48 * n + 8 * (n - 1)}
     peak, peak_kind = measured_peaks()
     build_bytes = sum(alg.values())
     build_gbs = build_bytes / (build_ms * 1e-3) / 1e9

@@ -4,7 +4,9 @@
 //   lbvh_bounds  : per-triangle box (+-FLT_EPSILON) reduced into the scene box, whose initial value
 //                  is the origin box (LBVH_CUDA.cu:60-119). Reads faces + vertices once.
 //   lbvh_morton  : re-reads the triangle, centroid -> 30- or 63-bit Morton key + index
-//                  (LBVH_CUDA.cu:132-183); also resets the build's exchange slots.
+//                  (LBVH_CUDA.cu:132-183); also resets the build's exchange slots and, when the
+//                  workspace has them, writes each triangle's box as a 32-byte record in face order
+//                  (the build then gathers one sector per leaf instead of a face and three vertices).
 //   sort         : sort.cu (replaces cub::DeviceRadixSort, LBVH_CUDA.cu:185-193).
 //   lbvh_build   : one thread per sorted leaf writes the leaf and climbs (Apetrei 2014 style): at each
 //                  step it picks the parent from the two neighbouring key deltas, meets its sibling
@@ -26,6 +28,7 @@ struct bvhgb_lbvh_workspace {
   uint32_t *vals = nullptr;
   uint32_t *valsSorted = nullptr;
   uint32_t *slots = nullptr;
+  float4 *triBoxes = nullptr;  // 2 x float4 per face (mn.xyz mx.x | mx.yz 0 0); null: gather the triangle
   bool slotsArmed = false;  // slots hold kNone (set by the Morton kernel)
   void *sortTemp = nullptr;
   size_t sortTempBytes = 0;
@@ -139,7 +142,8 @@ __global__ void __launch_bounds__(kMortonThreads) lbvh_morton_kernel(const float
                                                                      const uint32_t *__restrict__ faces, uint32_t n,
                                                                      const uint32_t *__restrict__ scene, void *keysOut,
                                                                      uint32_t *__restrict__ vals,
-                                                                     uint32_t *__restrict__ slots) {
+                                                                     uint32_t *__restrict__ slots,
+                                                                     float4 *__restrict__ boxes) {
   // Host part of LBVH_calcMortonCodes (LBVH_CUDA.cu:171-180), evaluated per block.
   float off[3], sc[3];
 #pragma unroll
@@ -165,6 +169,10 @@ __global__ void __launch_bounds__(kMortonThreads) lbvh_morton_kernel(const float
     }
     vals[i] = (uint32_t)i;
     if (i + 1 < n) slots[i] = kNone;
+    if (boxes) {
+      boxes[2 * i] = make_float4(b.mn[0], b.mn[1], b.mn[2], b.mx[0]);
+      boxes[2 * i + 1] = make_float4(b.mx[1], b.mx[2], 0.0f, 0.0f);
+    }
   }
 }
 
@@ -205,6 +213,7 @@ __global__ void __launch_bounds__(kBuildThreads) lbvh_build_kernel(const float *
                                                                    const uint32_t *__restrict__ faces,
                                                                    const K *__restrict__ keys,
                                                                    const uint32_t *__restrict__ idx, uint32_t n,
+                                                                   const float4 *__restrict__ boxes,
                                                                    bvhgb_node *nodes, uint32_t *slots,
                                                                    uint32_t *err) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -212,7 +221,13 @@ __global__ void __launch_bounds__(kBuildThreads) lbvh_build_kernel(const float *
   // Leaf (kGenLeafNodes, LBVH_CUDA.cu:273-292): left = face, right = 1, level = UINT8_MAX.
   const uint32_t face = __ldg(idx + i);
   Box box;
-  tri_box(vert, faces, face, box, nullptr);
+  if (boxes) {
+    const float4 a = __ldg(boxes + 2 * (size_t)face), c = __ldg(boxes + 2 * (size_t)face + 1);
+    box.mn[0] = a.x; box.mn[1] = a.y; box.mn[2] = a.z;
+    box.mx[0] = a.w; box.mx[1] = c.x; box.mx[2] = c.y;
+  } else {
+    tri_box(vert, faces, face, box, nullptr);
+  }
   const uint32_t leafIdx = n - 1 + i;
   if (n == 1) {
     store_record(nodes + leafIdx, box, 0u, face, 1u, 1u, 0u, 255u);
@@ -266,10 +281,12 @@ int launch_build(bvhgb_lbvh_workspace *ws, const float *vert, const uint32_t *fa
   dim3 grid(ceil_div(n, kBuildThreads));
   if (ws->keyBytes == 4)
     lbvh_build_kernel<MODE, uint32_t><<<grid, kBuildThreads, 0, s>>>(
-        vert, faces, static_cast<const uint32_t *>(ws->keysSorted), ws->valsSorted, n, nodes, ws->slots, ws->scene + 6);
+        vert, faces, static_cast<const uint32_t *>(ws->keysSorted), ws->valsSorted, n, ws->triBoxes, nodes, ws->slots,
+        ws->scene + 6);
   else
     lbvh_build_kernel<MODE, uint64_t><<<grid, kBuildThreads, 0, s>>>(
-        vert, faces, static_cast<const uint64_t *>(ws->keysSorted), ws->valsSorted, n, nodes, ws->slots, ws->scene + 6);
+        vert, faces, static_cast<const uint64_t *>(ws->keysSorted), ws->valsSorted, n, ws->triBoxes, nodes, ws->slots,
+        ws->scene + 6);
   BVHGB_LAUNCH_CHECK("lbvh build");
   return BVHGB_OK;
 }
@@ -306,6 +323,7 @@ extern "C" BVHGB_API int bvhgb_lbvh_create(uint32_t maxFaces, const bvhgb_lbvh_c
   if (e == cudaSuccess) e = cudaMalloc(&ws->vals, 4 * m);
   if (e == cudaSuccess) e = cudaMalloc(&ws->valsSorted, 4 * m);
   if (e == cudaSuccess) e = cudaMalloc(&ws->slots, 4 * m);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->triBoxes, 32 * m);
   if (e == cudaSuccess) e = cudaMalloc(&ws->sortTemp, ws->sortTempBytes ? ws->sortTempBytes : 256);
   if (e != cudaSuccess) {
     set_last_error("bvhgb_lbvh_create", e);
@@ -324,6 +342,7 @@ extern "C" BVHGB_API int bvhgb_lbvh_destroy(bvhgb_lbvh_workspace *ws) {
   cudaFree(ws->vals);
   cudaFree(ws->valsSorted);
   cudaFree(ws->slots);
+  cudaFree(ws->triBoxes);
   cudaFree(ws->sortTemp);
   delete ws;
   return BVHGB_OK;
@@ -353,9 +372,11 @@ extern "C" BVHGB_API int bvhgb_lbvh_calc_morton(bvhgb_lbvh_workspace *ws, const 
   cudaStream_t s = as_stream(stream);
   uint32_t grid = ceil_div(n, kMortonThreads * 2);
   if (ws->cfg.mortonBits == 30)
-    lbvh_morton_kernel<30><<<grid, kMortonThreads, 0, s>>>(vert, faces, n, ws->scene, ws->keys, ws->vals, ws->slots);
+    lbvh_morton_kernel<30><<<grid, kMortonThreads, 0, s>>>(vert, faces, n, ws->scene, ws->keys, ws->vals, ws->slots,
+                                                           ws->triBoxes);
   else
-    lbvh_morton_kernel<63><<<grid, kMortonThreads, 0, s>>>(vert, faces, n, ws->scene, ws->keys, ws->vals, ws->slots);
+    lbvh_morton_kernel<63><<<grid, kMortonThreads, 0, s>>>(vert, faces, n, ws->scene, ws->keys, ws->vals, ws->slots,
+                                                           ws->triBoxes);
   BVHGB_LAUNCH_CHECK("lbvh morton");
   ws->slotsArmed = true;
   return BVHGB_OK;
