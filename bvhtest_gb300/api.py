@@ -12,7 +12,8 @@ import numpy as np
 import torch
 
 from . import native
-from .native import (Aabb, BvhgbError, Bn13Config, Bn13Stats, Camera, HIT_DTYPE, LbvhConfig, NODE_DTYPE, PIXEL_DTYPE,
+from .native import (Aabb, BatchConfig, BatchTuneReport, BvhgbError, Bn13Config, Bn13Stats, Camera, HIT_DTYPE,
+                     LbvhConfig, NODE_DTYPE, PIXEL_DTYPE,
                      TraceConfig, check, load)
 
 REFCOMPAT, KARRAS = 0, 1
@@ -413,3 +414,98 @@ def hits_to_numpy(h: torch.Tensor) -> np.ndarray:
 
 def pixels_to_numpy(p: torch.Tensor) -> np.ndarray:
     return p.detach().cpu().numpy().view(PIXEL_DTYPE).reshape(-1)
+
+
+class Batch:
+    """Batched multi-mesh pipeline (bvhgb_batch_*): many meshes built, optimised and traced together.
+
+    vert / faces are the meshes' vertices and faces concatenated (face vertex indices into the
+    concatenated vertices); nodes holds every mesh's node array at its node offset."""
+
+    def __init__(self, face_counts, topology="refCompat", num_chunks=32, batch_percent=1.0, sort_tile=8192,
+                 refit_block=128, trace_block=128):
+        self.lib = load()
+        counts = np.ascontiguousarray(face_counts, dtype=np.uint32)
+        self.num_meshes = int(counts.shape[0])
+        cfg = BatchConfig(30, TOPOLOGY[topology], num_chunks, batch_percent, sort_tile, refit_block, trace_block)
+        h = C.c_void_p()
+        check(self.lib.bvhgb_batch_create(self.num_meshes, counts.ctypes.data_as(C.c_void_p), C.byref(cfg), C.byref(h)),
+              "bvhgb_batch_create")
+        self.ws = h
+        fo = np.zeros(self.num_meshes + 1, np.uint32)
+        no = np.zeros(self.num_meshes + 1, np.uint32)
+        check(self.lib.bvhgb_batch_offsets(self.ws, fo.ctypes.data_as(C.c_void_p), no.ctypes.data_as(C.c_void_p)),
+              "bvhgb_batch_offsets")
+        self.face_offsets, self.node_offsets = fo, no
+
+    def close(self):
+        if self.ws:
+            self.lib.bvhgb_batch_destroy(self.ws)
+            self.ws = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def total_nodes(self) -> int:
+        return int(self.node_offsets[-1])
+
+    def empty_nodes(self) -> torch.Tensor:
+        return empty_nodes(self.total_nodes)
+
+    @property
+    def config(self) -> dict:
+        c = BatchConfig()
+        check(self.lib.bvhgb_batch_get_config(self.ws, C.byref(c)), "bvhgb_batch_get_config")
+        return {k: getattr(c, k) for k, _ in BatchConfig._fields_}
+
+    def set_config(self, **kw):
+        c = BatchConfig()
+        check(self.lib.bvhgb_batch_get_config(self.ws, C.byref(c)), "bvhgb_batch_get_config")
+        for k, v in kw.items():
+            setattr(c, k, TOPOLOGY[v] if k == "topology" else v)
+        check(self.lib.bvhgb_batch_set_config(self.ws, C.byref(c)), "bvhgb_batch_set_config")
+
+    def build(self, vert, faces, nodes, stream=None):
+        check(self.lib.bvhgb_batch_build(self.ws, _ptr(vert), _ptr(faces), _ptr(nodes), _stream(stream)),
+              "bvhgb_batch_build")
+
+    def optimize(self, nodes, iterations, stream=None):
+        check(self.lib.bvhgb_batch_optimize(self.ws, _ptr(nodes), iterations, _stream(stream)), "bvhgb_batch_optimize")
+
+    def trace_random(self, nodes, vert, faces, rays_per_mesh, seed=1, with_rays=False, stream=None):
+        r = self.num_meshes * rays_per_mesh
+        hits = torch.empty(r, dtype=torch.int64, device="cuda")
+        org = torch.empty((r, 3), dtype=torch.float32, device="cuda") if with_rays else None
+        dirs = torch.empty((r, 3), dtype=torch.float32, device="cuda") if with_rays else None
+        check(self.lib.bvhgb_batch_trace_random(self.ws, _ptr(nodes), _ptr(vert), _ptr(faces), rays_per_mesh, seed,
+                                                _ptr(hits), _ptr(org), _ptr(dirs), _stream(stream)),
+              "bvhgb_batch_trace_random")
+        return (hits, org, dirs) if with_rays else hits
+
+    def run(self, vert, faces, nodes, iterations, rays_per_mesh, hits, seed=1, stream=None):
+        check(self.lib.bvhgb_batch_run(self.ws, _ptr(vert), _ptr(faces), _ptr(nodes), iterations, rays_per_mesh, seed,
+                                       _ptr(hits), _stream(stream)), "bvhgb_batch_run")
+
+    def stats(self, stream=None):
+        st = Bn13Stats()
+        err = C.c_uint32()
+        check(self.lib.bvhgb_batch_get_stats(self.ws, C.byref(st), C.byref(err), _stream(stream)),
+              "bvhgb_batch_get_stats")
+        return {k: getattr(st, k) for k, _ in Bn13Stats._fields_}, err.value
+
+    def autotune(self, vert, faces, nodes, rays_per_mesh, hits, seed=1, stream=None) -> dict:
+        rep = BatchTuneReport()
+        check(self.lib.bvhgb_batch_autotune(self.ws, _ptr(vert), _ptr(faces), _ptr(nodes), rays_per_mesh, seed,
+                                            _ptr(hits), C.byref(rep), _stream(stream)), "bvhgb_batch_autotune")
+        chosen = {k: getattr(rep.chosen, k) for k, _ in BatchConfig._fields_}
+        return {"sort_tile": dict(zip(list(rep.sortTileKeys), [round(v, 4) for v in rep.sortTileMs])),
+                "refit_block": dict(zip(list(rep.refitBlock), [round(v, 4) for v in rep.refitBlockMs])),
+                "trace_block": dict(zip(list(rep.traceBlock), [round(v, 4) for v in rep.traceBlockMs])),
+                "chosen": chosen}
+
+    def mesh_nodes(self, nodes: torch.Tensor, m: int) -> torch.Tensor:
+        return nodes[int(self.node_offsets[m]): int(self.node_offsets[m + 1])]

@@ -1,0 +1,642 @@
+// Device side of the parallel Bittner13 optimizer (lib/builder/Bittner13CUDA.cu,
+// lib/base/BVHPatch.hpp), shared by the single-tree kernels (bittner.cu) and the batched ones
+// (batch.cu): node views, the 10-slot patch, both reinsertion searches, removal / reinsertion,
+// and the per-item steps of a chunk.
+#pragma once
+
+#include "common.cuh"
+
+namespace bvhgb {
+namespace {
+
+constexpr int NSLOT = 10;
+enum : uint32_t {
+  P_GRAND_PARENT = 0, P_1ST_ROOT = 1, P_1ST_BEST = 2, P_NODE = 3, P_1ST_INSERT = 4,
+  P_2ND_ROOT = 5, P_2ND_BEST = 6, P_2ND_INSERT = 7, P_SIBLING = 8, P_PARENT = 9
+};
+enum StatIdx { S_ITEMS = 0, S_APPLIED = 1, S_CONFLICT = 2, S_INVALID = 3, S_OVERFLOW = 4, S_VISITS = 5, S_COUNT = 6 };
+
+struct SearchCounters {
+  uint32_t overflow;  // queue pushes dropped at capacity
+  uint32_t visits;    // nodes evaluated by the branch and bound
+};
+
+struct NodeP {
+  uint32_t parent, left, right;
+  uint16_t isLeafFlag, isLeft;
+};
+
+struct HeapItem {
+  uint32_t node;
+  float cost;
+};
+
+struct PatchOut {  // what the apply kernel needs
+  NodeP nd[NSLOT];
+  uint32_t idx[NSLOT];
+};
+
+// Read-only view of the tree during the patch kernel (nothing writes the tree in that launch).
+__device__ __forceinline__ NodeP tree_node(const bvhgb_node *t, uint32_t x) {
+  const float4 *p = reinterpret_cast<const float4 *>(t + x);
+  const float4 b = __ldg(p + 1), c = __ldg(p + 2);
+  NodeP r;
+  r.parent = __float_as_uint(b.z);
+  r.left = __float_as_uint(b.w);
+  r.right = __float_as_uint(c.x);
+  const uint32_t fl = __float_as_uint(c.y);
+  r.isLeafFlag = (uint16_t)(fl & 0xFFFFu);
+  r.isLeft = (uint16_t)(fl >> 16);
+  return r;
+}
+__device__ __forceinline__ Box tree_box(const bvhgb_node *t, uint32_t x) {
+  const float4 *p = reinterpret_cast<const float4 *>(t + x);
+  const float4 a = __ldg(p), b = __ldg(p + 1);
+  Box r;
+  r.mn[0] = a.x; r.mn[1] = a.y; r.mn[2] = a.z;
+  r.mx[0] = a.w; r.mx[1] = b.x; r.mx[2] = b.y;
+  return r;
+}
+__device__ __forceinline__ float tree_sa(const bvhgb_node *t, uint32_t x) { return __ldg(&t[x].surfaceArea); }
+__device__ __forceinline__ bool tree_leaf(const bvhgb_node *t, uint32_t x) { return __ldg(&t[x].isLeafFlag) != 0; }
+
+// BVHPatch (BVHPatch.hpp:87-335), ENABLE_AABB_PATH = 0.
+struct Patch {
+  NodeP nd[NSLOT];
+  uint32_t idx[NSLOT];
+  uint32_t apath[4];
+  Box abox[4];
+  const bvhgb_node *t;
+  uint32_t root;
+  uint32_t numNodes;
+  mutable bool bad;  // an index outside the node array was met (corrupted input); item is dropped
+
+  __device__ uint32_t chk(uint32_t x) const {
+    if (x < numNodes) return x;
+    bad = true;
+    return root;
+  }
+
+  __device__ void clear() {
+#pragma unroll
+    for (int i = 0; i < NSLOT; ++i) idx[i] = kNone;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) apath[i] = kNone;
+  }
+  __device__ uint32_t index_subset(uint32_t x) const {
+    if (idx[0] == x) return 0;
+    if (idx[1] == kNone) return kNone;
+    if (idx[1] == x) return 1;
+    if (idx[2] == x) return 2;
+    if (idx[3] == x) return 3;
+    return kNone;
+  }
+  __device__ uint32_t index(uint32_t x) const {
+    for (uint32_t i = 0; i < NSLOT; ++i)
+      if (idx[i] == x) return i;
+    return kNone;
+  }
+  __device__ NodeP get(uint32_t x) const {
+    uint32_t i = index(x);
+    return i == kNone ? tree_node(t, chk(x)) : nd[i];
+  }
+  __device__ NodeP get_subset(uint32_t x) const {
+    uint32_t i = index_subset(x);
+    return i == kNone ? tree_node(t, chk(x)) : nd[i];
+  }
+  __device__ uint32_t patch_node(uint32_t x, uint32_t slot) {
+    idx[slot] = x;
+    nd[slot] = tree_node(t, chk(x));
+    return slot;
+  }
+  __device__ uint32_t move(uint32_t from, uint32_t to) {
+    idx[to] = idx[from];
+    idx[from] = kNone;
+    nd[to] = nd[from];
+    return to;
+  }
+  __device__ uint32_t sibling(const NodeP &n) const {
+    NodeP p = get(n.parent);
+    return n.isLeft == 0 ? p.left : p.right;
+  }
+  __device__ Box get_aabb(uint32_t x) const {
+    for (int i = 0; i < 4; ++i)
+      if (apath[i] == x) return abox[i];
+    return tree_box(t, chk(x));
+  }
+  // patchAABBFrom (BVHPatch.hpp:293-316)
+  __device__ void patch_aabb_from(uint32_t x, uint32_t pidx) {
+    uint32_t ni = x;
+    NodeP n = get_subset(ni);
+    Box b = get_aabb(n.left);
+    bool lastLeft = true;
+    for (uint32_t i = 0; i < 2; ++i) {
+      uint32_t sib = lastLeft ? n.right : n.left;
+      Box sb = get_aabb(sib);
+      merge_into(b, sb);
+      abox[pidx * 2 + i] = b;
+      apath[pidx * 2 + i] = ni;
+      lastLeft = n.isLeft != 0;
+      if (ni == root) break;
+      ni = n.parent;
+      n = get_subset(ni);
+    }
+  }
+};
+
+// Heap with the hole-based sift of the standard library heap algorithms (CUDAHeap.hpp:33-112);
+// "less(a, b)" is a.cost > b.cost, so h[0] holds the smallest induced cost.
+__device__ __forceinline__ bool hless(const HeapItem &a, const HeapItem &b) { return a.cost > b.cost; }
+
+// Two-level storage: the first kHeapShared entries of each search live in shared memory,
+// interleaved across the warp's lanes (entry i of lane l at i * 32 + l, conflict-free when lanes
+// touch the same depth); deeper entries spill to the item's global region. The index space and
+// the capacity are unchanged, so the pop order is exactly that of a flat array.
+constexpr int kSearchThreads = 32;
+constexpr int kHeapShared = 128;
+
+struct Heap {
+  HeapItem *sm;  // this lane's entry 0 in shared memory (stride kSearchThreads)
+  HeapItem *gm;  // this item's global region (cap entries)
+  __device__ __forceinline__ HeapItem &at(long i) const { return i < kHeapShared ? sm[i * kSearchThreads] : gm[i]; }
+};
+
+__device__ __forceinline__ void sift_up(const Heap &h, long hole, long top, HeapItem v) {
+  long parent = (hole - 1) / 2;
+  while (hole > top && hless(h.at(parent), v)) {
+    h.at(hole) = h.at(parent);
+    hole = parent;
+    parent = (hole - 1) / 2;
+  }
+  h.at(hole) = v;
+}
+__device__ __forceinline__ void heap_push(const Heap &h, long lenAfter) { sift_up(h, lenAfter - 1, 0, h.at(lenAfter - 1)); }
+__device__ __forceinline__ void heap_pop(const Heap &h, long len) {
+  if (len <= 1) return;
+  const long last = len - 1;
+  const HeapItem v = h.at(last);
+  h.at(last) = h.at(0);
+  const long n = last;
+  long hole = 0, second = 0;
+  while (second < (n - 1) / 2) {
+    second = 2 * (second + 1);
+    if (hless(h.at(second), h.at(second - 1))) second--;
+    h.at(hole) = h.at(second);
+    hole = second;
+  }
+  if ((n & 1) == 0 && second == (n - 2) / 2) {
+    second = 2 * (second + 1);
+    h.at(hole) = h.at(second - 1);
+    hole = second - 1;
+  }
+  sift_up(h, hole, 0, v);
+}
+
+// Starts fetching a node's 48-byte record into L2 while the search keeps working.
+__device__ __forceinline__ void prefetch_node(const bvhgb_node *t, uint32_t x) {
+  const char *p = reinterpret_cast<const char *>(t + x);
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p + 32));
+}
+
+// findNode1 (Bittner13CUDA.cu:141-191).
+__device__ uint32_t find_node(const Patch &p, uint32_t n, const Heap &pq, uint32_t cap, SearchCounters &ctr) {
+  float best_cost = __int_as_float(0x7f800000);
+  uint32_t best = 0;
+  const Box nbox = tree_box(p.t, p.chk(n));
+  const float sarea = tree_sa(p.t, p.chk(n));
+  long size = 1;
+  pq.at(0).node = p.root;
+  pq.at(0).cost = 0.0f;
+  // A tree pops each node at most once; the bound only matters for corrupted input.
+  for (uint32_t it = 0; size > 0; ++it) {
+    if (it > p.numNodes) {
+      p.bad = true;
+      break;
+    }
+    const HeapItem cur = pq.at(0);
+    if (fadd(cur.cost, sarea) >= best_cost) break;
+    heap_pop(pq, size);
+    size--;
+    ctr.visits++;
+    const NodeP cn = p.get_subset(cur.node);
+    Box b = p.get_aabb(cur.node);
+    float induced = fmul(-1.0f, surface_area(b));
+    merge_into(b, nbox);
+    const float direct = surface_area(b);
+    const float total = fadd(cur.cost, direct);
+    if (total < best_cost) {
+      best_cost = total;
+      best = cur.node;
+    }
+    induced = fadd(induced, total);
+    if (fadd(induced, sarea) < best_cost && !cn.isLeafFlag) {
+      if ((uint32_t)size + 2 <= cap) {
+        if (cn.left < p.numNodes) prefetch_node(p.t, cn.left);
+        if (cn.right < p.numNodes) prefetch_node(p.t, cn.right);
+        pq.at(size).node = cn.left;
+        pq.at(size).cost = induced;
+        pq.at(size + 1).node = cn.right;
+        pq.at(size + 1).cost = induced;
+        heap_push(pq, size + 1);
+        heap_push(pq, size + 2);
+        size += 2;
+      } else {
+        ctr.overflow++;
+      }
+    }
+  }
+  return best;
+}
+
+// removeNode (Bittner13CUDA.cu:267-305).
+__device__ bool remove_node(Patch &p, uint32_t x, uint32_t ins[2], uint32_t un[2], uint32_t &g_out) {
+  if (tree_leaf(p.t, p.chk(x)) || x == p.root) return false;
+  const uint32_t sn = p.patch_node(x, P_NODE);
+  const uint32_t s = p.sibling(p.nd[sn]);
+  const uint32_t pi = p.nd[sn].parent;
+  if (pi == p.root) return false;
+  const uint32_t ss = p.patch_node(s, P_SIBLING);
+  const uint32_t sp = p.patch_node(pi, P_PARENT);
+  const uint32_t gi = p.nd[sp].parent;
+  const uint32_t sg = p.patch_node(gi, P_GRAND_PARENT);
+  if (p.nd[sp].isLeft) {
+    p.nd[sg].left = s;
+    p.nd[ss].isLeft = 1;
+  } else {
+    p.nd[sg].right = s;
+    p.nd[ss].isLeft = 0;
+  }
+  p.nd[ss].parent = gi;
+  p.patch_aabb_from(gi, 0);
+  const uint32_t l = p.nd[sn].left, r = p.nd[sn].right;
+  if (tree_sa(p.t, p.chk(l)) > tree_sa(p.t, p.chk(r))) { ins[0] = l; ins[1] = r; }
+  else { ins[0] = r; ins[1] = l; }
+  un[0] = x;
+  un[1] = pi;
+  g_out = gi;
+  return true;
+}
+
+// ---- batched best-first search: one warp per item -------------------------------------------
+//
+// The frontier (up to 128 entries) lives in registers, 4 slots per lane, entry e = slot * 32 + lane,
+// kept sorted by (cost, node). Each round the warp evaluates slot 0 (the 32 lowest-bound entries)
+// in parallel, reduces the best total, sorts the up-to-64 children with a bitonic network and
+// merges them into slots 1..3 with a bitonic merge; entries past 128 are dropped and counted.
+// oracle/bittner.c (gpu_find_node_batched) restates the same rounds.
+constexpr uint32_t kFull = 0xFFFFFFFFu;
+constexpr int kFrontier = 4;  // slots per lane (128 entries)
+
+__device__ __forceinline__ bool fe_gt(float ca, uint32_t na, float cb, uint32_t nb) {
+  return ca > cb || (ca == cb && na > nb);
+}
+
+// One compare-exchange stage of a bitonic network over S slots x 32 lanes.
+template <int S>
+__device__ __forceinline__ void bitonic_stage(float (&c)[S], uint32_t (&n)[S], int j, int k, bool descending,
+                                              uint32_t lane) {
+  if (j >= 32) {
+    const int d = j >> 5;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      if (s & d) continue;
+      const int t = s + d;
+      const uint32_t e = (uint32_t)s * 32u + lane;
+      const bool asc = ((e & (uint32_t)k) == 0) != descending;
+      const bool swap = asc ? fe_gt(c[s], n[s], c[t], n[t]) : fe_gt(c[t], n[t], c[s], n[s]);
+      if (swap) {
+        const float tc = c[s]; c[s] = c[t]; c[t] = tc;
+        const uint32_t tn = n[s]; n[s] = n[t]; n[t] = tn;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      const float oc = __shfl_xor_sync(kFull, c[s], j);
+      const uint32_t on = __shfl_xor_sync(kFull, n[s], j);
+      const uint32_t e = (uint32_t)s * 32u + lane;
+      const bool asc = ((e & (uint32_t)k) == 0) != descending;
+      const bool keepMin = ((lane & (uint32_t)j) == 0) == asc;
+      if (keepMin ? fe_gt(c[s], n[s], oc, on) : fe_gt(oc, on, c[s], n[s])) {
+        c[s] = oc;
+        n[s] = on;
+      }
+    }
+  }
+}
+
+template <int S>
+__device__ __forceinline__ void bitonic_sort(float (&c)[S], uint32_t (&n)[S], bool descending, uint32_t lane) {
+#pragma unroll
+  for (int k = 2; k <= S * 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) bitonic_stage<S>(c, n, j, k, descending, lane);
+  }
+}
+
+template <int S>
+__device__ __forceinline__ void bitonic_merge(float (&c)[S], uint32_t (&n)[S], uint32_t lane) {
+#pragma unroll
+  for (int j = S * 16; j > 0; j >>= 1) bitonic_stage<S>(c, n, j, S * 32, false, lane);
+}
+
+// findNode1's cost model in batched rounds (every lane of the warp calls it with the same patch).
+__device__ uint32_t find_node_batched(const Patch &p, uint32_t n, SearchCounters &ctr) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const float kInf = __int_as_float(0x7f800000);
+  float best_cost = kInf;
+  uint32_t best = 0;
+  const Box nbox = tree_box(p.t, p.chk(n));
+  const float sarea = tree_sa(p.t, p.chk(n));
+  float fc[kFrontier];
+  uint32_t fn[kFrontier];
+#pragma unroll
+  for (int s = 0; s < kFrontier; ++s) {
+    fc[s] = kInf;
+    fn[s] = kNone;
+  }
+  if (lane == 0) {
+    fc[0] = 0.0f;
+    fn[0] = p.root;
+  }
+  uint32_t fsize = 1;  // finite frontier entries (warp-uniform)
+  for (uint32_t round = 0;; ++round) {
+    if (round > p.numNodes) {  // bounded: every round evaluates at least one node
+      p.bad = true;
+      break;
+    }
+    const bool cand = fc[0] != kInf && fadd(fc[0], sarea) < best_cost;
+    const uint32_t vmask = __ballot_sync(kFull, cand);
+    if (vmask == 0) break;
+    ctr.visits += __popc(vmask);
+    NodeP cn;
+    float total = kInf, induced = kInf;
+    if (cand) {
+      cn = p.get_subset(fn[0]);
+      Box b = p.get_aabb(fn[0]);
+      induced = fmul(-1.0f, surface_area(b));
+      merge_into(b, nbox);
+      total = fadd(fc[0], surface_area(b));
+      induced = fadd(induced, total);
+    }
+    // Best of the round: smallest total, first in frontier order on ties.
+    const uint32_t key = cand ? f2ord(total) : 0xFFFFFFFFu;
+    const uint32_t kmin = __reduce_min_sync(kFull, key);
+    const uint32_t first = __ffs(__ballot_sync(kFull, cand && key == kmin)) - 1;
+    const float rbest = __shfl_sync(kFull, total, first);
+    const uint32_t rnode = __shfl_sync(kFull, fn[0], first);
+    if (rbest < best_cost) {
+      best_cost = rbest;
+      best = rnode;
+    }
+    const bool kids = cand && !cn.isLeafFlag && fadd(induced, sarea) < best_cost;
+    if (kids) {
+      if (cn.left < p.numNodes) prefetch_node(p.t, cn.left);
+      if (cn.right < p.numNodes) prefetch_node(p.t, cn.right);
+    }
+    const uint32_t kmask = __ballot_sync(kFull, kids);
+    const uint32_t m = 2u * __popc(kmask);                 // children this round
+    const uint32_t rest = fsize - min(fsize, 32u);        // frontier entries left in slots 1..3
+    if (m == 0) {
+      // Nothing to insert: the remaining frontier is already in order, shift it down a slot.
+#pragma unroll
+      for (int s = 0; s + 1 < kFrontier; ++s) {
+        fc[s] = fc[s + 1];
+        fn[s] = fn[s + 1];
+      }
+      fc[kFrontier - 1] = kInf;
+      fn[kFrontier - 1] = kNone;
+      fsize = rest;
+    } else if (m <= 32) {
+      // Common case: gather the children into one slot (lane j takes child j), sort it
+      // descending and merge it with the remaining frontier; at most 128 entries, no overflow.
+      const uint32_t src = lane < m ? __fns(kmask, 0, (lane >> 1) + 1) : lane;
+      const float sc = __shfl_sync(kFull, induced, src);
+      const uint32_t sl = __shfl_sync(kFull, cn.left, src), sr = __shfl_sync(kFull, cn.right, src);
+      float c1[1] = {lane < m ? sc : kInf};
+      uint32_t n1[1] = {lane < m ? ((lane & 1) ? sr : sl) : kNone};
+      bitonic_sort<1>(c1, n1, true, lane);
+      if (rest <= 32) {
+        float mc[2] = {fc[1], c1[0]};
+        uint32_t mn[2] = {fn[1], n1[0]};
+        bitonic_merge<2>(mc, mn, lane);
+        fc[0] = mc[0]; fn[0] = mn[0];
+        fc[1] = mc[1]; fn[1] = mn[1];
+        fc[2] = fc[3] = kInf;
+        fn[2] = fn[3] = kNone;
+      } else {
+        float mc[4] = {fc[1], fc[2], fc[3], c1[0]};
+        uint32_t mn[4] = {fn[1], fn[2], fn[3], n1[0]};
+        bitonic_merge<4>(mc, mn, lane);
+#pragma unroll
+        for (int s = 0; s < kFrontier; ++s) {
+          fc[s] = mc[s];
+          fn[s] = mn[s];
+        }
+      }
+      fsize = rest + m;
+    } else {
+      // Wide round: sort all children (two slots) and merge into 256, keeping the lowest 128.
+      float cc[2] = {kids ? induced : kInf, kids ? induced : kInf};
+      uint32_t cnn[2] = {kids ? cn.left : kNone, kids ? cn.right : kNone};
+      bitonic_sort<2>(cc, cnn, true, lane);
+      float mc[8] = {fc[1], fc[2], fc[3], kInf, kInf, kInf, cc[0], cc[1]};
+      uint32_t mn[8] = {fn[1], fn[2], fn[3], kNone, kNone, kNone, cnn[0], cnn[1]};
+      bitonic_merge<8>(mc, mn, lane);
+#pragma unroll
+      for (int s = 0; s < kFrontier; ++s) {
+        fc[s] = mc[s];
+        fn[s] = mn[s];
+      }
+      const uint32_t total = rest + m;
+      ctr.overflow += total > 128u ? total - 128u : 0u;
+      fsize = min(total, 128u);
+    }
+  }
+  p.bad = __any_sync(kFull, p.bad);
+  return best;
+}
+
+// reinsert (Bittner13CUDA.cu:308-358).
+template <bool BATCHED>
+__device__ bool reinsert(Patch &p, uint32_t x, uint32_t unused, bool update, const Heap &pq, uint32_t cap,
+                         SearchCounters &ctr) {
+  const uint32_t best = BATCHED ? find_node_batched(p, x, ctr) : find_node(p, x, pq, cap, ctr);
+  if (best == p.root) return false;
+  const uint32_t bpi = p.index(best);
+  uint32_t sb;
+  if (bpi == kNone) sb = p.patch_node(best, update ? P_1ST_BEST : P_2ND_BEST);
+  else if (bpi == P_GRAND_PARENT) sb = P_GRAND_PARENT;
+  else sb = p.move(bpi, update ? P_1ST_BEST : P_2ND_BEST);
+  const uint32_t sx = p.patch_node(x, update ? P_1ST_INSERT : P_2ND_INSERT);
+  const uint32_t su = update ? P_NODE : P_PARENT;
+  const uint32_t ri = p.nd[sb].parent;
+  const uint32_t rpi = p.index(ri);
+  const uint32_t sr = rpi == kNone ? p.patch_node(ri, update ? P_1ST_ROOT : P_2ND_ROOT)
+                                   : p.move(rpi, update ? P_1ST_ROOT : P_2ND_ROOT);
+  if (p.nd[sb].isLeft) {
+    p.nd[sr].left = unused;
+    p.nd[su].isLeft = 1;
+  } else {
+    p.nd[sr].right = unused;
+    p.nd[su].isLeft = 0;
+  }
+  p.nd[su].parent = ri;
+  p.nd[su].left = best;
+  p.nd[su].right = x;
+  p.nd[sb].parent = unused;
+  p.nd[sb].isLeft = 1;
+  p.nd[sx].parent = unused;
+  p.nd[sx].isLeft = 0;
+  if (update) p.patch_aabb_from(unused, 1);
+  return true;
+}
+
+
+// ---- per-item steps shared by the single-tree and the batched kernels ---------------------------
+// (t, root, numNodes) describe one tree; owner / counter point at that tree's entries; rank is the
+// item's position in its tree's chunk (lower rank wins a conflict).
+
+constexpr int kWarpItemsPerBlock = 4;
+
+// kRemoveAndReinsert for one item on a whole warp (batched search); lane 0 publishes.
+__device__ __forceinline__ void warp_patch_item(const bvhgb_node *__restrict__ t, uint32_t root, uint32_t numNodes,
+                                                uint32_t node, bool ok, uint32_t rank, PatchOut *__restrict__ out,
+                                                uint32_t *__restrict__ valid, uint32_t *__restrict__ toFix3,
+                                                uint32_t *__restrict__ owner, unsigned long long *__restrict__ stats,
+                                                uint32_t *__restrict__ err) {
+  const uint32_t lane = threadIdx.x & 31u;
+  Patch p;
+  p.t = t;
+  p.root = root;
+  p.numNodes = numNodes;
+  p.bad = false;
+  p.clear();
+  SearchCounters ctr = {0u, 0u};
+  uint32_t ins[2], un[2], g = kNone;
+  const Heap unused{nullptr, nullptr};
+  ok = ok && remove_node(p, node, ins, un, g);
+  ok = ok && reinsert<true>(p, ins[0], un[0], true, unused, 0, ctr);
+  ok = ok && reinsert<true>(p, ins[1], un[1], false, unused, 0, ctr);
+  if (p.bad) ok = false;
+  if (lane != 0) return;
+  if (p.bad) atomicOr(err, kErrBadIndex);
+  *valid = ok ? 1u : 0u;
+  toFix3[0] = ok ? g : kNone;
+  toFix3[1] = ok ? un[0] : kNone;
+  toFix3[2] = ok ? un[1] : kNone;
+#pragma unroll
+  for (int s = 0; s < NSLOT; ++s) {
+    out->nd[s] = p.nd[s];
+    out->idx[s] = ok ? p.idx[s] : kNone;
+    if (ok && p.idx[s] != kNone) atomicMin(&owner[p.idx[s]], rank);
+  }
+  if (!ok) atomicAdd(&stats[S_INVALID], 1ull);
+  if (ctr.overflow) atomicAdd(&stats[S_OVERFLOW], (unsigned long long)ctr.overflow);
+  atomicAdd(&stats[S_VISITS], (unsigned long long)ctr.visits);
+  atomicAdd(&stats[S_ITEMS], 1ull);
+}
+
+// kCheckConflicts + kApplyPatches for one item.
+__device__ __forceinline__ void apply_item(bvhgb_node *t, const PatchOut &in, uint32_t *__restrict__ valid,
+                                           uint32_t *__restrict__ toFix3, const uint32_t *__restrict__ owner,
+                                           uint32_t rank, unsigned long long *__restrict__ stats) {
+  if (!*valid) return;
+  bool win = true;
+#pragma unroll
+  for (int s = 0; s < NSLOT; ++s) {
+    const uint32_t x = in.idx[s];
+    if (x != kNone && owner[x] != rank) win = false;
+  }
+  if (!win) {
+    *valid = 0;
+    toFix3[0] = toFix3[1] = toFix3[2] = kNone;
+    atomicAdd(&stats[S_CONFLICT], 1ull);
+    return;
+  }
+#pragma unroll
+  for (int s = 0; s < NSLOT; ++s) {
+    const uint32_t x = in.idx[s];
+    if (x == kNone) continue;
+    const NodeP n = in.nd[s];
+    t[x].parent = n.parent;
+    t[x].left = n.left;
+    t[x].right = n.right;
+    t[x].isLeft = n.isLeft;
+  }
+  atomicAdd(&stats[S_APPLIED], 1ull);
+}
+
+// Release a third of an item's claims and count the arrivals along one dirty path (kFixTree3_1);
+// the parent link is loaded together with the counter update, so a level costs one round trip.
+__device__ __forceinline__ void count_path(const bvhgb_node *__restrict__ t, uint32_t root, uint32_t numNodes,
+                                          const PatchOut &in, uint32_t j, uint32_t x, uint32_t *__restrict__ owner,
+                                          uint32_t *__restrict__ counter, uint32_t *__restrict__ err) {
+  for (uint32_t s = j; s < (uint32_t)NSLOT; s += 3) {
+    const uint32_t y = in.idx[s];
+    if (y != kNone) owner[y] = kNone;
+  }
+  if (x == kNone) return;
+  for (uint32_t steps = 0;; ++steps) {
+    if (x >= numNodes || steps > numNodes) {
+      atomicOr(err, kErrBadIndex);
+      break;
+    }
+    const uint32_t px = t[x].parent;  // issued before the update; the links are final here
+    if (atomicAdd(&counter[x], 1u) != 0u) break;
+    if (x == root) break;
+    x = px;
+  }
+}
+
+// The last path to arrive at a node recomputes its box (kFixTree3_2). A node's links do not change
+// in this launch, so they are read before its counter; after the acq_rel update only the other
+// child's box is loaded (the box of the child the path came from is still in registers).
+__device__ __forceinline__ void refit_path(bvhgb_node *t, uint32_t root, uint32_t numNodes, uint32_t x,
+                                          uint32_t *__restrict__ counter, uint32_t *__restrict__ err) {
+  if (x == kNone) return;
+  uint32_t from = kNone;  // child the path came from, whose box is 'cur'
+  Box cur;
+  for (uint32_t steps = 0;; ++steps) {
+    if (x >= numNodes || steps > numNodes) {
+      atomicOr(err, kErrBadIndex);
+      return;
+    }
+    const float4 w1 = __ldcg(reinterpret_cast<const float4 *>(t + x) + 1);  // mx.y mx.z parent left
+    const float4 w2 = __ldcg(reinterpret_cast<const float4 *>(t + x) + 2);  // right flags level sa
+    if (atom_add_acq_rel(&counter[x], 0xFFFFFFFFu) != 1u) return;  // not the last arrival
+    const uint32_t parent = __float_as_uint(w1.z), l = __float_as_uint(w1.w), r = __float_as_uint(w2.x);
+    if ((__float_as_uint(w2.y) & 0xFFFFu) || l >= numNodes || r >= numNodes) {
+      if (!(__float_as_uint(w2.y) & 0xFFFFu)) atomicOr(err, kErrBadIndex);
+      return;
+    }
+    Box b = from == l ? cur : load_box_cg(t + l);
+    const Box rb = from == r ? cur : load_box_cg(t + r);
+    merge_into(b, rb);
+    float4 *p = reinterpret_cast<float4 *>(t + x);
+    p[0] = make_float4(b.mn[0], b.mn[1], b.mn[2], b.mx[0]);
+    p[1] = make_float4(b.mx[1], b.mx[2], w1.z, w1.w);
+    t[x].surfaceArea = surface_area(b);
+    if (x == root) return;
+    from = x;
+    cur = b;
+    x = parent;
+  }
+}
+
+// kCalcCost for one inner node (0 for a leaf).
+__device__ __forceinline__ float inefficiency(const bvhgb_node *__restrict__ t, uint32_t x) {
+  const float4 *p = reinterpret_cast<const float4 *>(t + x);
+  const float4 b = __ldg(p + 1), c = __ldg(p + 2);
+  if ((__float_as_uint(c.y) & 0xFFFFu) != 0) return 0.0f;
+  const float sa = c.w;
+  const float l = __ldg(&t[__float_as_uint(b.w)].surfaceArea);
+  const float r = __ldg(&t[__float_as_uint(c.x)].surfaceArea);
+  const float num = fmul(fmul(fmul(sa, sa), sa), 2.0f);
+  const float den = fmul(fadd(l, r), l < r ? l : r);
+  return fdiv(num, den);
+}
+
+}  // namespace
+}  // namespace bvhgb

@@ -19,10 +19,8 @@ namespace bvhgb {
 
 namespace {
 
-constexpr int kThreads = 512;
-constexpr int kItems = 16;
-constexpr int kTile = kThreads * kItems;  // 8192 keys per CTA
-constexpr int kWarps = kThreads / 32;
+constexpr int kThreads = 512;  // histogram blocks; the onesweep tile shape is a template parameter
+constexpr int kMinTile = 2048;  // smallest tile: the status arrays are sized for it
 constexpr int kRadix = 256;
 constexpr int kBins = kRadix + 1;  // + a bin for padding keys of the last tile
 constexpr uint32_t kFlagAgg = 1u << 30;
@@ -43,10 +41,10 @@ struct Layout {
   uint32_t passes, tiles;
 };
 
-Layout make_layout(uint32_t n, uint32_t keyBytes, uint32_t beginBit, uint32_t endBit) {
+Layout make_layout(uint32_t n, uint32_t keyBytes, uint32_t beginBit, uint32_t endBit, uint32_t tile = kMinTile) {
   Layout L{};
   L.passes = (endBit > beginBit) ? (endBit - beginBit + 7) / 8 : 0;
-  L.tiles = n ? (uint32_t)((n + kTile - 1) / kTile) : 0;
+  L.tiles = n ? (uint32_t)((n + tile - 1) / tile) : 0;
   size_t off = 0;
   L.hist = off;     off = align256(off + sizeof(uint32_t) * kRadix * (L.passes ? L.passes : 1));
   L.counters = off; off = align256(off + sizeof(uint32_t) * (L.passes ? L.passes : 1));
@@ -94,8 +92,10 @@ __global__ void __launch_bounds__(kRadix) scan_kernel(uint32_t *hist) {
   h[threadIdx.x] = s[threadIdx.x] - v;
 }
 
-template <typename K>
+template <typename K, int THREADS, int ITEMS>
 struct OnesweepSmem {
+  static constexpr int kWarps = THREADS / 32;
+  static constexpr int kTile = THREADS * ITEMS;
   uint32_t warpHist[kWarps][kBins];
   uint32_t tileStart[kRadix];
   uint32_t globalBase[kRadix];
@@ -104,17 +104,19 @@ struct OnesweepSmem {
   K keys[kTile];
   uint32_t vals[kTile];
 };
-static_assert(kThreads >= kRadix, "one thread per digit in the look-back");
 
-template <typename K>
-__global__ void __launch_bounds__(kThreads, 1) onesweep_kernel(const K *__restrict__ keysIn, K *__restrict__ keysOut,
+template <typename K, int THREADS, int ITEMS>
+__global__ void __launch_bounds__(THREADS, 1) onesweep_kernel(const K *__restrict__ keysIn, K *__restrict__ keysOut,
                                                             const uint32_t *__restrict__ valsIn,
                                                             uint32_t *__restrict__ valsOut, uint32_t n,
                                                             uint32_t shift, uint32_t mask,
                                                             const uint32_t *__restrict__ offsets,
                                                             uint32_t *tileCounter, uint32_t *status, uint32_t *err) {
+  using Smem = OnesweepSmem<K, THREADS, ITEMS>;
+  constexpr int kWarps = Smem::kWarps, kTile = Smem::kTile, kItems = ITEMS, kThreads = THREADS;
+  static_assert(THREADS >= kRadix, "one thread per digit in the look-back");
   extern __shared__ __align__(16) unsigned char smraw[];
-  OnesweepSmem<K> &sm = *reinterpret_cast<OnesweepSmem<K> *>(smraw);
+  Smem &sm = *reinterpret_cast<Smem *>(smraw);
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
 
   if (threadIdx.x == 0) sm.tileIdx = atomicAdd(tileCounter, 1u);
@@ -251,47 +253,74 @@ __global__ void __launch_bounds__(kThreads, 1) onesweep_kernel(const K *__restri
   }
 }
 
+template <typename K, int THREADS, int ITEMS>
+int onesweep_passes(const Layout &L, const K *keysIn, K *keysOut, const uint32_t *valsIn, uint32_t *valsOut, K *altK,
+                    uint32_t *altV, uint32_t *hist, uint32_t *counters, uint32_t *status, uint32_t *err, uint32_t n,
+                    uint32_t beginBit, uint32_t endBit, cudaStream_t s) {
+  const size_t smem = sizeof(OnesweepSmem<K, THREADS, ITEMS>);
+  // Ping-pong so that the last pass lands in keysOut/valsOut.
+  const K *srcK = keysIn;
+  const uint32_t *srcV = valsIn;
+  for (uint32_t p = 0; p < L.passes; ++p) {
+    const bool toOut = ((L.passes - 1 - p) % 2) == 0;
+    K *dstK = toOut ? keysOut : altK;
+    uint32_t *dstV = toOut ? valsOut : altV;
+    const uint32_t shift = beginBit + 8 * p;
+    onesweep_kernel<K, THREADS, ITEMS><<<L.tiles, THREADS, smem, s>>>(
+        srcK, dstK, srcV, dstV, n, shift, digit_mask(shift, endBit), hist + p * kRadix, counters + p,
+        status + (size_t)p * L.tiles * kRadix, err);
+    BVHGB_LAUNCH_CHECK("radix onesweep");
+    srcK = dstK;
+    srcV = dstV;
+  }
+  return BVHGB_OK;
+}
+
 template <typename K>
-int sort_impl(void *temp, const Layout &L, const K *keysIn, K *keysOut, const uint32_t *valsIn, uint32_t *valsOut,
+int sort_impl(void *temp, uint32_t tileKeys, const K *keysIn, K *keysOut, const uint32_t *valsIn, uint32_t *valsOut,
               uint32_t n, uint32_t beginBit, uint32_t endBit, cudaStream_t s) {
+  const Layout L = make_layout(n, sizeof(K), beginBit, endBit, tileKeys);
+  const Layout Lmax = make_layout(n, sizeof(K), beginBit, endBit, kMinTile);  // the temp space's layout
   char *t = static_cast<char *>(temp);
-  uint32_t *hist = reinterpret_cast<uint32_t *>(t + L.hist);
-  uint32_t *counters = reinterpret_cast<uint32_t *>(t + L.counters);
-  uint32_t *err = reinterpret_cast<uint32_t *>(t + L.err);
-  uint32_t *status = reinterpret_cast<uint32_t *>(t + L.status);
-  K *altK = reinterpret_cast<K *>(t + L.altKeys);
-  uint32_t *altV = reinterpret_cast<uint32_t *>(t + L.altVals);
+  uint32_t *hist = reinterpret_cast<uint32_t *>(t + Lmax.hist);
+  uint32_t *counters = reinterpret_cast<uint32_t *>(t + Lmax.counters);
+  uint32_t *err = reinterpret_cast<uint32_t *>(t + Lmax.err);
+  uint32_t *status = reinterpret_cast<uint32_t *>(t + Lmax.status);
+  K *altK = reinterpret_cast<K *>(t + Lmax.altKeys);
+  uint32_t *altV = reinterpret_cast<uint32_t *>(t + Lmax.altVals);
   if (n == 0) return BVHGB_OK;
   if (L.passes == 0) {
     BVHGB_CUDA_TRY(cudaMemcpyAsync(keysOut, keysIn, sizeof(K) * n, cudaMemcpyDeviceToDevice, s));
     BVHGB_CUDA_TRY(cudaMemcpyAsync(valsOut, valsIn, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s));
     return BVHGB_OK;
   }
-  BVHGB_CUDA_TRY(cudaMemsetAsync(t, 0, L.altKeys, s));
+  // hist, counters, err and the status words this tile size uses start at zero
+  BVHGB_CUDA_TRY(cudaMemsetAsync(t, 0, Lmax.status + sizeof(uint32_t) * kRadix * (size_t)L.tiles * L.passes, s));
   uint32_t hgrid = min(ceil_div(n, kThreads * 8), (uint32_t)sm_count() * 4);
-  histogram_kernel<K><<<hgrid, kThreads, sizeof(uint32_t) * kRadix * L.passes, s>>>(keysIn, n, beginBit, endBit, L.passes, hist);
+  histogram_kernel<K><<<hgrid, kThreads, sizeof(uint32_t) * kRadix * L.passes, s>>>(keysIn, n, beginBit, endBit,
+                                                                                      L.passes, hist);
   BVHGB_LAUNCH_CHECK("radix histogram");
   scan_kernel<<<L.passes, kRadix, 0, s>>>(hist);
   BVHGB_LAUNCH_CHECK("radix scan");
-  const size_t smem = sizeof(OnesweepSmem<K>);
   int st = sort_prepare();
   if (st) return st;
-  // Ping-pong so that the last pass lands in keysOut/valsOut.
-  const K *srcK = keysIn;
-  const uint32_t *srcV = valsIn;
-  for (uint32_t p = 0; p < L.passes; ++p) {
-    bool toOut = ((L.passes - 1 - p) % 2) == 0;
-    K *dstK = toOut ? keysOut : altK;
-    uint32_t *dstV = toOut ? valsOut : altV;
-    const uint32_t shift = beginBit + 8 * p;
-    onesweep_kernel<K><<<L.tiles, kThreads, smem, s>>>(srcK, dstK, srcV, dstV, n, shift, digit_mask(shift, endBit),
-                                                       hist + p * kRadix,
-                                                       counters + p, status + (size_t)p * L.tiles * kRadix, err);
-    BVHGB_LAUNCH_CHECK("radix onesweep");
-    srcK = dstK;
-    srcV = dstV;
+  switch (tileKeys) {
+    case 2048:
+      return onesweep_passes<K, 256, 8>(L, keysIn, keysOut, valsIn, valsOut, altK, altV, hist, counters, status, err, n,
+                                        beginBit, endBit, s);
+    case 4096:
+      return onesweep_passes<K, 256, 16>(L, keysIn, keysOut, valsIn, valsOut, altK, altV, hist, counters, status, err,
+                                         n, beginBit, endBit, s);
+    default:
+      return onesweep_passes<K, 512, 16>(L, keysIn, keysOut, valsIn, valsOut, altK, altV, hist, counters, status, err,
+                                         n, beginBit, endBit, s);
   }
-  return BVHGB_OK;
+}
+
+template <typename K, int THREADS, int ITEMS>
+cudaError_t set_smem_attr() {
+  return cudaFuncSetAttribute(onesweep_kernel<K, THREADS, ITEMS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)sizeof(OnesweepSmem<K, THREADS, ITEMS>));
 }
 
 }  // namespace
@@ -300,10 +329,12 @@ int sort_prepare() {
   // Opt in to more than 48 KB of dynamic shared memory once per process (before any capture).
   static int done = 0;
   if (done) return BVHGB_OK;
-  BVHGB_CUDA_TRY(cudaFuncSetAttribute(onesweep_kernel<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)sizeof(OnesweepSmem<uint32_t>)));
-  BVHGB_CUDA_TRY(cudaFuncSetAttribute(onesweep_kernel<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)sizeof(OnesweepSmem<uint64_t>)));
+  BVHGB_CUDA_TRY((set_smem_attr<uint32_t, 256, 8>()));
+  BVHGB_CUDA_TRY((set_smem_attr<uint32_t, 256, 16>()));
+  BVHGB_CUDA_TRY((set_smem_attr<uint32_t, 512, 16>()));
+  BVHGB_CUDA_TRY((set_smem_attr<uint64_t, 256, 8>()));
+  BVHGB_CUDA_TRY((set_smem_attr<uint64_t, 256, 16>()));
+  BVHGB_CUDA_TRY((set_smem_attr<uint64_t, 512, 16>()));
   done = 1;
   return BVHGB_OK;
 }
@@ -318,13 +349,12 @@ uint32_t *sort_error_word(void *temp, uint32_t n, uint32_t keyBytes, uint32_t be
 }
 
 int sort_pairs(void *temp, const void *keysIn, void *keysOut, const uint32_t *valsIn, uint32_t *valsOut, uint32_t n,
-               uint32_t keyBytes, uint32_t beginBit, uint32_t endBit, cudaStream_t s) {
-  Layout L = make_layout(n, keyBytes, beginBit, endBit);
+               uint32_t keyBytes, uint32_t beginBit, uint32_t endBit, cudaStream_t s, uint32_t tileKeys) {
   if (keyBytes == 4)
-    return sort_impl<uint32_t>(temp, L, static_cast<const uint32_t *>(keysIn), static_cast<uint32_t *>(keysOut), valsIn,
-                               valsOut, n, beginBit, endBit, s);
-  return sort_impl<uint64_t>(temp, L, static_cast<const uint64_t *>(keysIn), static_cast<uint64_t *>(keysOut), valsIn,
-                             valsOut, n, beginBit, endBit, s);
+    return sort_impl<uint32_t>(temp, tileKeys, static_cast<const uint32_t *>(keysIn), static_cast<uint32_t *>(keysOut),
+                               valsIn, valsOut, n, beginBit, endBit, s);
+  return sort_impl<uint64_t>(temp, tileKeys, static_cast<const uint64_t *>(keysIn), static_cast<uint64_t *>(keysOut),
+                             valsIn, valsOut, n, beginBit, endBit, s);
 }
 
 }  // namespace bvhgb

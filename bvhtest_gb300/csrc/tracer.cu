@@ -13,204 +13,12 @@
 #include <cmath>
 
 #include "common.cuh"
+#include "tracer_device.cuh"
 
 namespace bvhgb {
 namespace {
 
-constexpr int kStack = 96;
-constexpr float kFarScale = 1.0000004f;   // 1 + 2 * gamma(3), gamma(n) = n u / (1 - n u), u = 2^-24
-constexpr float kBestSlack = 1.0000153f;  // relative slack on the best t when culling boxes
-
 __device__ uint32_t g_trace_errors = 0;
-
-struct RayPre {
-  float o[3], d[3], inv[3];
-  float sx, sy, sz;
-  int kx, ky, kz;
-};
-
-__device__ __forceinline__ void setup_ray(RayPre &r) {
-#pragma unroll
-  for (int k = 0; k < 3; ++k) r.inv[k] = fdiv(1.0f, r.d[k]);
-  float ax = fabsf(r.d[0]), ay = fabsf(r.d[1]), az = fabsf(r.d[2]);
-  int kz = (ax >= ay) ? (ax >= az ? 0 : 2) : (ay >= az ? 1 : 2);
-  int kx = kz + 1 == 3 ? 0 : kz + 1;
-  int ky = kx + 1 == 3 ? 0 : kx + 1;
-  float dz = kz == 0 ? r.d[0] : (kz == 1 ? r.d[1] : r.d[2]);
-  if (dz < 0.0f) { int t = kx; kx = ky; ky = t; }
-  r.kx = kx; r.ky = ky; r.kz = kz;
-  float dx = kx == 0 ? r.d[0] : (kx == 1 ? r.d[1] : r.d[2]);
-  float dy = ky == 0 ? r.d[0] : (ky == 1 ? r.d[1] : r.d[2]);
-  r.sx = fdiv(dx, dz);
-  r.sy = fdiv(dy, dz);
-  r.sz = fdiv(1.0f, dz);
-}
-
-__device__ __forceinline__ float pick(const float *v, int k) { return k == 0 ? v[0] : (k == 1 ? v[1] : v[2]); }
-
-// Watertight ray/triangle test; every operation rounds once (matches the oracle bit for bit).
-__device__ __forceinline__ bool ray_tri(const RayPre &r, const float *v0, const float *v1, const float *v2, float tmin,
-                                        float tmax, bool cull, float &tout) {
-  float A[3], B[3], C[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    A[k] = fsub(v0[k], r.o[k]);
-    B[k] = fsub(v1[k], r.o[k]);
-    C[k] = fsub(v2[k], r.o[k]);
-  }
-  const float Akz = pick(A, r.kz), Bkz = pick(B, r.kz), Ckz = pick(C, r.kz);
-  const float Ax = fsub(pick(A, r.kx), fmul(r.sx, Akz)), Ay = fsub(pick(A, r.ky), fmul(r.sy, Akz));
-  const float Bx = fsub(pick(B, r.kx), fmul(r.sx, Bkz)), By = fsub(pick(B, r.ky), fmul(r.sy, Bkz));
-  const float Cx = fsub(pick(C, r.kx), fmul(r.sx, Ckz)), Cy = fsub(pick(C, r.ky), fmul(r.sy, Ckz));
-  float U = fsub(fmul(Cx, By), fmul(Cy, Bx));
-  float V = fsub(fmul(Ax, Cy), fmul(Ay, Cx));
-  float W = fsub(fmul(Bx, Ay), fmul(By, Ax));
-  if (U == 0.0f || V == 0.0f || W == 0.0f) {
-    U = (float)__dsub_rn(__dmul_rn((double)Cx, (double)By), __dmul_rn((double)Cy, (double)Bx));
-    V = (float)__dsub_rn(__dmul_rn((double)Ax, (double)Cy), __dmul_rn((double)Ay, (double)Cx));
-    W = (float)__dsub_rn(__dmul_rn((double)Bx, (double)Ay), __dmul_rn((double)By, (double)Ax));
-  }
-  if (cull) {
-    if (U < 0.0f || V < 0.0f || W < 0.0f) return false;
-  } else {
-    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
-  }
-  const float det = fadd(fadd(U, V), W);
-  if (det == 0.0f) return false;
-  const float Az = fmul(r.sz, Akz), Bz = fmul(r.sz, Bkz), Cz = fmul(r.sz, Ckz);
-  const float T = fadd(fadd(fmul(U, Az), fmul(V, Bz)), fmul(W, Cz));
-  const float t = fdiv(T, det);
-  if (!(t > tmin) || !(t <= tmax)) return false;
-  tout = t;
-  return true;
-}
-
-// Robust slab test; sign-selected planes make 0 * inf NaNs drop out of the min/max.
-__device__ __forceinline__ bool box_hit(const RayPre &r, float4 a, float4 b, float tmin, float tmax, float &tn) {
-  const float mn[3] = {a.x, a.y, a.z};
-  const float mx[3] = {a.w, b.x, b.y};
-  float t0 = tmin, t1 = tmax;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const bool neg = r.inv[k] < 0.0f || (r.inv[k] == 0.0f && signbit(r.inv[k]));
-    const float nearP = neg ? mx[k] : mn[k], farP = neg ? mn[k] : mx[k];
-    const float tNear = fmul(fsub(nearP, r.o[k]), r.inv[k]);
-    const float tFar = fmul(fmul(fsub(farP, r.o[k]), r.inv[k]), kFarScale);
-    t0 = fmaxf(t0, tNear);
-    t1 = fminf(t1, tFar);
-  }
-  tn = t0;
-  return t0 <= t1;
-}
-
-struct Hit {
-  uint32_t prim;
-  float t;
-};
-
-__device__ __forceinline__ void load_tri(const float *__restrict__ vert, const uint32_t *__restrict__ faces, uint32_t f,
-                                         float *v0, float *v1, float *v2) {
-  const uint32_t a = __ldg(faces + 3 * (size_t)f), b = __ldg(faces + 3 * (size_t)f + 1), c = __ldg(faces + 3 * (size_t)f + 2);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    v0[k] = __ldg(vert + 3 * (size_t)a + k);
-    v1[k] = __ldg(vert + 3 * (size_t)b + k);
-    v2[k] = __ldg(vert + 3 * (size_t)c + k);
-  }
-}
-
-__device__ __forceinline__ void test_leaf(const RayPre &r, const float *__restrict__ vert,
-                                          const uint32_t *__restrict__ faces, uint32_t first, uint32_t count,
-                                          float tmin, float tmax, bool cull, Hit &h) {
-  for (uint32_t f = first; f < first + count; ++f) {
-    float v0[3], v1[3], v2[3], t;
-    load_tri(vert, faces, f, v0, v1, v2);
-    if (ray_tri(r, v0, v1, v2, tmin, tmax, cull, t)) {
-      if (h.prim == kNone || t < h.t || (t == h.t && f < h.prim)) {
-        h.t = t;
-        h.prim = f;
-      }
-    }
-  }
-}
-
-// Closest hit through the 48-byte node array. Returns the number of inner nodes visited.
-__device__ __forceinline__ uint32_t traverse(const RayPre &r, const bvhgb_node *__restrict__ nodes, uint32_t numNodes,
-                                             uint32_t root, const float *__restrict__ vert,
-                                             const uint32_t *__restrict__ faces, float tmin, float tmax, bool cull,
-                                             Hit &h) {
-  uint2 stack[kStack];
-  int sp = 0;
-  uint32_t visits = 0;
-  h.prim = kNone;
-  h.t = tmax;
-  float4 a, b, c;
-  load_node(nodes, root, a, b, c);
-  float tn;
-  if (!box_hit(r, a, b, tmin, tmax, tn)) return 0;
-  uint32_t left = __float_as_uint(b.w), right = __float_as_uint(c.x);
-  bool leaf = (__float_as_uint(c.y) & 0xFFFFu) != 0;
-  // A tree visits each node at most once; the bound turns a cyclic (corrupted) input into an error.
-  for (uint32_t it = 0;; ++it) {
-    if (it > numNodes) {
-      atomicOr(&g_trace_errors, kErrBadIndex);
-      break;
-    }
-    if (leaf) {
-      test_leaf(r, vert, faces, left, right, tmin, tmax, cull, h);
-    } else {
-      ++visits;
-      if (left >= numNodes || right >= numNodes) {
-        atomicOr(&g_trace_errors, kErrBadIndex);
-      } else {
-        float4 la, lb, lc, ra, rb, rc;
-        load_node(nodes, left, la, lb, lc);
-        load_node(nodes, right, ra, rb, rc);
-        const float lim = h.prim == kNone ? tmax : fmul(h.t, kBestSlack);
-        float tl, tr;
-        const bool hl = box_hit(r, la, lb, tmin, lim, tl);
-        const bool hr = box_hit(r, ra, rb, tmin, lim, tr);
-        if (hl && hr) {
-          const bool lfirst = tl <= tr;
-          const uint32_t farIdx = lfirst ? right : left;
-          if (sp < kStack) stack[sp++] = make_uint2(farIdx, __float_as_uint(lfirst ? tr : tl));
-          else atomicOr(&g_trace_errors, kErrStackOverflow);
-          const float4 &nb = lfirst ? lb : rb;
-          const float4 &nc = lfirst ? lc : rc;
-          left = __float_as_uint(nb.w);
-          right = __float_as_uint(nc.x);
-          leaf = (__float_as_uint(nc.y) & 0xFFFFu) != 0;
-          continue;
-        }
-        if (hl || hr) {
-          const float4 &nb = hl ? lb : rb;
-          const float4 &nc = hl ? lc : rc;
-          left = __float_as_uint(nb.w);
-          right = __float_as_uint(nc.x);
-          leaf = (__float_as_uint(nc.y) & 0xFFFFu) != 0;
-          continue;
-        }
-      }
-    }
-    // Pop the next subtree whose entry distance can still beat the best hit.
-    bool found = false;
-    while (sp > 0) {
-      const uint2 e = stack[--sp];
-      const float lim = h.prim == kNone ? tmax : fmul(h.t, kBestSlack);
-      if (__uint_as_float(e.y) <= lim) {
-        const float4 *p = reinterpret_cast<const float4 *>(nodes + e.x);
-        const float4 nb = __ldg(p + 1), nc = __ldg(p + 2);
-        left = __float_as_uint(nb.w);
-        right = __float_as_uint(nc.x);
-        leaf = (__float_as_uint(nc.y) & 0xFFFFu) != 0;
-        found = true;
-        break;
-      }
-    }
-    if (!found) break;
-  }
-  return visits;
-}
 
 __device__ __forceinline__ void normalize3(float *v) {
   const float l2 = fadd(fadd(fmul(v[0], v[0]), fmul(v[1], v[1])), fmul(v[2], v[2]));
@@ -347,7 +155,7 @@ __global__ void __launch_bounds__(128) trace_bounce_kernel(const bvhgb_node *__r
   }
   setup_ray(r);
   Hit h;
-  traverse(r, nodes, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h);
+  traverse(r, nodes, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
   o.primId = h.prim;
   o.t = h.prim == kNone ? __int_as_float(0x7f800000) : h.t;
   out[pix] = o;
@@ -364,7 +172,7 @@ __global__ void __launch_bounds__(128) trace_image_kernel(const bvhgb_node *__re
   RayPre r;
   camera_ray(cam, x, y, r);
   Hit h;
-  const uint32_t visits = traverse(r, nodes, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h);
+  const uint32_t visits = traverse(r, nodes, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
   bvhgb_pixel px_out;
   px_out.hit = 0;
   px_out.diffuse = 0;
@@ -400,7 +208,7 @@ __global__ void __launch_bounds__(128) trace_rays_kernel(const bvhgb_node *__res
   }
   setup_ray(r);
   Hit h;
-  traverse(r, nodes, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h);
+  traverse(r, nodes, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
   bvhgb_hit o;
   o.primId = h.prim;
   o.t = h.prim == kNone ? __int_as_float(0x7f800000) : h.t;

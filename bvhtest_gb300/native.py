@@ -59,6 +59,18 @@ class TraceConfig(C.Structure):
     _fields_ = [("light", C.c_float * 3), ("faceCulling", C.c_uint32), ("tmin", C.c_float), ("tmax", C.c_float)]
 
 
+class BatchConfig(C.Structure):
+    _fields_ = [("mortonBits", C.c_uint32), ("topology", C.c_uint32), ("numChunks", C.c_uint32),
+                ("batchPercent", C.c_float), ("sortTileKeys", C.c_uint32), ("refitBlock", C.c_uint32),
+                ("traceBlock", C.c_uint32)]
+
+
+class BatchTuneReport(C.Structure):
+    _fields_ = [("sortTileKeys", C.c_uint32 * 3), ("sortTileMs", C.c_float * 3), ("refitBlock", C.c_uint32 * 3),
+                ("refitBlockMs", C.c_float * 3), ("traceBlock", C.c_uint32 * 3), ("traceBlockMs", C.c_float * 3),
+                ("chosen", BatchConfig)]
+
+
 class MeshRaw(C.Structure):
     _fields_ = [("vert", C.c_void_p), ("norm", C.c_void_p), ("faces", C.c_void_p), ("numVert", C.c_uint32),
                 ("numNorm", C.c_uint32), ("numFaces", C.c_uint32)]
@@ -103,6 +115,17 @@ PROTOS = {
     "bvhgb_bn13_set_iteration": (I32, [VP, U64]),
     "bvhgb_bn13_read_selection": (I32, [VP, VP, U32, VP]),
     "bvhgb_bn13_set_selection": (I32, [VP, VP, U32, VP]),
+    "bvhgb_batch_create": (I32, [U32, VP, C.POINTER(BatchConfig), C.POINTER(VP)]),
+    "bvhgb_batch_destroy": (I32, [VP]),
+    "bvhgb_batch_offsets": (I32, [VP, VP, VP]),
+    "bvhgb_batch_get_config": (I32, [VP, C.POINTER(BatchConfig)]),
+    "bvhgb_batch_set_config": (I32, [VP, C.POINTER(BatchConfig)]),
+    "bvhgb_batch_build": (I32, [VP, VP, VP, VP, VP]),
+    "bvhgb_batch_optimize": (I32, [VP, VP, U32, VP]),
+    "bvhgb_batch_trace_random": (I32, [VP, VP, VP, VP, U32, U64, VP, VP, VP, VP]),
+    "bvhgb_batch_run": (I32, [VP, VP, VP, VP, U32, U32, U64, VP, VP]),
+    "bvhgb_batch_get_stats": (I32, [VP, C.POINTER(Bn13Stats), C.POINTER(U32), VP]),
+    "bvhgb_batch_autotune": (I32, [VP, VP, VP, VP, U32, U64, VP, C.POINTER(BatchTuneReport), VP]),
     "bvhgb_mlp_create": (I32, [U64, C.POINTER(VP)]),
     "bvhgb_mlp_destroy": (I32, [VP]),
     "bvhgb_mlp_set_params": (I32, [VP, VP]),

@@ -80,3 +80,26 @@ def random_rays(n: int, lo, hi, seed: int = 3):
     d = g.normal(0.0, 1.0, (n, 3))
     d /= np.linalg.norm(d, axis=1, keepdims=True)
     return org.astype(np.float32), d.astype(np.float32)
+
+
+def batch_meshes(count: int = 256, lo: int = 1024, hi: int = 524288, seed: int = 9, clusters=(1, 16),
+                 sigma=(0.005, 0.08), vertex_sigma: float = 0.004):
+    """Batched-build scenes: count meshes with log-uniform triangle counts in [lo, hi]; mesh m is a
+    Gaussian mixture in the unit cube (1-16 clusters, means uniform in [0,1]^3, sigma log-uniform in
+    the given range, per-vertex offsets N(0, vertex_sigma^2)) with its own seed. Returns
+    (vert [sum 3n, 3] float32, faces [sum n, 3] uint32 indexing the concatenated vertices, counts)."""
+    g = _rng(seed)
+    counts = np.exp(g.uniform(np.log(lo), np.log(hi), count)).astype(np.int64).clip(lo, hi)
+    verts, faces, base = [], [], 0
+    for m, n in enumerate(counts.tolist()):
+        k = int(g.integers(clusters[0], clusters[1] + 1))
+        gm = _rng(seed * 1000003 + m)
+        means = gm.random((k, 3))
+        sig = np.exp(gm.uniform(np.log(sigma[0]), np.log(sigma[1]), k))
+        comp = gm.integers(0, k, n)
+        c = means[comp] + gm.normal(0.0, 1.0, (n, 3)) * sig[comp, None]
+        v = (c[:, None, :] + gm.normal(0.0, vertex_sigma, (n, 3, 3))).astype(np.float32).reshape(-1, 3)
+        verts.append(v)
+        faces.append((np.arange(3 * n, dtype=np.uint32).reshape(n, 3) + base).astype(np.uint32))
+        base += 3 * n
+    return np.concatenate(verts), np.concatenate(faces), counts.astype(np.uint32)

@@ -318,6 +318,77 @@ BVHGB_API int bvhgb_bn13_set_selection(bvhgb_bn13_workspace *ws, const uint32_t 
 BVHGB_API int bvhgb_bn13_read_selection(const bvhgb_bn13_workspace *ws, uint32_t *out, uint32_t capacity,
                                         bvhgb_stream stream);
 
+/* ---- batched multi-mesh pipeline ------------------------------------------------------------------
+ * No counterpart in the reference (its commands take one mesh at a time: LBVH.cpp, Bittner13GPU.cpp,
+ * CUDATracer.cpp). Many independent meshes of uneven size are built, optimised and traced together,
+ * one launch per phase for the whole batch; bvhgb_batch_run captures build + iterations + trace as one
+ * CUDA graph. Each mesh's node array equals what bvhgb_lbvh_build + bvhgb_bn13_run give for that mesh
+ * alone (same topology mode, 30-bit Morton codes, same optimizer settings).
+ *
+ * Inputs: vert = the meshes' float3 vertices concatenated; faces = their uint3 faces concatenated,
+ * mesh after mesh (faceCounts[m] faces each), with vertex indices into the concatenated vertices.
+ * Output: nodes = mesh m's 2 * faceCounts[m] - 1 nodes at node offset m (bvhgb_batch_offsets), child
+ * indices local to the mesh, leaves naming faces by their index within the mesh, root 0. */
+typedef struct bvhgb_batch_config {
+  uint32_t mortonBits;   /* 30 */
+  uint32_t topology;     /* BVHGB_TOPO_REFCOMPAT or BVHGB_TOPO_KARRAS */
+  uint32_t numChunks;    /* Bittner13 chunks per iteration (32) */
+  float batchPercent;    /* Bittner13 batch, % of each mesh's nodes (1.0) */
+  uint32_t sortTileKeys; /* tuning: keys per CTA in the sort passes (2048, 4096, 8192) */
+  uint32_t refitBlock;   /* tuning: threads per block of the apply / count / refit kernels */
+  uint32_t traceBlock;   /* tuning: threads per block of the tracer */
+} bvhgb_batch_config;
+
+typedef struct bvhgb_batch_workspace bvhgb_batch_workspace;
+
+/* Workspace for numMeshes (<= 4096) meshes of faceCounts[m] (host array) faces; cfg NULL = defaults. */
+BVHGB_API int bvhgb_batch_create(uint32_t numMeshes, const uint32_t *faceCounts, const bvhgb_batch_config *cfg,
+                                 bvhgb_batch_workspace **out);
+BVHGB_API int bvhgb_batch_destroy(bvhgb_batch_workspace *ws);
+/* Host copies of the numMeshes + 1 face and node offsets (either may be NULL). */
+BVHGB_API int bvhgb_batch_offsets(const bvhgb_batch_workspace *ws, uint32_t *faceOffsets, uint32_t *nodeOffsets);
+BVHGB_API int bvhgb_batch_get_config(const bvhgb_batch_workspace *ws, bvhgb_batch_config *cfg);
+/* Changes the tuning knobs and the topology (other fields must be unchanged). */
+BVHGB_API int bvhgb_batch_set_config(bvhgb_batch_workspace *ws, const bvhgb_batch_config *cfg);
+/* LBVH of every mesh (scene boxes, Morton codes, one sort, build + refit). */
+BVHGB_API int bvhgb_batch_build(bvhgb_batch_workspace *ws, const float *vert, const uint32_t *faces, bvhgb_node *nodes,
+                                bvhgb_stream stream);
+/* Bittner13 iterations of every mesh (selection + chunks, each chunk of all meshes at once). */
+BVHGB_API int bvhgb_batch_optimize(bvhgb_batch_workspace *ws, bvhgb_node *nodes, uint32_t iterations,
+                                   bvhgb_stream stream);
+/* raysPerMesh random rays per mesh (origins uniform in the mesh box grown 1.5x about its centre,
+ * directions uniform on the sphere, from a counter hash of seed), closest hit in the mesh's tree:
+ * hits[m * raysPerMesh + j] = (face index within the mesh, t). rayOrg / rayDir (float3 per ray, both
+ * or neither) receive the rays. */
+BVHGB_API int bvhgb_batch_trace_random(bvhgb_batch_workspace *ws, const bvhgb_node *nodes, const float *vert,
+                                       const uint32_t *faces, uint32_t raysPerMesh, uint64_t seed, bvhgb_hit *hits,
+                                       float *rayOrg, float *rayDir, bvhgb_stream stream);
+/* build + iterations + trace captured once as one CUDA graph (again whenever an argument changes)
+ * and launched on stream. */
+BVHGB_API int bvhgb_batch_run(bvhgb_batch_workspace *ws, const float *vert, const uint32_t *faces, bvhgb_node *nodes,
+                              uint32_t iterations, uint32_t raysPerMesh, uint64_t seed, bvhgb_hit *hits,
+                              bvhgb_stream stream);
+/* Optimizer statistics summed over the batch, and the device error bits (synchronous). */
+BVHGB_API int bvhgb_batch_get_stats(bvhgb_batch_workspace *ws, bvhgb_bn13_stats *stats, uint32_t *errors,
+                                    bvhgb_stream stream);
+
+typedef struct bvhgb_batch_tune_report {
+  uint32_t sortTileKeys[3];
+  float sortTileMs[3];   /* batched build with each sort tile */
+  uint32_t refitBlock[3];
+  float refitBlockMs[3]; /* one optimizer iteration with each apply / count / refit block */
+  uint32_t traceBlock[3];
+  float traceBlockMs[3]; /* the random-ray trace with each tracer block */
+  bvhgb_batch_config chosen;
+} bvhgb_batch_tune_report;
+
+/* Autotuner: times the candidates of each knob on the caller's data (coordinate search, CUDA events,
+ * best of two runs each) and keeps the fastest in the workspace. Results do not depend on the knobs.
+ * Leaves nodes holding a one-iteration tree; synchronous. */
+BVHGB_API int bvhgb_batch_autotune(bvhgb_batch_workspace *ws, const float *vert, const uint32_t *faces,
+                                   bvhgb_node *nodes, uint32_t raysPerMesh, uint64_t seed, bvhgb_hit *hits,
+                                   bvhgb_batch_tune_report *report, bvhgb_stream stream);
+
 /* ---- tracer (lib/tracer/CUDAKernels.hpp:39-77, CUDATracer.cpp:86-118) ------------------------ */
 
 typedef struct bvhgb_camera {
