@@ -8,7 +8,8 @@ diffuse bounce per hit. Synthetic inputs stand in for the reference's mesh files
 
 One step = build + optimize + trace. `value` is the build + optimize time in ms (inputs already in
 HBM); `e2e` is the same metric through the C ABI with the mesh copied from pinned host memory
-and the optimised node array copied back inside the timed region. `learned_vs_plain` trains the
+and the optimised node array copied back inside the timed region. `batched` builds, optimises and
+traces 256 meshes of uneven size as one captured graph after autotuning. `learned_vs_plain` trains the
 learned reinsertion scorer (32 seeded 65,536-triangle scenes, about 52M logged pairs, 20k AdamW
 steps) and times build + optimisation to equal SAH on an unseen scene, plain against learned.
 
@@ -383,7 +384,67 @@ def run_ours(args, w, rank, world, local):
                 line["roofline_search"] = line["roofline"]
                 line["roofline"] = big["roofline"]
         line["learned_vs_plain"] = learned_arm(args, dev, flush, stream)
+    if not args.no_batch:
+        line["batched"] = batch_arm(args, dev, flush)
     print(json.dumps(line), flush=True)
+
+
+def batch_arm(args, dev, flush):
+    """Batched build (256 meshes, log-uniform 1,024..524,288 triangles, about 20M in total): autotune,
+    then time the whole pipeline (LBVH, 50 Bittner13 iterations, 65,536 random rays per mesh) as one
+    captured CUDA graph, plus each phase on its own."""
+    import torch
+    from bvhtest_gb300 import api, native, scenes
+
+    lib = native.load()
+    iters, rays = 50, 65536
+    vert_h, faces_h, counts = scenes.batch_meshes(256, 1024, 524288, seed=9)
+    v = torch.from_numpy(vert_h).to(dev)
+    f = torch.from_numpy(faces_h.view(np.int32)).to(dev)
+    b = api.Batch(counts)
+    nodes = b.empty_nodes()
+    hits = torch.empty(256 * rays, dtype=torch.int64, device=dev)
+    tune = b.autotune(v, f, nodes, rays, hits, seed=11)
+
+    def timed(fn):
+        out = []
+        for i in range(args.warmup + args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            if i >= args.warmup:
+                out.append(e0.elapsed_time(e1))
+        return statistics.mean(out)
+
+    c0 = lib.bvhgb_launch_count()
+    graph_ms = timed(lambda: b.run(v, f, nodes, iters, rays, hits, seed=11))
+    launches = (lib.bvhgb_launch_count() - c0) // (args.warmup + args.steps)
+    build_ms = timed(lambda: b.build(v, f, nodes))
+
+    def build_opt():
+        b.build(v, f, nodes)
+        b.optimize(nodes, iters)
+    opt_ms = timed(build_opt) - build_ms
+    trace_ms = timed(lambda: b.trace_random(nodes, v, f, rays, seed=11))
+    st, err = b.stats()
+    h = api.hits_to_numpy(hits)
+    n = int(counts.sum())
+    return {
+        "workload": ("256 meshes, triangle counts log-uniform in [1,024, 524,288], each a Gaussian mixture in the "
+                     "unit cube with 1-16 clusters and its own seed; 30-bit Morton, refCompat LBVH, 50 Bittner13 "
+                     "iterations at 1% (32 chunks), 65,536 random rays per mesh (origins in the mesh box grown "
+                     "1.5x, directions uniform on the sphere)"),
+        "meshes": 256, "triangles": n, "min_triangles": int(counts.min()), "max_triangles": int(counts.max()),
+        "pipeline_ms": round(graph_ms, 3), "build_ms": round(build_ms, 3), "optimize_ms": round(opt_ms, 3),
+        "trace_ms": round(trace_ms, 3), "rays": 256 * rays, "mrays_per_s": round(256 * rays / (trace_ms * 1e-3) / 1e6, 1),
+        "build_mtris_per_s": round(n / (build_ms * 1e-3) / 1e6, 1), "gpu_launches": int(launches),
+        "hit_fraction": round(float((h["prim"] != 0xFFFFFFFF).mean()), 4), "errors": err,
+        "autotune": tune, "launch": "one CUDA graph per pipeline (build + iterations + trace)",
+    }
 
 
 def first_hit(opt, nodes, target, max_iters, rebuild):
@@ -635,6 +696,7 @@ def main():
                     help="do not bracket the search kernel with CUDA events (for runs under ncu)")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-scorer comparison")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched multi-mesh build")
     ap.add_argument("--only", choices=["build", "optimize", "trace"], default=None,
                     help="repeat one phase only and print its time (profiling runs; no benchmark record)")
     ap.add_argument("--scorer", default=None, help="with --only optimize: learned selection with these weights")
