@@ -647,11 +647,40 @@ def learned_arm(args, dev, flush, stream):
     }
 
 
+def run_batch_phase(args):
+    """--only batch: the batched 256-mesh scene, build + args.iters Bittner13 iterations per run."""
+    import torch
+    from bvhtest_gb300 import api, scenes
+    vert_h, faces_h, counts = scenes.batch_meshes(256, 1024, 524288, seed=9)
+    v = torch.from_numpy(vert_h).cuda()
+    f = torch.from_numpy(faces_h.view(np.int32)).cuda()
+    b = api.Batch(counts, topology=args.batch_topology)
+    nodes = b.empty_nodes()
+    iters = args.iters if args.iters is not None else 50
+    times = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        b.build(v, f, nodes)
+        b.optimize(nodes, iters)
+        e1.record()
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            times.append(e0.elapsed_time(e1))
+    st, err = b.stats()
+    print(f"batch: {statistics.mean(times):.3f} ms mean over {args.steps} runs ({iters} iterations, "
+          f"{args.batch_topology}); visits {st['nodesVisited']} items {st['items']} applied {st['applied']} err {err}",
+          flush=True)
+
+
 def run_phase(args, w):
     """--only PHASE: repeat one phase of the pipeline (for profilers; prints one timing line, not the
     benchmark record)."""
     import torch
     from bvhtest_gb300 import api
+    if args.only == "batch":
+        return run_batch_phase(args)
     n = int(w["faces"].shape[0])
     vert = torch.from_numpy(w["vert"]).cuda()
     faces = torch.from_numpy(w["faces"].view(np.int32)).cuda()
@@ -697,7 +726,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-scorer comparison")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched multi-mesh build")
-    ap.add_argument("--only", choices=["build", "optimize", "trace"], default=None,
+    ap.add_argument("--batch-topology", choices=["refCompat", "karras"], default="refCompat",
+                    help="with --only batch: the LBVH topology of the batched meshes")
+    ap.add_argument("--only", choices=["build", "optimize", "trace", "batch"], default=None,
                     help="repeat one phase only and print its time (profiling runs; no benchmark record)")
     ap.add_argument("--scorer", default=None, help="with --only optimize: learned selection with these weights")
     ap.add_argument("--plain-every", type=int, default=2, help="with --scorer: every k-th iteration is plain")
