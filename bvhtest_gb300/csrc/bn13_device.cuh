@@ -341,6 +341,13 @@ __device__ __forceinline__ void bitonic_merge(float (&c)[S], uint32_t (&n)[S], u
   for (int j = S * 16; j > 0; j >>= 1) bitonic_stage<S>(c, n, j, S * 32, false, lane);
 }
 
+// Per-warp scratch of the children's rank sort (blocks of up to kRankWarps warps).
+constexpr int kRankWarps = 8;
+__device__ __forceinline__ uint2 *rank_buffer() {
+  __shared__ uint2 buf[kRankWarps][32];
+  return buf[(threadIdx.x >> 5) & (kRankWarps - 1)];
+}
+
 // findNode1's cost model in batched rounds (every lane of the warp calls it with the same patch).
 __device__ uint32_t find_node_batched(const Patch &p, uint32_t n, SearchCounters &ctr) {
   const uint32_t lane = threadIdx.x & 31u;
@@ -414,9 +421,25 @@ __device__ uint32_t find_node_batched(const Patch &p, uint32_t n, SearchCounters
       const uint32_t src = lane < m ? __fns(kmask, 0, (lane >> 1) + 1) : lane;
       const float sc = __shfl_sync(kFull, induced, src);
       const uint32_t sl = __shfl_sync(kFull, cn.left, src), sr = __shfl_sync(kFull, cn.right, src);
-      float c1[1] = {lane < m ? sc : kInf};
-      uint32_t n1[1] = {lane < m ? ((lane & 1) ? sr : sl) : kNone};
-      bitonic_sort<1>(c1, n1, true, lane);
+      const float cj = lane < m ? sc : kInf;
+      const uint32_t nj = lane < m ? ((lane & 1) ? sr : sl) : kNone;
+      // Descending order of the children by rank: child j's rank is the number of children below
+      // it in (cost, node) order (keys are distinct: a node enters the frontier once), and it goes
+      // to lane 31 - rank; the unused lanes fill lanes 0 .. 31 - m with the empty entry. The same
+      // order the bitonic sort gives, with m independent broadcasts instead of 15 dependent stages.
+      uint32_t rank = 0;
+      for (uint32_t i = 0; i < m; ++i) {
+        const float ci = __shfl_sync(kFull, cj, i);
+        const uint32_t ni = __shfl_sync(kFull, nj, i);
+        rank += (ci < cj || (ci == cj && ni < nj)) ? 1u : 0u;
+      }
+      uint2 *buf = rank_buffer();
+      buf[lane < m ? 31u - rank : lane - m] = make_uint2(__float_as_uint(cj), nj);
+      __syncwarp();
+      const uint2 e = buf[lane];
+      __syncwarp();
+      float c1[1] = {__uint_as_float(e.x)};
+      uint32_t n1[1] = {e.y};
       if (rest <= 32) {
         float mc[2] = {fc[1], c1[0]};
         uint32_t mn[2] = {fn[1], n1[0]};
