@@ -99,6 +99,252 @@ __global__ void __launch_bounds__(256) mlp_forward_kernel(const __nv_bfloat16 *_
   }
 }
 
+// ---- inference on the 5th-generation tensor cores (tcgen05) ----------------------------------------
+// Persistent CTAs of 4 warps; a tile is 128 rows. Layer 1: D1[128 x 64] = X[128 x 32] * W1^T (the 24
+// features padded to K = 32), layer 2: D2[128 x 64] = A1[128 x 64] * W2^T, both BF16 operands in
+// shared memory and FP32 accumulators in tensor memory (columns 0-63 and 64-127 of a 128-column
+// allocation). Thread 0 issues the MMAs and commits them to an mbarrier; each warp then reads its 32
+// accumulator rows (TMEM lanes 32w .. 32w + 31) with tcgen05.ld, adds the bias, applies GELU and
+// rounds to BF16 (layer 1 into the next A operand, layer 2 straight into the 64 -> 1 dot product).
+// Operand layout: the no-swizzle K-major canonical layout of 8-row x 16-byte core matrices, core
+// (r8, k8) at r8 * SBO + k8 * LBO with LBO = 128 bytes (next 8 K-elements) and SBO = K * 16 bytes
+// (next 8 rows); an MMA consumes K = 16, so its descriptors advance by 2 * LBO per step.
+constexpr int kTcRows = 128;
+constexpr uint32_t kTcCols = 128;        // tensor-memory columns per CTA
+constexpr int kTcK1 = 32;                // layer-1 K (24 features + zero padding)
+constexpr uint32_t kTcWaitLimit = 1u << 22;
+
+struct TcSmem {
+  alignas(128) uint8_t a1[kTcRows * kTcK1 * 2];  // X tile, 8 KB
+  alignas(128) uint8_t b1[kH * kTcK1 * 2];       // W1 (N = 64 rows x K = 32), 4 KB
+  alignas(128) uint8_t a2[kTcRows * kH * 2];     // layer-1 activations, 16 KB
+  alignas(128) uint8_t b2[kH * kH * 2];          // W2 (64 x 64), 8 KB
+  float b1f[kH], b2f[kH], w3f[kH], b3f;
+  alignas(8) uint64_t bar;
+  uint32_t tmem;
+  uint32_t fail;
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// byte offset of element (row, k) of a K-major operand with K columns in the core-matrix layout
+__device__ __forceinline__ uint32_t core_off(uint32_t row, uint32_t k, uint32_t K) {
+  return (row >> 3) * (K * 16u) + (k >> 3) * 128u + (row & 7u) * 16u + (k & 7u) * 2u;
+}
+
+__device__ __forceinline__ uint64_t tc_smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1u << 46;  // descriptor version 0b001 (bits 46-48); base offset 0; no swizzle (bits 61-63 = 0)
+  return d;
+}
+
+// kind::f16 instruction descriptor: FP32 accumulator, BF16 A and B, both K-major, N = 64, M = 128.
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kH >> 3) << 17) |
+                              ((uint32_t)(kTcRows >> 4) << 24);
+
+__device__ __forceinline__ void tc_mma(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(a), "l"(b), "r"(kTcIdesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for the phase 'parity' of the barrier; false (and the CTA's fail flag) on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t *fail) {
+  for (uint32_t i = 0; i < kTcWaitLimit; ++i) {
+    if (mbar_try(bar, parity)) return true;
+    if (i > 64) __nanosleep(64);
+  }
+  atomicOr(fail, 1u);
+  return false;
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 32 consecutive FP32 accumulator columns of this thread's TMEM lane.
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <bool KEYS>
+__global__ void __launch_bounds__(128, 4) mlp_forward_tc_kernel(const __nv_bfloat16 *__restrict__ w,
+                                                                const uint16_t *__restrict__ x, uint32_t n,
+                                                                float *__restrict__ y,
+                                                                const uint32_t *__restrict__ inner,
+                                                                uint32_t *__restrict__ keys,
+                                                                uint32_t *__restrict__ vals, uint32_t *err) {
+  __shared__ TcSmem sm;
+  const uint32_t tid = threadIdx.x, warp = tid >> 5;
+  const uint16_t *wb = reinterpret_cast<const uint16_t *>(w);
+  // weights -> B operands (zero K padding for layer 1) and FP32 epilogue constants
+  for (uint32_t i = tid; i < (uint32_t)(kH * kTcK1); i += blockDim.x) {
+    const uint32_t j = i / kTcK1, k = i % kTcK1;
+    *reinterpret_cast<uint16_t *>(sm.b1 + core_off(j, k, kTcK1)) = k < (uint32_t)kIn ? wb[oW1 + j * kIn + k] : 0;
+  }
+  for (uint32_t i = tid; i < (uint32_t)(kH * kH); i += blockDim.x) {
+    const uint32_t j = i / kH, k = i % kH;
+    *reinterpret_cast<uint16_t *>(sm.b2 + core_off(j, k, kH)) = wb[oW2 + j * kH + k];
+  }
+  for (uint32_t i = tid; i < (uint32_t)kH; i += blockDim.x) {
+    sm.b1f[i] = __bfloat162float(w[oB1 + i]);
+    sm.b2f[i] = __bfloat162float(w[oB2 + i]);
+    sm.w3f[i] = __bfloat162float(w[oW3 + i]);
+  }
+  if (tid == 0) {
+    sm.b3f = __bfloat162float(w[oB3]);
+    sm.fail = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&sm.bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&sm.tmem)),
+                 "r"(kTcCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  proxy_fence();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = sm.tmem;
+  const uint32_t lanebase = (warp * 32u) << 16;  // this warp's TMEM lanes
+  const uint32_t a1 = smem_addr(sm.a1), b1 = smem_addr(sm.b1), a2 = smem_addr(sm.a2), b2 = smem_addr(sm.b2);
+  uint32_t phase = 0;
+  bool failed = false;  // block-uniform: decided by __syncthreads_or after every wait
+  const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
+  for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const uint32_t row = tile * kTcRows + tid;  // this thread's row (= its TMEM lane)
+    const bool live = row < n;
+    {  // feature row -> A1 (3 x 16 bytes of features, one 16-byte chunk of zero padding)
+      uint4 q[3] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
+      if (live) {
+        const uint4 *src = reinterpret_cast<const uint4 *>(x + (size_t)row * kIn);
+        q[0] = __ldg(src);
+        q[1] = __ldg(src + 1);
+        q[2] = __ldg(src + 2);
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) *reinterpret_cast<uint4 *>(sm.a1 + core_off(tid, 8 * c, kTcK1)) = q[c];
+      *reinterpret_cast<uint4 *>(sm.a1 + core_off(tid, 24, kTcK1)) = make_uint4(0, 0, 0, 0);
+    }
+    proxy_fence();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid == 0) {
+#pragma unroll
+      for (int k = 0; k < kTcK1 / 16; ++k)
+        tc_mma(tmem, tc_smem_desc(a1 + 256u * k, 128u, kTcK1 * 16u), tc_smem_desc(b1 + 256u * k, 128u, kTcK1 * 16u),
+               k > 0);
+      tc_commit(&sm.bar);
+    }
+    if (__syncthreads_or(!mbar_wait(&sm.bar, phase, &sm.fail))) {
+      failed = true;
+      break;
+    }
+    phase ^= 1u;
+    tc_fence_after();
+    // layer-1 epilogue: bias, GELU, BF16 -> A2 (this thread's row)
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      float v[32];
+      tc_ld32(tmem + lanebase + 32u * half, v);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        uint32_t u[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const int j0 = 32 * half + 8 * c + 2 * h;
+          const float g0 = gelu(v[8 * c + 2 * h] + sm.b1f[j0]), g1 = gelu(v[8 * c + 2 * h + 1] + sm.b1f[j0 + 1]);
+          u[h] = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(g0)) |
+                 ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(g1)) << 16);
+        }
+        *reinterpret_cast<uint4 *>(sm.a2 + core_off(tid, 32 * half + 8 * c, kH)) = make_uint4(u[0], u[1], u[2], u[3]);
+      }
+    }
+    proxy_fence();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid == 0) {
+#pragma unroll
+      for (int k = 0; k < kH / 16; ++k)
+        tc_mma(tmem + 64u, tc_smem_desc(a2 + 256u * k, 128u, kH * 16u), tc_smem_desc(b2 + 256u * k, 128u, kH * 16u),
+               k > 0);
+      tc_commit(&sm.bar);
+    }
+    if (__syncthreads_or(!mbar_wait(&sm.bar, phase, &sm.fail))) {
+      failed = true;
+      break;
+    }
+    phase ^= 1u;
+    tc_fence_after();
+    // layer-2 epilogue and layer 3: y = b3 + sum_j W3[j] * bf16(gelu(D2[j] + b2[j]))
+    float out = sm.b3f;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      float v[32];
+      tc_ld32(tmem + lanebase + 64u + 32u * half, v);
+#pragma unroll
+      for (int i = 0; i < 32; ++i) out += sm.w3f[32 * half + i] * bf16r(gelu(v[i] + sm.b2f[32 * half + i]));
+    }
+    if (live) {
+      y[row] = out;
+      if (KEYS) {
+        keys[row] = ~f2ord(out);
+        vals[row] = __ldg(inner + row);
+      }
+    }
+    tc_fence_before();  // the next tile's MMAs overwrite the accumulators these loads read
+  }
+  // Release the tensor memory on every path. After a timeout an MMA may still be in flight: wait
+  // (bounded) for the last commit before freeing its columns.
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (failed) {
+    if (tid == 0) {
+      atomicOr(err, kErrTimeout);
+      mbar_wait(&sm.bar, phase, &sm.fail);
+    }
+    __syncthreads();
+  }
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols) : "memory");
+}
+
 // Forward + backward of one tile of kTile samples per block (one thread per sample). Gradients of
 // loss = sum (y - t)^2 / scaleN are added to grad (FP32); the tile's loss to loss[slot].
 constexpr int kTile = 128;
@@ -317,49 +563,63 @@ __global__ void leaf_count_kernel(const bvhgb_node *__restrict__ t, uint32_t n, 
   }
 }
 
+// Raw features and the four rank histograms. The loop is warp-uniform so that the lanes of a warp
+// that fall into the same histogram bin add their count with one atomic (the values of neighbouring
+// nodes are alike, so a few bins are hot).
 __global__ void features_raw_kernel(const bvhgb_node *__restrict__ t, const uint32_t *__restrict__ inner,
                                     uint32_t numInner, uint32_t numNodes, uint32_t root,
                                     const uint32_t *__restrict__ depth, const uint32_t *__restrict__ leafCount,
                                     float invLog2Leaves, float *__restrict__ raw, float *__restrict__ src,
                                     uint32_t *__restrict__ hist, uint32_t *__restrict__ err) {
   const float sroot = __ldg(&t[root].surfaceArea);
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < numInner; i += gridDim.x * blockDim.x) {
-    const uint32_t x = __ldg(inner + i);
-    if (x >= numNodes) {  // not a node: a zero row, flagged
-      atomicOr(err, kErrBadIndex);
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < numInner; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    const bool live = i < numInner;
+    float s4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (live) {
+      const uint32_t x = __ldg(inner + i);
+      if (x >= numNodes) {  // not a node: a zero row, flagged
+        atomicOr(err, kErrBadIndex);
 #pragma unroll
-      for (int k = 0; k < kMlpRaw; ++k) raw[(size_t)i * kMlpRaw + k] = 0.0f;
-      *reinterpret_cast<float4 *>(src + (size_t)i * 4) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        for (int k = 0; k < kMlpRaw; ++k) raw[(size_t)i * kMlpRaw + k] = 0.0f;
+      } else {
+        const float sa = __ldg(&t[x].surfaceArea);
+        const uint32_t l = min(__ldg(&t[x].left), numNodes - 1), r = min(__ldg(&t[x].right), numNodes - 1);
+        const float sl = __ldg(&t[l].surfaceArea), sr = __ldg(&t[r].surfaceArea);
+        const uint32_t p = x == root ? root : min(__ldg(&t[x].parent), numNodes - 1);
+        const uint32_t g = p == root ? root : min(__ldg(&t[p].parent), numNodes - 1);
+        const float mn = sl < sr ? sl : sr;
+        const float sum = fadd(sl, sr);
+        const float cost = fdiv(fmul(fmul(fmul(sa, sa), sa), 2.0f), fmul(sum, mn));  // kCalcCost
+        const uint32_t d = min(depth[x], 1u << kDepthRounds);
+        float f[kMlpRaw];
+        f[0] = log2f(sa);
+        f[1] = fdiv(sa, __ldg(&t[p].surfaceArea));
+        f[2] = fdiv(sa, __ldg(&t[g].surfaceArea));
+        f[3] = fdiv(sa, sum);
+        f[4] = fmul((float)d, invLog2Leaves);
+        f[5] = log2f((float)__ldcg(leafCount + l));
+        f[6] = log2f((float)__ldcg(leafCount + r));
+        f[7] = log2f(fdiv(sa, sroot));
+        f[8] = log2f(fdiv(sa, mn));
+        f[9] = log2f(cost);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) atomicAdd(hist + q * kRankBins + rank_bin(0.0f), 1u);
-      continue;
+        for (int k = 0; k < kMlpRaw; ++k) raw[(size_t)i * kMlpRaw + k] = clamp64(f[k]);
+        s4[0] = nan0(cost);
+        s4[1] = nan0(fdiv(sa, mn));
+        s4[2] = nan0(fdiv(sa, sum));
+        s4[3] = nan0(sa);
+      }
+      *reinterpret_cast<float4 *>(src + (size_t)i * 4) = make_float4(s4[0], s4[1], s4[2], s4[3]);
     }
-    const float sa = __ldg(&t[x].surfaceArea);
-    const uint32_t l = min(__ldg(&t[x].left), numNodes - 1), r = min(__ldg(&t[x].right), numNodes - 1);
-    const float sl = __ldg(&t[l].surfaceArea), sr = __ldg(&t[r].surfaceArea);
-    const uint32_t p = x == root ? root : min(__ldg(&t[x].parent), numNodes - 1);
-    const uint32_t g = p == root ? root : min(__ldg(&t[p].parent), numNodes - 1);
-    const float mn = sl < sr ? sl : sr;
-    const float sum = fadd(sl, sr);
-    const float cost = fdiv(fmul(fmul(fmul(sa, sa), sa), 2.0f), fmul(sum, mn));  // kCalcCost
-    const uint32_t d = min(depth[x], 1u << kDepthRounds);
-    float f[kMlpRaw];
-    f[0] = log2f(sa);
-    f[1] = fdiv(sa, __ldg(&t[p].surfaceArea));
-    f[2] = fdiv(sa, __ldg(&t[g].surfaceArea));
-    f[3] = fdiv(sa, sum);
-    f[4] = fmul((float)d, invLog2Leaves);
-    f[5] = log2f((float)__ldcg(leafCount + l));
-    f[6] = log2f((float)__ldcg(leafCount + r));
-    f[7] = log2f(fdiv(sa, sroot));
-    f[8] = log2f(fdiv(sa, mn));
-    f[9] = log2f(cost);
 #pragma unroll
-    for (int k = 0; k < kMlpRaw; ++k) raw[(size_t)i * kMlpRaw + k] = clamp64(f[k]);
-    const float s4[4] = {nan0(cost), nan0(fdiv(sa, mn)), nan0(fdiv(sa, sum)), nan0(sa)};
-    *reinterpret_cast<float4 *>(src + (size_t)i * 4) = make_float4(s4[0], s4[1], s4[2], s4[3]);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) atomicAdd(hist + q * kRankBins + rank_bin(s4[q]), 1u);
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t bin = live ? rank_bin(s4[q]) : 0xFFFFFFFFu;
+      const uint32_t peers = __match_any_sync(0xFFFFFFFFu, bin);
+      if (live && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(hist + q * kRankBins + bin, (uint32_t)__popc(peers));
+    }
   }
 }
 
@@ -429,6 +689,11 @@ __global__ void features_pack_kernel(const float *__restrict__ raw, const float 
       o[w] = make_uint4(u[0], u[1], u[2], u[3]);
     }
   }
+}
+
+// Persistent tensor-core CTAs: up to four per SM (4 x 128 of the 512 tensor-memory columns).
+uint32_t tc_grid(uint32_t rows) {
+  return std::max(1u, std::min(ceil_div(rows, kTcRows), (uint32_t)sm_count() * 4));
 }
 
 uint32_t grid_for(uint32_t n, uint32_t block) {
@@ -521,6 +786,7 @@ struct bvhgb_mlp {
   float *p = nullptr, *g = nullptr, *m = nullptr, *v = nullptr, *loss = nullptr;
   __nv_bfloat16 *pb = nullptr;
   uint32_t *stepDev = nullptr;
+  uint32_t *err = nullptr;  // error bits of the inference kernel (kErrTimeout)
   uint32_t *idx = nullptr;
   uint32_t idxCap = 0, lossCap = 0;
 };
@@ -534,7 +800,7 @@ namespace bvhgb {
 int lr_score_keys(const bvhgb_mlp *m, LrScratch &s, const bvhgb_node *nodes, uint32_t root, const uint32_t *inner,
                   uint32_t numInner, uint32_t *keys, uint32_t *vals, cudaStream_t st) {
   if (numInner == 0) return BVHGB_OK;
-  mlp_forward_kernel<true><<<grid_for(numInner, 256), 256, 0, st>>>(m->pb, s.x, numInner, s.y, inner, keys, vals);
+  mlp_forward_tc_kernel<true><<<tc_grid(numInner), 128, 0, st>>>(m->pb, s.x, numInner, s.y, inner, keys, vals, m->err);
   BVHGB_LAUNCH_CHECK("lr score");
   return BVHGB_OK;
 }
@@ -573,6 +839,8 @@ extern "C" BVHGB_API int bvhgb_mlp_create(uint64_t seed, bvhgb_mlp **out) {
   if (e == cudaSuccess) e = cudaMalloc(&m->v, 4 * kMlpParams);
   if (e == cudaSuccess) e = cudaMalloc(&m->pb, 2 * kMlpParams);
   if (e == cudaSuccess) e = cudaMalloc(&m->stepDev, 4);
+  if (e == cudaSuccess) e = cudaMalloc(&m->err, 4);
+  if (e == cudaSuccess) e = cudaMemset(m->err, 0, 4);
   if (e != cudaSuccess) {
     set_last_error("bvhgb_mlp_create", e);
     bvhgb_mlp_destroy(m);
@@ -608,6 +876,7 @@ extern "C" BVHGB_API int bvhgb_mlp_destroy(bvhgb_mlp *m) {
   cudaFree(m->loss);
   cudaFree(m->pb);
   cudaFree(m->stepDev);
+  cudaFree(m->err);
   cudaFree(m->idx);
   delete m;
   return BVHGB_OK;
@@ -636,8 +905,8 @@ extern "C" BVHGB_API int bvhgb_mlp_forward(const bvhgb_mlp *m, const uint16_t *x
                                            bvhgb_stream stream) {
   if (!m || (n && (!x || !y))) return BVHGB_INVALID_ARGUMENT;
   if (n == 0) return BVHGB_OK;
-  mlp_forward_kernel<false><<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(m->pb, x, n, y, nullptr, nullptr,
-                                                                            nullptr);
+  mlp_forward_tc_kernel<false><<<tc_grid(n), 128, 0, as_stream(stream)>>>(m->pb, x, n, y, nullptr, nullptr, nullptr,
+                                                                         m->err);
   BVHGB_LAUNCH_CHECK("mlp forward");
   return BVHGB_OK;
 }
@@ -744,5 +1013,12 @@ extern "C" BVHGB_API int bvhgb_lr_features(bvhgb_lr_features_ctx *ctx, const bvh
   const int st = lr_features(ctx->s, nodes, numNodes, root, inner, numInner, lr_inv_log2_leaves(numLeaves), s);
   if (st) return st;
   if (numInner) BVHGB_CUDA_TRY(cudaMemcpyAsync(x, ctx->s.x, 2ull * kIn * numInner, cudaMemcpyDeviceToDevice, s));
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_mlp_read_errors(bvhgb_mlp *m, uint32_t *flags, int reset) {
+  if (!m || !flags) return BVHGB_INVALID_ARGUMENT;
+  BVHGB_CUDA_TRY(cudaMemcpy(flags, m->err, 4, cudaMemcpyDeviceToHost));
+  if (reset) BVHGB_CUDA_TRY(cudaMemset(m->err, 0, 4));
   return BVHGB_OK;
 }

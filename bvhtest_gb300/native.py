@@ -131,6 +131,7 @@ PROTOS = {
     "bvhgb_mlp_set_params": (I32, [VP, VP]),
     "bvhgb_mlp_get_params": (I32, [VP, VP]),
     "bvhgb_mlp_forward": (I32, [VP, VP, U32, VP, VP]),
+    "bvhgb_mlp_read_errors": (I32, [VP, C.POINTER(U32), I32]),
     "bvhgb_mlp_gradient": (I32, [VP, VP, VP, U32, VP, VP, VP]),
     "bvhgb_mlp_train": (I32, [VP, VP, VP, U32, U32, U32, F32, F32, U64, VP, VP]),
     "bvhgb_lr_features_create": (I32, [U32, C.POINTER(VP)]),

@@ -263,8 +263,11 @@ BVHGB_API int bvhgb_mlp_destroy(bvhgb_mlp *m);
 /* Host FP32 arrays of BVHGB_MLP_PARAMS values; set also resets the AdamW state and step. */
 BVHGB_API int bvhgb_mlp_set_params(bvhgb_mlp *m, const float *params);
 BVHGB_API int bvhgb_mlp_get_params(const bvhgb_mlp *m, float *params);
-/* y[i] = MLP(x[i]) for n device rows of BVHGB_LR_FEATURES BF16 values (raw uint16 bit patterns). */
+/* y[i] = MLP(x[i]) for n device rows of BVHGB_LR_FEATURES BF16 values (raw uint16 bit patterns), on
+ * the tcgen05 tensor cores (128-row tiles, FP32 accumulators in tensor memory). */
 BVHGB_API int bvhgb_mlp_forward(const bvhgb_mlp *m, const uint16_t *x, uint32_t n, float *y, bvhgb_stream stream);
+/* Error bits of the inference kernel (1 = a bounded wait gave up: results not valid); synchronous. */
+BVHGB_API int bvhgb_mlp_read_errors(bvhgb_mlp *m, uint32_t *flags, int reset);
 /* Gradient of the mean squared error over n device samples (x, target t) without an update:
  * gradHost receives BVHGB_MLP_PARAMS floats, lossHost the loss (either may be NULL). Synchronous.
  * The BF16 rounding of weights and activations is passed through as identity. */
