@@ -58,47 +58,6 @@ __device__ __forceinline__ void load_weights(const __nv_bfloat16 *__restrict__ w
   for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) W[i] = __bfloat162float(w[i]);
 }
 
-// One sample through the network with weights W (FP32 copies of the BF16 values) in shared memory.
-__device__ __forceinline__ float mlp_eval(const float *W, const float in[kIn]) {
-  float a1[kH];  // fully unrolled so that it stays in registers
-#pragma unroll
-  for (int j = 0; j < kH; ++j) {
-    float z = W[oB1 + j];
-#pragma unroll
-    for (int k = 0; k < kIn; ++k) z += W[oW1 + j * kIn + k] * in[k];
-    a1[j] = bf16r(gelu(z));
-  }
-  float out = W[oB3];
-  for (int j = 0; j < kH; ++j) {
-    float z = W[oB2 + j];
-#pragma unroll
-    for (int i = 0; i < kH; ++i) z += W[oW2 + j * kH + i] * a1[i];
-    out += W[oW3 + j] * bf16r(gelu(z));
-  }
-  return out;
-}
-
-// Inference; with KEYS the selection keys of the optimizer are written as well.
-template <bool KEYS>
-__global__ void __launch_bounds__(256) mlp_forward_kernel(const __nv_bfloat16 *__restrict__ w,
-                                                          const uint16_t *__restrict__ x, uint32_t n,
-                                                          float *__restrict__ y, const uint32_t *__restrict__ inner,
-                                                          uint32_t *__restrict__ keys, uint32_t *__restrict__ vals) {
-  __shared__ float W[kWPad];
-  load_weights(w, W);
-  __syncthreads();
-  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
-    float in[kIn];
-    load_row(x, s, in);
-    const float out = mlp_eval(W, in);
-    y[s] = out;
-    if (KEYS) {
-      keys[s] = ~f2ord(out);
-      vals[s] = __ldg(inner + s);
-    }
-  }
-}
-
 // ---- inference on the 5th-generation tensor cores (tcgen05) ----------------------------------------
 // Persistent CTAs of 4 warps; a tile is 128 rows. Layer 1: D1[128 x 64] = X[128 x 32] * W1^T (the 24
 // features padded to K = 32), layer 2: D2[128 x 64] = A1[128 x 64] * W2^T, both BF16 operands in
