@@ -134,6 +134,14 @@ def radix_sort_pairs(keys: torch.Tensor, vals: torch.Tensor, begin_bit=0, end_bi
     return ko, vo
 
 
+def sort_default_tile(tile_keys: int = 0) -> int:
+    """Sets the onesweep tile (2048, 4096 or 8192 keys per CTA) of the sorts that are not given one
+    (LBVH build, optimizer selection) and returns the previous setting; 0 only reads it."""
+    prev = C.c_uint32()
+    check(load().bvhgb_sort_set_default_tile(int(tile_keys), C.byref(prev)), "bvhgb_sort_set_default_tile")
+    return prev.value
+
+
 def calc_sah(nodes: torch.Tensor, root: int = 0, num_nodes=None, stream=None) -> float:
     out = C.c_double()
     n = nodes.shape[0] if num_nodes is None else num_nodes

@@ -109,6 +109,9 @@ __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t *p) {
   asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(r) : "l"(p) : "memory");
   return r;
 }
+__device__ __forceinline__ void st_relaxed(uint32_t *p, uint32_t v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 
 // Order-preserving float <-> uint32 mapping for atomicMin/atomicMax on floats.
 __device__ __forceinline__ uint32_t f2ord(float f) {

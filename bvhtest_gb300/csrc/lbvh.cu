@@ -10,9 +10,10 @@
 //   sort         : sort.cu (replaces cub::DeviceRadixSort, LBVH_CUDA.cu:185-193).
 //   lbvh_build   : one thread per sorted leaf writes the leaf and climbs (Apetrei 2014 style): at each
 //                  step it picks the parent from the two neighbouring key deltas, meets its sibling
-//                  through one acq_rel exchange on the split slot, and the second thread to arrive
-//                  merges the boxes and writes the parent with the Karras node index the reference
-//                  assigns (kGenLeafNodes + kBuildTree + kFixAABBTree, LBVH_CUDA.cu:273-374).
+//                  at the split, and the second thread to arrive merges the boxes and writes the
+//                  parent with the Karras node index the reference assigns (kGenLeafNodes +
+//                  kBuildTree + kFixAABBTree, LBVH_CUDA.cu:273-374), meeting its sibling through one
+//                  acq_rel exchange on the split's slot.
 #include <cstring>
 
 #include "common.cuh"

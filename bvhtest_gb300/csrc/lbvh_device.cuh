@@ -117,26 +117,19 @@ __device__ __forceinline__ void set_parent(bvhgb_node *nd, uint32_t parent, uint
   nd->isLeft = isLeft;
 }
 
-// One sorted leaf of a tree of n leaves: write the leaf (left = the face's index in its mesh) and
-// climb while this thread is the second to arrive at a node (kGenLeafNodes + kBuildTree +
-// kFixAABBTree, LBVH_CUDA.cu:273-374). keys, nodes and slots are the tree's own arrays.
+// From node [l, r] with box 'box' (right: the node is its parent's left child, so the parent's
+// split is r; otherwise l - 1) climb through the tree's exchange slots: at each split the first
+// thread to arrive leaves its far end in the slot and stops; the second merges the boxes, writes
+// the parent with the Karras node index the reference assigns and goes on (kBuildTree +
+// kFixAABBTree, LBVH_CUDA.cu:273-374). The node [l, r] itself must already be written.
 template <int MODE, typename K>
-__device__ __forceinline__ void lbvh_climb(uint32_t i, uint32_t n, const K *__restrict__ keys, uint32_t face,
-                                           Box box, bvhgb_node *nodes, uint32_t *slots, uint32_t *err) {
-  const uint32_t leafIdx = n - 1 + i;
-  if (n == 1) {
-    store_record(nodes + leafIdx, box, 0u, face, 1u, 1u, 0u, 255u);
-    return;
-  }
-  store_record(nodes + leafIdx, box, kNone, face, 1u, 1u, 0u, 255u);
-
-  uint32_t l = i, r = i;
-  bool right = parent_is_right<MODE, K>(keys, l, r, n);
-  // Each step at least doubles nothing but strictly grows [l, r], so n - 1 steps reach the root;
-  // the bound and the range checks turn corrupted exchange slots into an error, not a hang.
+__device__ __forceinline__ void lbvh_climb_from(uint32_t l, uint32_t r, bool right, Box box, uint32_t n,
+                                                const K *__restrict__ keys, bvhgb_node *nodes, uint32_t *slots,
+                                                uint32_t *err) {
+  // Each step strictly grows [l, r], so n - 1 steps reach the root; the bound and the range checks
+  // turn corrupted exchange slots into an error, not a hang.
   for (uint32_t step = 0;; ++step) {
     const uint32_t split = right ? r : l - 1;
-    // Meet the sibling: the first thread leaves its far end in the slot and stops.
     const uint32_t other = atom_exch_acq_rel(&slots[split], right ? l : r);
     if (other == kNone) return;
     const uint32_t L = right ? l : other, R = right ? other : r;
@@ -164,6 +157,20 @@ __device__ __forceinline__ void lbvh_climb(uint32_t i, uint32_t n, const K *__re
     if (root) return;
     box = pb;
   }
+}
+
+// One sorted leaf of a tree of n leaves: write the leaf (left = the face's index in its mesh) and
+// climb (kGenLeafNodes + the climb above). keys, nodes and slots are the tree's own arrays.
+template <int MODE, typename K>
+__device__ __forceinline__ void lbvh_climb(uint32_t i, uint32_t n, const K *__restrict__ keys, uint32_t face,
+                                           Box box, bvhgb_node *nodes, uint32_t *slots, uint32_t *err) {
+  const uint32_t leafIdx = n - 1 + i;
+  if (n == 1) {
+    store_record(nodes + leafIdx, box, 0u, face, 1u, 1u, 0u, 255u);
+    return;
+  }
+  store_record(nodes + leafIdx, box, kNone, face, 1u, 1u, 0u, 255u);
+  lbvh_climb_from<MODE, K>(i, i, parent_is_right<MODE, K>(keys, i, i, n), box, n, keys, nodes, slots, err);
 }
 
 }  // namespace

@@ -9,9 +9,14 @@
 //      holding the same digit are found with 9 ballots and a warp-private counter per digit is
 //      advanced by one shared-memory atomic of the lowest such lane; the atomics of all items are
 //      issued before any result is used), publishes per-digit counts, resolves its exclusive prefix
-//      by decoupled look-back (four predecessors per round trip, bounded spin), stages the tile in
+//      by decoupled look-back (kLook predecessors per round trip, bounded spin), stages the tile in
 //      shared memory in digit order and writes it out in runs, so each digit's run is a contiguous
 //      store.
+// A status word holds a flag and a count together and nothing else is read through it, so it is
+// published and polled with relaxed gpu-scope accesses (no fences); the next pass reads the keys
+// this pass wrote only after the kernel boundary.
+#include <atomic>
+
 #include "common.cuh"
 #include "sort.cuh"
 
@@ -27,6 +32,9 @@ constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagInc = 2u << 30;
 constexpr uint32_t kFlagMask = 3u << 30;
 constexpr uint32_t kValMask = (1u << 30) - 1u;
+// Predecessors read per look-back round trip. The tiles of a wave start together, so a tile k
+// places behind the last finished one needs about k / kLook round trips.
+constexpr int kLook = 16;
 
 // The last digit may be narrower than 8 bits when (endBit - beginBit) is not a multiple of 8.
 __host__ __device__ __forceinline__ uint32_t digit_mask(uint32_t shift, uint32_t endBit) {
@@ -106,7 +114,7 @@ struct OnesweepSmem {
 };
 
 template <typename K, int THREADS, int ITEMS>
-__global__ void __launch_bounds__(THREADS, 1) onesweep_kernel(const K *__restrict__ keysIn, K *__restrict__ keysOut,
+__global__ void __launch_bounds__(THREADS, THREADS <= 256 ? 2 : 1) onesweep_kernel(const K *__restrict__ keysIn, K *__restrict__ keysOut,
                                                             const uint32_t *__restrict__ valsIn,
                                                             uint32_t *__restrict__ valsOut, uint32_t n,
                                                             uint32_t shift, uint32_t mask,
@@ -181,7 +189,7 @@ __global__ void __launch_bounds__(THREADS, 1) onesweep_kernel(const K *__restric
       count += c;
     }
     uint32_t *st = status + (size_t)tile * kRadix + d;
-    st_release(st, (tile == 0 ? kFlagInc : kFlagAgg) | count);
+    st_relaxed(st, (tile == 0 ? kFlagInc : kFlagAgg) | count);
     incl = count;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -194,11 +202,11 @@ __global__ void __launch_bounds__(THREADS, 1) onesweep_kernel(const K *__restric
       int64_t pred = (int64_t)tile - 1;
       bool done = false;
       while (!done) {
-        uint32_t v[4];
+        uint32_t v[kLook];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) v[q] = pred - q >= 0 ? ld_acquire(status + (size_t)(pred - q) * kRadix + d) : kFlagInc;
+        for (int q = 0; q < kLook; ++q) v[q] = pred - q >= 0 ? ld_relaxed(status + (size_t)(pred - q) * kRadix + d) : kFlagInc;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < kLook; ++q) {
           if (done) break;
           if (pred - q < 0) {
             done = true;
@@ -212,7 +220,7 @@ __global__ void __launch_bounds__(THREADS, 1) onesweep_kernel(const K *__restric
               break;
             }
             __nanosleep(32);
-            v[q] = ld_acquire(ps);
+            v[q] = ld_relaxed(ps);
           }
           if ((v[q] & kFlagMask) == 0u) {
             done = true;
@@ -221,9 +229,9 @@ __global__ void __launch_bounds__(THREADS, 1) onesweep_kernel(const K *__restric
           excl += v[q] & kValMask;
           if (v[q] & kFlagInc) done = true;
         }
-        pred -= 4;
+        pred -= kLook;
       }
-      st_release(st, kFlagInc | (excl + count));
+      st_relaxed(st, kFlagInc | (excl + count));
     }
     sm.globalBase[d] = offsets[d] + excl;
   }
@@ -276,9 +284,12 @@ int onesweep_passes(const Layout &L, const K *keysIn, K *keysOut, const uint32_t
   return BVHGB_OK;
 }
 
+std::atomic<uint32_t> g_default_tile{kSortTileDefault};
+
 template <typename K>
 int sort_impl(void *temp, uint32_t tileKeys, const K *keysIn, K *keysOut, const uint32_t *valsIn, uint32_t *valsOut,
               uint32_t n, uint32_t beginBit, uint32_t endBit, cudaStream_t s) {
+  if (tileKeys == 0) tileKeys = g_default_tile.load(std::memory_order_relaxed);
   const Layout L = make_layout(n, sizeof(K), beginBit, endBit, tileKeys);
   const Layout Lmax = make_layout(n, sizeof(K), beginBit, endBit, kMinTile);  // the temp space's layout
   char *t = static_cast<char *>(temp);
@@ -339,6 +350,8 @@ int sort_prepare() {
   return BVHGB_OK;
 }
 
+bool sort_tile_valid(uint32_t tileKeys) { return tileKeys == 2048 || tileKeys == 4096 || tileKeys == 8192; }
+
 size_t sort_temp_bytes(uint32_t n, uint32_t keyBytes, uint32_t beginBit, uint32_t endBit) {
   return make_layout(n, keyBytes, beginBit, endBit).total;
 }
@@ -374,4 +387,11 @@ extern "C" BVHGB_API int bvhgb_radix_sort_pairs(void *temp, size_t *tempBytes, c
   if (*tempBytes < need || (n && (!keysIn || !keysOut || !valsIn || !valsOut))) return BVHGB_INVALID_ARGUMENT;
   return bvhgb::sort_pairs(temp, keysIn, keysOut, valsIn, valsOut, n, keyBytes, beginBit, endBit,
                            bvhgb::as_stream(stream));
+}
+
+extern "C" BVHGB_API int bvhgb_sort_set_default_tile(uint32_t tileKeys, uint32_t *previous) {
+  if (tileKeys != 0 && !bvhgb::sort_tile_valid(tileKeys)) return BVHGB_INVALID_ARGUMENT;
+  const uint32_t old = tileKeys ? bvhgb::g_default_tile.exchange(tileKeys) : bvhgb::g_default_tile.load();
+  if (previous) *previous = old;
+  return BVHGB_OK;
 }

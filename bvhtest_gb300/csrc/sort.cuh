@@ -13,9 +13,10 @@ size_t sort_temp_bytes(uint32_t n, uint32_t keyBytes, uint32_t beginBit, uint32_
 // Device word that the look-back sets to a non-zero error bit if a bounded wait gives up.
 uint32_t *sort_error_word(void *temp, uint32_t n, uint32_t keyBytes, uint32_t beginBit, uint32_t endBit);
 // Stable ascending sort; temp must hold sort_temp_bytes(...) bytes. tileKeys = keys per CTA of the
-// onesweep passes (2048, 4096 or 8192; the result does not depend on it).
+// onesweep passes (2048, 4096 or 8192; the result does not depend on it); 0 takes the process-wide
+// default (kSortTileDefault unless bvhgb_sort_set_default_tile changed it).
 constexpr uint32_t kSortTileDefault = 8192;
+bool sort_tile_valid(uint32_t tileKeys);
 int sort_pairs(void *temp, const void *keysIn, void *keysOut, const uint32_t *valsIn, uint32_t *valsOut, uint32_t n,
-               uint32_t keyBytes, uint32_t beginBit, uint32_t endBit, cudaStream_t s,
-               uint32_t tileKeys = kSortTileDefault);
+               uint32_t keyBytes, uint32_t beginBit, uint32_t endBit, cudaStream_t s, uint32_t tileKeys = 0);
 }  // namespace bvhgb

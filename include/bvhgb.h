@@ -179,6 +179,12 @@ BVHGB_API int bvhgb_radix_sort_pairs(void *temp, size_t *tempBytes, const void *
                                      const uint32_t *valsIn, uint32_t *valsOut, uint32_t n, uint32_t keyBytes,
                                      uint32_t beginBit, uint32_t endBit, bvhgb_stream stream);
 
+/* Keys per CTA of the onesweep passes (2048, 4096 or 8192) for sorts that are not given one: the
+ * LBVH build's and the optimizer's selection sort, launched (or captured into a graph) after the
+ * call. tileKeys = 0 only reads the setting. *previous (may be NULL) receives the old value. The
+ * results do not depend on it. No counterpart in the reference (cub picks its own tiles). */
+BVHGB_API int bvhgb_sort_set_default_tile(uint32_t tileKeys, uint32_t *previous);
+
 /* ---- SAH (Bittner13CUDA.cu:776-803, BVH.cpp:23-37) ------------------------------------------- */
 
 /* (sum of all node areas except the root) / root area, cInner = cLeaf = 1; deterministic

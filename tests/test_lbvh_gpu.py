@@ -153,3 +153,26 @@ def test_radix_sort_bit_range(gpu):
     digit = (keys >> 8) & ((1 << 12) - 1)
     order = np.argsort(digit, kind="stable")
     assert np.array_equal(vo.cpu().numpy(), order)
+
+
+@pytest.mark.parametrize("tile", [2048, 4096, 8192])
+def test_sort_default_tile_gives_the_same_order(gpu, tile):
+    import torch
+    g = np.random.default_rng(tile)
+    n = 1000003
+    keys = g.integers(0, 1 << 63, n, dtype=np.uint64)
+    keys[::3] = keys[7]  # runs of equal keys keep their input order
+    kt = torch.from_numpy(keys.view(np.int64)).cuda()
+    vt = torch.arange(n, dtype=torch.int32, device="cuda")
+    prev = gpu.sort_default_tile(tile)
+    try:
+        assert gpu.sort_default_tile(0) == tile
+        ko, vo = gpu.radix_sort_pairs(kt, vt)
+        torch.cuda.synchronize()
+    finally:
+        gpu.sort_default_tile(prev)
+    order = np.argsort(keys, kind="stable")
+    assert np.array_equal(vo.cpu().numpy().view(np.uint32), order.astype(np.uint32))
+    assert np.array_equal(ko.cpu().numpy().view(np.uint64), keys[order])
+    with pytest.raises(gpu.BvhgbError):
+        gpu.sort_default_tile(1000)
