@@ -364,9 +364,13 @@ def run_ours(args, w, rank, world, local):
         "clocks": clocks,
         "plain": plain,
     }
+    scorer = None
+    if not args.no_learned or not args.no_stress:
+        from bvhtest_gb300 import learned
+        scorer, train = learned.train_family("large")
     if not args.no_learned:
         big = learned_large(args, w, dev, flush, stream, vert, faces, nodes, lbvh, sah, lib, ev, vh, fh, nh, vd, fd,
-                            per_launch_ms * max(1, search_launches))
+                            per_launch_ms * max(1, search_launches), scorer, train)
         line["learned"] = big
         if "build_optimize_ms" in big:
             # the headline: build + optimisation to the SAH of the configured plain run (equal SAH)
@@ -386,7 +390,142 @@ def run_ours(args, w, rank, world, local):
         line["learned_vs_plain"] = learned_arm(args, dev, flush, stream)
     if not args.no_batch:
         line["batched"] = batch_arm(args, dev, flush)
+    if not args.no_stress:
+        line["stress"] = stress_arm(args, dev, flush, scorer)
     print(json.dumps(line), flush=True)
+
+
+def stress_arm(args, dev, flush, scorer):
+    """Combined stress test: 33,554,432 triangles (512 randomly rotated boxes, 52 x 52 quads per face,
+    and a 256-component Gaussian mixture), 63-bit Morton, karras LBVH; 300 plain Bittner13
+    iterations set the target, the learned policy (scorer of the large-scene family, alternating with
+    the plain measure) runs until its SAH is within 0.5% of it; then 16,777,216 incoherent rays in 16
+    batches of 64k to 4M (origins uniform in the scene box, directions uniform on the sphere,
+    tmax = inf). The plain run is timed once (per-iteration events, no host synchronisation), the
+    learned run W + K times."""
+    import torch
+    from bvhtest_gb300 import api, native, scenes
+
+    lib = native.load()
+    vert_h, faces_h = scenes.stress_scene()
+    n = int(faces_h.shape[0])
+    n_nodes = 2 * n - 1
+    v = torch.from_numpy(vert_h).to(dev)
+    f = torch.from_numpy(faces_h.view(np.int32)).to(dev)
+    nodes = api.empty_nodes(n_nodes)
+    lbvh = api.LBVH(n, 63, "karras")
+    rebuild = lambda: lbvh.build(v, f, nodes)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    plain_iters = 300
+
+    def events_run(opt, iters):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        marks = [ev()]
+        marks[0].record()
+        rebuild()
+        m = ev()
+        m.record()
+        marks.append(m)
+        opt.iteration = 0
+        for _ in range(iters):
+            opt.run(1)
+            m = ev()
+            m.record()
+            marks.append(m)
+        torch.cuda.synchronize()
+        return [marks[0].elapsed_time(x) for x in marks[1:]]  # build, then after each iteration
+
+    # warm-up of every kernel, then the untimed calibration: the SAH after each plain iteration
+    rebuild()
+    popt = api.Bittner13GPU(nodes, num_nodes=n_nodes)
+    popt.run(3)
+    rebuild()
+    popt.iteration = 0
+    trace = []
+    for _ in range(plain_iters):
+        popt.run(1)
+        trace.append(api.calc_sah(nodes))
+    target = 1.005 * trace[-1]
+    kp = next(i + 1 for i, x in enumerate(trace) if x <= target)
+    pt = events_run(popt, plain_iters)
+    plain_sah = api.calc_sah(nodes)
+    pst = popt.stats()
+    popt.close()
+    # learned selection until the target
+    lopt = api.Bittner13GPU(rebuild(), num_nodes=n_nodes)
+    lopt.set_scorer(scorer, 2)
+    lopt.iteration = 0
+    k = None
+    for it in range(1, plain_iters + 1):
+        lopt.run(1)
+        if api.calc_sah(nodes) <= target:
+            k = it
+            break
+    out = {
+        "workload": ("33,554,432 triangles: 512 randomly rotated boxes (centres uniform in [0,10]^3, half extents "
+                     "uniform in [0.1,0.6]) with 52 x 52 quads per face (16,613,376 triangles) and a 256-component "
+                     "Gaussian mixture (16,941,056); 63-bit Morton, karras LBVH; learned Bittner13 until within 0.5% "
+                     "of the SAH of 300 plain iterations; 16,777,216 incoherent rays in 16 batches of 64k..4M"),
+        "triangles": n, "nodes": n_nodes,
+        "build_ms": round(pt[0], 3),
+        "build_hbm_gbs": round(n * 612.0 / (pt[0] * 1e-3) / 1e9, 1),
+        "plain": {"iterations": plain_iters, "build_optimize_ms": round(pt[-1], 3), "sah": round(plain_sah, 4),
+                  "sah_trace_300": round(trace[-1], 4), "first_within_0.5pct_iterations": kp,
+                  "first_within_0.5pct_build_optimize_ms": round(pt[kp], 3),
+                  "applied": pst["applied"], "skipped_conflict": pst["skippedConflict"]},
+        "sah_target": round(target, 4),
+    }
+    if k is None:
+        out["error"] = "learned selection did not come within 0.5% of the plain SAH in 300 iterations"
+    else:
+        times = []
+        c0 = lib.bvhgb_launch_count()
+        for i in range(1 + args.steps):
+            if i == 1:
+                c0 = lib.bvhgb_launch_count()
+            t = events_run(lopt, k)
+            if i >= 1:
+                times.append(t)
+        launches = (lib.bvhgb_launch_count() - c0) // args.steps
+        lb = statistics.mean(t[0] for t in times)
+        lt = statistics.mean(t[-1] for t in times)
+        out["learned"] = {"iterations": k, "build_optimize_ms": round(lt, 3), "build_ms": round(lb, 3),
+                          "sah": round(api.calc_sah(nodes), 4), "gpu_launches": int(launches),
+                          "policy": "scorer iterations alternating with plain ones (plainEvery 2)"}
+        out["wall_time_ratio_vs_plain_300"] = round(lt / pt[-1], 4)
+        out["wall_time_ratio_vs_plain_first_within_0.5pct"] = round(lt / pt[kp], 4)
+    lopt.close()
+    # incoherent rays in 16 batches through the optimised tree
+    lo, hi = vert_h.min(0), vert_h.max(0)
+    del vert_h, faces_h
+    org_h, dir_h, sizes = scenes.stress_rays(lo, hi)
+    org = torch.from_numpy(org_h).to(dev)
+    dirs = torch.from_numpy(dir_h).to(dev)
+    api.trace_rays(nodes, v, f, org[:65536], dirs[:65536], num_nodes=n_nodes)  # warm-up
+    flush.fill_(1)
+    torch.cuda.synchronize()
+    marks = [ev()]
+    marks[0].record()
+    hits, off = [], 0
+    for sz in sizes:
+        hits.append(api.trace_rays(nodes, v, f, org[off:off + sz], dirs[off:off + sz], num_nodes=n_nodes))
+        off += sz
+        m = ev()
+        m.record()
+        marks.append(m)
+    torch.cuda.synchronize()
+    per = [marks[i].elapsed_time(marks[i + 1]) for i in range(len(sizes))]
+    total = sum(per)
+    h = api.hits_to_numpy(torch.cat(hits))
+    out["trace"] = {"rays": int(sum(sizes)), "batches": list(sizes), "ms": round(total, 3),
+                    "mrays_per_s": round(sum(sizes) / (total * 1e-3) / 1e6, 1),
+                    "batch_mrays_per_s": [round(sz / (t * 1e-3) / 1e6, 1) for sz, t in zip(sizes, per)],
+                    "hit_fraction": round(float((h["prim"] != 0xFFFFFFFF).mean()), 4),
+                    "errors": api.trace_errors()}
+    out["lbvh_errors"] = lbvh.errors()
+    lbvh.close()
+    return out
 
 
 def batch_arm(args, dev, flush):
@@ -460,7 +599,7 @@ def first_hit(opt, nodes, target, max_iters, rebuild):
 
 
 def learned_large(args, w, dev, flush, stream, vert, faces, nodes, lbvh, target, lib, ev, vh, fh, nh, vd, fd,
-                  search_ms_per_iteration):
+                  search_ms_per_iteration, scorer, train):
     """Learned selection (alternating with the plain measure) on the benchmark scene until the SAH of
     the configured plain run is reached; the plain optimizer's first hit of the same SAH beside it."""
     import torch
@@ -468,8 +607,6 @@ def learned_large(args, w, dev, flush, stream, vert, faces, nodes, lbvh, target,
 
     n = int(w["faces"].shape[0])
     n_nodes = 2 * n - 1
-    from bvhtest_gb300 import learned
-    scorer, train = learned.train_family("large")
     rebuild = lambda: lbvh.build(vert, faces, nodes)
     lopt = api.Bittner13GPU(rebuild(), num_nodes=n_nodes)
     lopt.set_scorer(scorer, 2)
@@ -681,6 +818,13 @@ def run_phase(args, w):
     from bvhtest_gb300 import api
     if args.only == "batch":
         return run_batch_phase(args)
+    if args.only == "stress":
+        import torch
+        from bvhtest_gb300 import api, learned
+        scorer = api.Mlp.load(args.scorer) if args.scorer else learned.train_family("large")[0]
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        print(json.dumps(stress_arm(args, torch.device("cuda"), flush, scorer)), flush=True)
+        return
     n = int(w["faces"].shape[0])
     vert = torch.from_numpy(w["vert"]).cuda()
     faces = torch.from_numpy(w["faces"].view(np.int32)).cuda()
@@ -726,11 +870,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-scorer comparison")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched multi-mesh build")
+    ap.add_argument("--no-stress", action="store_true", help="skip the 33.5M-triangle combined stress test")
     ap.add_argument("--batch-topology", choices=["refCompat", "karras"], default="refCompat",
                     help="with --only batch: the LBVH topology of the batched meshes")
-    ap.add_argument("--only", choices=["build", "optimize", "trace", "batch"], default=None,
+    ap.add_argument("--only", choices=["build", "optimize", "trace", "batch", "stress"], default=None,
                     help="repeat one phase only and print its time (profiling runs; no benchmark record)")
-    ap.add_argument("--scorer", default=None, help="with --only optimize: learned selection with these weights")
+    ap.add_argument("--scorer", default=None,
+                    help="with --only optimize / stress: learned selection with these weights")
     ap.add_argument("--plain-every", type=int, default=2, help="with --scorer: every k-th iteration is plain")
     args = ap.parse_args()
     if args.warmup < 3:

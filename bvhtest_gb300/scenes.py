@@ -103,3 +103,80 @@ def batch_meshes(count: int = 256, lo: int = 1024, hi: int = 524288, seed: int =
         faces.append((np.arange(3 * n, dtype=np.uint32).reshape(n, 3) + base).astype(np.uint32))
         base += 3 * n
     return np.concatenate(verts), np.concatenate(faces), counts.astype(np.uint32)
+
+
+def _cube_faces(cells: int) -> np.ndarray:
+    """The six faces of the cube [-1, 1]^3, each cells x cells quads split into two triangles,
+    as [6 * cells^2 * 2, 3, 3] float64 vertices (outward winding is not relied on)."""
+    t = np.linspace(-1.0, 1.0, cells + 1)
+    u0, v0 = np.meshgrid(t[:-1], t[:-1], indexing="ij")
+    u1, v1 = np.meshgrid(t[1:], t[1:], indexing="ij")
+    u0, v0, u1, v1 = (a.reshape(-1) for a in (u0, v0, u1, v1))
+    quads = []
+    for axis in range(3):
+        a, b = [k for k in range(3) if k != axis]
+        for side in (-1.0, 1.0):
+            def pt(u, v):
+                p = np.empty((u.shape[0], 3))
+                p[:, axis] = side
+                p[:, a] = u
+                p[:, b] = v
+                return p
+            p00, p10, p11, p01 = pt(u0, v0), pt(u1, v0), pt(u1, v1), pt(u0, v1)
+            quads.append(np.stack([p00, p10, p11], 1))
+            quads.append(np.stack([p00, p11, p01], 1))
+    return np.concatenate(quads, 0)
+
+
+def _random_rotations(g: np.random.Generator, k: int) -> np.ndarray:
+    """k rotation matrices from uniformly distributed unit quaternions."""
+    q = g.normal(0.0, 1.0, (k, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    w, x, y, z = q.T
+    return np.stack([
+        np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)], -1),
+        np.stack([2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)], -1),
+        np.stack([2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], -1)], 1)
+
+
+def box_soup(boxes: int = 512, cells: int = 52, seed: int = 5, extent: float = 10.0,
+             half_lo: float = 0.1, half_hi: float = 0.6):
+    """boxes randomly rotated boxes, centres uniform in [0, extent]^3, half extents uniform in
+    [half_lo, half_hi] per axis; every face tessellated into cells x cells quads of two triangles
+    (512 boxes x 6 faces x 52^2 x 2 = 16,613,376 triangles by default). Returns [n, 3, 3] float32."""
+    g = _rng(seed)
+    unit = _cube_faces(cells)                       # [T, 3, 3]
+    centre = g.random((boxes, 3)) * extent
+    half = g.uniform(half_lo, half_hi, (boxes, 3))
+    rot = _random_rotations(g, boxes)
+    out = np.empty((boxes, unit.shape[0], 3, 3), np.float32)
+    step = 32
+    for b0 in range(0, boxes, step):  # scale the cube, then rotate and move it (32 boxes at a time)
+        b1 = min(boxes, b0 + step)
+        local = unit[None] * half[b0:b1, None, None, :]
+        out[b0:b1] = np.einsum("btvk,bjk->btvj", local, rot[b0:b1]) + centre[b0:b1, None, None, :]
+    return out.reshape(-1, 3, 3)
+
+
+def stress_scene(n: int = 33554432, boxes: int = 512, cells: int = 52, clusters: int = 256, seed: int = 5):
+    """Combined stress scene: the rotated, tessellated boxes of box_soup (16,613,376 triangles)
+    and a clusters-component Gaussian mixture (means uniform in [0,10]^3, sigma log-uniform in
+    [0.05, 0.8], per-vertex offsets N(0, 0.01^2)) filling the rest: 33,554,432 triangles."""
+    bx = box_soup(boxes, cells, seed)
+    rest = n - bx.shape[0]
+    if rest < 0:
+        raise ValueError("the boxes alone exceed n")
+    g_vert, _ = gmm_soup(rest, clusters, seed + 1)
+    return _soup(np.concatenate([g_vert.reshape(-1, 3, 3), bx], 0))
+
+
+# 16 ray batches of the stress test, in units of 65,536 rays: 64k up to 4M, 16,777,216 in total.
+STRESS_RAY_BATCHES = (1, 2, 3, 4, 5, 6, 8, 10, 12, 14, 16, 20, 24, 32, 35, 64)
+
+
+def stress_rays(lo, hi, seed: int = 7):
+    """The stress test's incoherent rays: origins uniform in the scene box [lo, hi], directions
+    uniform on the sphere, cut into the STRESS_RAY_BATCHES sizes. Returns (org, dir, sizes)."""
+    sizes = [65536 * m for m in STRESS_RAY_BATCHES]
+    org, d = random_rays(sum(sizes), lo, hi, seed)
+    return org, d, sizes
