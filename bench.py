@@ -45,6 +45,14 @@ def workload(name: str):
                     desc=("large single scene: 4,194,304 triangles (64-component Gaussian mixture + 724x724 "
                           "ground grid), 63-bit Morton, karras LBVH, 200 Bittner13 iterations at 1% (32 chunks), "
                           "1920x1080 primary rays + 1 cosine-weighted bounce per hit"))
+    if name == "stress":
+        vert, faces = scenes.stress_scene()
+        return dict(name="stress", vert=vert, faces=faces, bits=63, topo="karras", iters=300,
+                    camera=dict(pos=(5.0, 16.0, 5.0), lookAt=(5.0, 0.0, 5.0), up=(0.0, 0.0, 1.0), fov=60.0,
+                                width=1920, height=1080),
+                    desc=("combined stress scene: 33,554,432 triangles (512 rotated boxes, 52x52 quads per face, "
+                          "+ 256-component Gaussian mixture), 63-bit Morton, karras LBVH, 300 Bittner13 "
+                          "iterations at 1%"))
     vert, faces = scenes.uniform_soup(65536, seed=1)
     return dict(name="small", vert=vert, faces=faces, bits=30, topo="refCompat", iters=100,
                 camera=scenes.camera_default(),
@@ -862,7 +870,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["large", "small"], default="large")
+    ap.add_argument("--workload", choices=["large", "small", "stress"], default="large",
+                    help="the benchmark scene (large); small and stress serve the --only profiling runs")
     ap.add_argument("--iters", type=int, default=None,
                     help="override the Bittner13 iteration count (profiling runs only; the headline uses the default)")
     ap.add_argument("--no-kernel-events", action="store_true",

@@ -119,6 +119,29 @@ struct Patch {
     NodeP p = get(n.parent);
     return n.isLeft == 0 ? p.left : p.right;
   }
+  // get_subset(x) and get_aabb(x) given the tree's 48-byte record of x (a, m, c: its three float4).
+  __device__ void subset_aabb_from(uint32_t x, const float4 &a, const float4 &m, const float4 &c, NodeP &n,
+                                   Box &b) const {
+    const uint32_t i = index_subset(x);
+    if (i != kNone) {
+      n = nd[i];
+    } else {
+      n.parent = __float_as_uint(m.z);
+      n.left = __float_as_uint(m.w);
+      n.right = __float_as_uint(c.x);
+      const uint32_t fl = __float_as_uint(c.y);
+      n.isLeafFlag = (uint16_t)(fl & 0xFFFFu);
+      n.isLeft = (uint16_t)(fl >> 16);
+    }
+    for (int k = 0; k < 4; ++k) {
+      if (apath[k] == x) {
+        b = abox[k];
+        return;
+      }
+    }
+    b.mn[0] = a.x; b.mn[1] = a.y; b.mn[2] = a.z;
+    b.mx[0] = a.w; b.mx[1] = m.x; b.mx[2] = m.y;
+  }
   __device__ Box get_aabb(uint32_t x) const {
     for (int i = 0; i < 4; ++i)
       if (apath[i] == x) return abox[i];
@@ -380,8 +403,9 @@ __device__ uint32_t find_node_batched(const Patch &p, uint32_t n, SearchCounters
     NodeP cn;
     float total = kInf, induced = kInf;
     if (cand) {
-      cn = p.get_subset(fn[0]);
-      Box b = p.get_aabb(fn[0]);
+      Box b;
+      const float4 *q = reinterpret_cast<const float4 *>(p.t + p.chk(fn[0]));
+      p.subset_aabb_from(fn[0], __ldg(q), __ldg(q + 1), __ldg(q + 2), cn, b);
       induced = fmul(-1.0f, surface_area(b));
       merge_into(b, nbox);
       total = fadd(fc[0], surface_area(b));
@@ -391,7 +415,7 @@ __device__ uint32_t find_node_batched(const Patch &p, uint32_t n, SearchCounters
     const uint32_t key = cand ? f2ord(total) : 0xFFFFFFFFu;
     const uint32_t kmin = __reduce_min_sync(kFull, key);
     const uint32_t first = __ffs(__ballot_sync(kFull, cand && key == kmin)) - 1;
-    const float rbest = __shfl_sync(kFull, total, first);
+    const float rbest = ord2f(kmin);
     const uint32_t rnode = __shfl_sync(kFull, fn[0], first);
     if (rbest < best_cost) {
       best_cost = rbest;
@@ -416,24 +440,50 @@ __device__ uint32_t find_node_batched(const Patch &p, uint32_t n, SearchCounters
       fn[kFrontier - 1] = kNone;
       fsize = rest;
     } else if (m <= 32) {
-      // Common case: gather the children into one slot (lane j takes child j), sort it
-      // descending and merge it with the remaining frontier; at most 128 entries, no overflow.
-      const uint32_t src = lane < m ? __fns(kmask, 0, (lane >> 1) + 1) : lane;
-      const float sc = __shfl_sync(kFull, induced, src);
-      const uint32_t sl = __shfl_sync(kFull, cn.left, src), sr = __shfl_sync(kFull, cn.right, src);
-      const float cj = lane < m ? sc : kInf;
-      const uint32_t nj = lane < m ? ((lane & 1) ? sr : sl) : kNone;
-      // Descending order of the children by rank: child j's rank is the number of children below
-      // it in (cost, node) order (keys are distinct: a node enters the frontier once), and it goes
-      // to lane 31 - rank; the unused lanes fill lanes 0 .. 31 - m with the empty entry. The same
-      // order the bitonic sort gives, with m independent broadcasts instead of 15 dependent stages.
-      uint32_t rank = 0;
-      for (uint32_t i = 0; i < m; ++i) {
-        const float ci = __shfl_sync(kFull, cj, i);
-        const uint32_t ni = __shfl_sync(kFull, nj, i);
-        rank += (ci < cj || (ci == cj && ni < nj)) ? 1u : 0u;
-      }
+      // Common case: gather the children into one slot (lane j takes child j), sort it and merge
+      // it with the remaining frontier; at most 128 entries, no overflow. The k-th lane with
+      // children (in lane order) writes children 2k and 2k + 1 to the warp's buffer; every lane
+      // then reads its own child and, for its rank, all m of them as broadcasts, four at a time.
+      // Child j's rank is the number of children below it in (cost, node) order (keys are
+      // distinct: a node enters the frontier once).
       uint2 *buf = rank_buffer();
+      if (kids) {
+        const uint32_t k = __popc(kmask & ((1u << lane) - 1u));
+        buf[2 * k] = make_uint2(__float_as_uint(induced), cn.left);
+        buf[2 * k + 1] = make_uint2(__float_as_uint(induced), cn.right);
+      }
+      __syncwarp();
+      const uint2 own = buf[lane];
+      const float cj = lane < m ? __uint_as_float(own.x) : kInf;
+      const uint32_t nj = lane < m ? own.y : kNone;
+      uint32_t rank = 0;
+      for (uint32_t i0 = 0; i0 < m; i0 += 4) {
+#pragma unroll
+        for (uint32_t q = 0; q < 4; ++q) {
+          const uint2 o = buf[(i0 + q) & 31u];
+          const float ci = __uint_as_float(o.x);
+          rank += (i0 + q < m && (ci < cj || (ci == cj && o.y < nj))) ? 1u : 0u;
+        }
+      }
+      __syncwarp();
+      if (rest == 0) {
+        // Nothing else is left in the frontier (the usual case): the children in ascending order
+        // are the new frontier; lanes m .. 31 keep the empty entry.
+        buf[lane < m ? rank : lane] = make_uint2(__float_as_uint(cj), nj);
+        __syncwarp();
+        const uint2 e = buf[lane];
+        __syncwarp();
+        fc[0] = __uint_as_float(e.x);
+        fn[0] = e.y;
+#pragma unroll
+        for (int s = 1; s < kFrontier; ++s) {
+          fc[s] = kInf;
+          fn[s] = kNone;
+        }
+        fsize = m;
+        continue;
+      }
+      // Otherwise descending (lane 31 - rank, the unused lanes fill 0 .. 31 - m) and merged.
       buf[lane < m ? 31u - rank : lane - m] = make_uint2(__float_as_uint(cj), nj);
       __syncwarp();
       const uint2 e = buf[lane];

@@ -494,30 +494,32 @@ __global__ void depth_jump_kernel(uint32_t n, uint32_t root, const uint32_t *__r
     }
   }
 }
-
-// Subtree leaf counts bottom-up: each leaf climbs; at every inner node the second arrival adds the
-// children's counts and continues (acq_rel counters order the counts it reads).
+// Leaf counts bottom-up. A leaf starts a climb with count 1; at each parent the two arrivals add
+// 2^40 + their count to the parent's 64-bit accumulator: the first sees 0 and stops, the second
+// receives the first's count in the same atomic, writes the parent's count and goes on. The count
+// travels in the atomic itself, so no fence or sibling load is needed; the next parent is loaded
+// before the atomic.
 __global__ void leaf_count_kernel(const bvhgb_node *__restrict__ t, uint32_t n, uint32_t root, uint32_t *cnt,
-                                  uint32_t *arrive, uint32_t *err) {
+                                  unsigned long long *acc, uint32_t *err) {
+  constexpr unsigned long long kArrival = 1ull << 40;
   for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
     if (__ldg(&t[x].isLeafFlag) == 0) continue;
     __stcg(cnt + x, 1u);
     if (x == root) continue;
+    uint32_t c = 1;
     uint32_t y = __ldg(&t[x].parent);
     for (uint32_t steps = 0;; ++steps) {
       if (y >= n || steps > n) {
         atomicOr(err, kErrBadIndex);
         break;
       }
-      if (atom_add_acq_rel(arrive + y, 1u) == 0u) break;  // first arrival: the sibling's path continues
-      const uint32_t l = __ldg(&t[y].left), r = __ldg(&t[y].right);
-      if (l >= n || r >= n) {
-        atomicOr(err, kErrBadIndex);
-        break;
-      }
-      __stcg(cnt + y, __ldcg(cnt + l) + __ldcg(cnt + r));
+      const uint32_t next = y == root ? root : __ldg(&t[y].parent);
+      const unsigned long long old = atomicAdd(acc + y, kArrival | c);
+      if (old == 0ull) break;  // first arrival: the sibling's climb continues
+      c += (uint32_t)(old & (kArrival - 1ull));
+      __stcg(cnt + y, c);
       if (y == root) break;
-      y = __ldg(&t[y].parent);
+      y = next;
     }
   }
 }
@@ -672,13 +674,14 @@ int lr_scratch_alloc(LrScratch &s, uint32_t numNodes) {
     if (e == cudaSuccess) e = cudaMalloc(&s.dep[k], 4 * n);
   }
   if (e == cudaSuccess) e = cudaMalloc(&s.leafCount, 4 * n);
-  if (e == cudaSuccess) e = cudaMalloc(&s.arrive, 4 * n + 4);  // last word: error flags
+  if (e == cudaSuccess) e = cudaMalloc(&s.acc, 8 * n);
+  if (e == cudaSuccess) e = cudaMalloc(&s.err, 4);
   if (e == cudaSuccess) e = cudaMalloc(&s.hist, 4ull * kRankBins * 8);
   if (e == cudaSuccess) e = cudaMalloc(&s.raw, 4 * kMlpRaw * ni);
   if (e == cudaSuccess) e = cudaMalloc(&s.src, 16 * ni);
   if (e == cudaSuccess) e = cudaMalloc(&s.x, 2ull * kIn * ni);
   if (e == cudaSuccess) e = cudaMalloc(&s.y, 4 * ni);
-  if (e == cudaSuccess) e = cudaMemset(s.arrive + n, 0, 4);
+  if (e == cudaSuccess) e = cudaMemset(s.err, 0, 4);
   if (e != cudaSuccess) {
     set_last_error("lr_scratch_alloc", e);
     lr_scratch_free(s);
@@ -695,19 +698,21 @@ void lr_scratch_free(LrScratch &s) {
     s.anc[k] = s.dep[k] = nullptr;
   }
   cudaFree(s.leafCount);
-  cudaFree(s.arrive);
+  cudaFree(s.acc);
+  cudaFree(s.err);
   cudaFree(s.hist);
   cudaFree(s.raw);
   cudaFree(s.src);
   cudaFree(s.x);
   cudaFree(s.y);
-  s.leafCount = s.arrive = s.hist = nullptr;
+  s.leafCount = s.hist = s.err = nullptr;
+  s.acc = nullptr;
   s.raw = s.src = s.y = nullptr;
   s.x = nullptr;
   s.numNodes = 0;
 }
 
-uint32_t *lr_error_word(LrScratch &s) { return s.arrive + s.numNodes; }
+uint32_t *lr_error_word(LrScratch &s) { return s.err; }
 
 int lr_features(LrScratch &s, const bvhgb_node *nodes, uint32_t numNodes, uint32_t root, const uint32_t *inner,
                 uint32_t numInner, float invLog2Leaves, cudaStream_t st) {
@@ -722,8 +727,8 @@ int lr_features(LrScratch &s, const bvhgb_node *nodes, uint32_t numNodes, uint32
     BVHGB_LAUNCH_CHECK("lr depth jump");
     cur ^= 1;
   }
-  BVHGB_CUDA_TRY(cudaMemsetAsync(s.arrive, 0, 4ull * numNodes, st));
-  leaf_count_kernel<<<g, 256, 0, st>>>(nodes, numNodes, root, s.leafCount, s.arrive, lr_error_word(s));
+  BVHGB_CUDA_TRY(cudaMemsetAsync(s.acc, 0, 8ull * numNodes, st));
+  leaf_count_kernel<<<g, 256, 0, st>>>(nodes, numNodes, root, s.leafCount, s.acc, lr_error_word(s));
   BVHGB_LAUNCH_CHECK("lr leaf count");
   BVHGB_CUDA_TRY(cudaMemsetAsync(s.hist, 0, 4ull * kRankBins * 4, st));
   const uint32_t gi = grid_for(numInner, 256);

@@ -21,7 +21,8 @@ constexpr float kTargetEps = 0.16f;           // target = sign(g) ln(1 + |g| num
 struct LrScratch {
   uint32_t numNodes = 0;
   uint32_t *anc[2] = {nullptr, nullptr}, *dep[2] = {nullptr, nullptr};
-  uint32_t *leafCount = nullptr, *arrive = nullptr, *hist = nullptr;
+  uint32_t *leafCount = nullptr, *hist = nullptr, *err = nullptr;
+  unsigned long long *acc = nullptr;  // leaf-count accumulators: 2^40 per arrival + the arriving count
   float *raw = nullptr, *src = nullptr;
   uint16_t *x = nullptr;  // BF16 feature rows [numInner][24]
   float *y = nullptr;     // scorer output per inner node
