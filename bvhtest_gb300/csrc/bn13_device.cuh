@@ -304,9 +304,13 @@ __device__ bool remove_node(Patch &p, uint32_t x, uint32_t ins[2], uint32_t un[2
 // ---- batched best-first search: one warp per item -------------------------------------------
 //
 // The frontier (up to 128 entries) lives in registers, 4 slots per lane, entry e = slot * 32 + lane,
-// kept sorted by (cost, node). Each round the warp evaluates slot 0 (the 32 lowest-bound entries)
-// in parallel, reduces the best total, sorts the up-to-64 children with a bitonic network and
-// merges them into slots 1..3 with a bitonic merge; entries past 128 are dropped and counted.
+// in (cost, node) order. Each round the warp evaluates slot 0 (the 32 lowest-bound entries) in
+// parallel and reduces the best total (ties: the first entry in (cost, node) order); the up-to-64
+// children are sorted and merged into slots 1..3; entries past 128 are dropped and counted.
+// When the children are the whole new frontier (nothing is left in slots 1..3 and there are at
+// most 32 of them, which is nearly every round) they stay unsorted in slot 0: a round evaluates all
+// of slot 0 anyway, and only the tie rule above depends on the order. Each lane then loads its
+// child's tree record at once, so the next round does not wait for it.
 // oracle/bittner.c (gpu_find_node_batched) restates the same rounds.
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 constexpr int kFrontier = 4;  // slots per lane (128 entries)
@@ -390,7 +394,9 @@ __device__ uint32_t find_node_batched(const Patch &p, uint32_t n, SearchCounters
     fc[0] = 0.0f;
     fn[0] = p.root;
   }
-  uint32_t fsize = 1;  // finite frontier entries (warp-uniform)
+  uint32_t fsize = 1;      // finite frontier entries (warp-uniform)
+  bool haveRec = false;     // slot 0's tree records are already in rec[] (warp-uniform)
+  float4 rec[3];
   for (uint32_t round = 0;; ++round) {
     if (round > p.numNodes) {  // bounded: every round evaluates at least one node
       p.bad = true;
@@ -404,17 +410,32 @@ __device__ uint32_t find_node_batched(const Patch &p, uint32_t n, SearchCounters
     float total = kInf, induced = kInf;
     if (cand) {
       Box b;
-      const float4 *q = reinterpret_cast<const float4 *>(p.t + p.chk(fn[0]));
-      p.subset_aabb_from(fn[0], __ldg(q), __ldg(q + 1), __ldg(q + 2), cn, b);
+      const uint32_t xs = p.chk(fn[0]);
+      if (!haveRec) {
+        const float4 *q = reinterpret_cast<const float4 *>(p.t + xs);
+        rec[0] = __ldg(q);
+        rec[1] = __ldg(q + 1);
+        rec[2] = __ldg(q + 2);
+      }
+      p.subset_aabb_from(fn[0], rec[0], rec[1], rec[2], cn, b);
       induced = fmul(-1.0f, surface_area(b));
       merge_into(b, nbox);
       total = fadd(fc[0], surface_area(b));
       induced = fadd(induced, total);
     }
-    // Best of the round: smallest total, first in frontier order on ties.
+    // Best of the round: smallest total, first in (cost, node) order on ties.
     const uint32_t key = cand ? f2ord(total) : 0xFFFFFFFFu;
     const uint32_t kmin = __reduce_min_sync(kFull, key);
-    const uint32_t first = __ffs(__ballot_sync(kFull, cand && key == kmin)) - 1;
+    uint32_t tie = __ballot_sync(kFull, cand && key == kmin);
+    if (__popc(tie) > 1) {
+      const bool in = (tie >> lane) & 1u;
+      const uint32_t co = in ? f2ord(fc[0]) : 0xFFFFFFFFu;
+      const uint32_t cmin = __reduce_min_sync(kFull, co);
+      const bool in2 = in && co == cmin;
+      const uint32_t nmin = __reduce_min_sync(kFull, in2 ? fn[0] : 0xFFFFFFFFu);
+      tie = __ballot_sync(kFull, in2 && fn[0] == nmin);
+    }
+    const uint32_t first = __ffs(tie) - 1;
     const float rbest = ord2f(kmin);
     const uint32_t rnode = __shfl_sync(kFull, fn[0], first);
     if (rbest < best_cost) {
@@ -422,13 +443,15 @@ __device__ uint32_t find_node_batched(const Patch &p, uint32_t n, SearchCounters
       best = rnode;
     }
     const bool kids = cand && !cn.isLeafFlag && fadd(induced, sarea) < best_cost;
-    if (kids) {
-      if (cn.left < p.numNodes) prefetch_node(p.t, cn.left);
-      if (cn.right < p.numNodes) prefetch_node(p.t, cn.right);
-    }
     const uint32_t kmask = __ballot_sync(kFull, kids);
     const uint32_t m = 2u * __popc(kmask);                 // children this round
     const uint32_t rest = fsize - min(fsize, 32u);        // frontier entries left in slots 1..3
+    const bool unsortedNext = rest == 0 && m <= 32;
+    if (kids && !unsortedNext) {
+      if (cn.left < p.numNodes) prefetch_node(p.t, cn.left);
+      if (cn.right < p.numNodes) prefetch_node(p.t, cn.right);
+    }
+    haveRec = false;
     if (m == 0) {
       // Nothing to insert: the remaining frontier is already in order, shift it down a slot.
 #pragma unroll
@@ -440,12 +463,12 @@ __device__ uint32_t find_node_batched(const Patch &p, uint32_t n, SearchCounters
       fn[kFrontier - 1] = kNone;
       fsize = rest;
     } else if (m <= 32) {
-      // Common case: gather the children into one slot (lane j takes child j), sort it and merge
-      // it with the remaining frontier; at most 128 entries, no overflow. The k-th lane with
-      // children (in lane order) writes children 2k and 2k + 1 to the warp's buffer; every lane
-      // then reads its own child and, for its rank, all m of them as broadcasts, four at a time.
-      // Child j's rank is the number of children below it in (cost, node) order (keys are
-      // distinct: a node enters the frontier once).
+      // At most 32 children: gather them into one slot (lane j takes child j) through the warp's
+      // buffer, where the k-th lane with children (in lane order) writes children 2k and 2k + 1.
+      // If slots 1..3 are empty they are the new frontier as they are; otherwise they are sorted
+      // and merged with the rest (at most 128 entries, no overflow): child j's rank is the number
+      // of children below it in (cost, node) order (keys are distinct: a node enters the frontier
+      // once), read from the buffer as broadcasts, four at a time.
       uint2 *buf = rank_buffer();
       if (kids) {
         const uint32_t k = __popc(kmask & ((1u << lane) - 1u));
@@ -456,6 +479,28 @@ __device__ uint32_t find_node_batched(const Patch &p, uint32_t n, SearchCounters
       const uint2 own = buf[lane];
       const float cj = lane < m ? __uint_as_float(own.x) : kInf;
       const uint32_t nj = lane < m ? own.y : kNone;
+      if (rest == 0) {
+        // The children are the whole new frontier: they stay in slot 0 in the order gathered, and
+        // each lane loads its child's record now (an index out of range loads the root's record,
+        // as the tree path would after flagging it).
+        if (lane < m) {
+          const float4 *q = reinterpret_cast<const float4 *>(p.t + (nj < p.numNodes ? nj : p.root));
+          rec[0] = __ldg(q);
+          rec[1] = __ldg(q + 1);
+          rec[2] = __ldg(q + 2);
+        }
+        __syncwarp();
+        fc[0] = cj;
+        fn[0] = nj;
+#pragma unroll
+        for (int s = 1; s < kFrontier; ++s) {
+          fc[s] = kInf;
+          fn[s] = kNone;
+        }
+        fsize = m;
+        haveRec = true;
+        continue;
+      }
       uint32_t rank = 0;
       for (uint32_t i0 = 0; i0 < m; i0 += 4) {
 #pragma unroll
@@ -466,24 +511,7 @@ __device__ uint32_t find_node_batched(const Patch &p, uint32_t n, SearchCounters
         }
       }
       __syncwarp();
-      if (rest == 0) {
-        // Nothing else is left in the frontier (the usual case): the children in ascending order
-        // are the new frontier; lanes m .. 31 keep the empty entry.
-        buf[lane < m ? rank : lane] = make_uint2(__float_as_uint(cj), nj);
-        __syncwarp();
-        const uint2 e = buf[lane];
-        __syncwarp();
-        fc[0] = __uint_as_float(e.x);
-        fn[0] = e.y;
-#pragma unroll
-        for (int s = 1; s < kFrontier; ++s) {
-          fc[s] = kInf;
-          fn[s] = kNone;
-        }
-        fsize = m;
-        continue;
-      }
-      // Otherwise descending (lane 31 - rank, the unused lanes fill 0 .. 31 - m) and merged.
+      // Descending (lane 31 - rank, the unused lanes fill 0 .. 31 - m), then merged.
       buf[lane < m ? 31u - rank : lane - m] = make_uint2(__float_as_uint(cj), nj);
       __syncwarp();
       const uint2 e = buf[lane];
