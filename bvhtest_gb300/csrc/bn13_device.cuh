@@ -303,17 +303,17 @@ __device__ bool remove_node(Patch &p, uint32_t x, uint32_t ins[2], uint32_t un[2
 
 // ---- batched best-first search: one warp per item -------------------------------------------
 //
-// The frontier (up to 128 entries) lives in registers, 4 slots per lane, entry e = slot * 32 + lane,
-// in (cost, node) order. Each round the warp evaluates slot 0 (the 32 lowest-bound entries) in
-// parallel and reduces the best total (ties: the first entry in (cost, node) order); the up-to-64
-// children are sorted and merged into slots 1..3; entries past 128 are dropped and counted.
-// When the children are the whole new frontier (nothing is left in slots 1..3 and there are at
-// most 32 of them, which is nearly every round) they stay unsorted in slot 0: a round evaluates all
-// of slot 0 anyway, and only the tie rule above depends on the order. Each lane then loads its
-// child's tree record at once, so the next round does not wait for it.
+// The frontier (up to 128 entries, unordered) lives in registers, 4 slots per lane, entry
+// e = slot * 32 + lane; slots at or past `used` are empty. Each round the warp evaluates every
+// entry whose bound passes (up to four per lane, their loads issued together), reduces the best
+// total (ties: the entry first in (cost, node) order) and gathers the children of the expanded
+// entries into the warp's shared buffer, which becomes the next frontier. Only when more than 128
+// children arrive are they sorted (bitonic, in registers) and the 128 lowest kept, the rest
+// counted as overflow. The records of the next round's slot 0 are loaded as soon as it is known.
 // oracle/bittner.c (gpu_find_node_batched) restates the same rounds.
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 constexpr int kFrontier = 4;  // slots per lane (128 entries)
+constexpr uint32_t kFrontierCap = 32u * kFrontier;
 
 __device__ __forceinline__ bool fe_gt(float ca, uint32_t na, float cb, uint32_t nb) {
   return ca > cb || (ca == cb && na > nb);
@@ -362,201 +362,195 @@ __device__ __forceinline__ void bitonic_sort(float (&c)[S], uint32_t (&n)[S], bo
   }
 }
 
-template <int S>
-__device__ __forceinline__ void bitonic_merge(float (&c)[S], uint32_t (&n)[S], uint32_t lane) {
-#pragma unroll
-  for (int j = S * 16; j > 0; j >>= 1) bitonic_stage<S>(c, n, j, S * 32, false, lane);
+// Per-warp buffer of a round's children (up to 256 entries; blocks of up to kRankWarps warps).
+constexpr int kRankWarps = 8;
+__device__ __forceinline__ uint2 *child_buffer() {
+  __shared__ uint2 buf[kRankWarps][2 * kFrontierCap];
+  return buf[(threadIdx.x >> 5) & (kRankWarps - 1)];
 }
 
-// Per-warp scratch of the children's rank sort (blocks of up to kRankWarps warps).
-constexpr int kRankWarps = 8;
-__device__ __forceinline__ uint2 *rank_buffer() {
-  __shared__ uint2 buf[kRankWarps][32];
-  return buf[(threadIdx.x >> 5) & (kRankWarps - 1)];
+// State of one batched search (warp-uniform except the per-lane frontier entries and records).
+struct BatchedSearch {
+  float fc[kFrontier];
+  uint32_t fn[kFrontier];
+  uint32_t used;     // slots holding entries
+  bool haveRec;      // slot 0's tree records are already in rec[]
+  float4 rec[3];
+  float bestCost;
+  uint32_t best;
+};
+
+// One round over the first S slots (S >= used). Returns false when no entry passed the bound.
+template <int S>
+__device__ __forceinline__ bool batched_round(const Patch &p, BatchedSearch &st, const Box &nbox, float sarea,
+                                              uint2 *buf, SearchCounters &ctr) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t ltMask = (1u << lane) - 1u;
+  const float kInf = __int_as_float(0x7f800000);
+  bool cand[S];
+  uint32_t nc = 0;
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    cand[s] = st.fc[s] != kInf && fadd(st.fc[s], sarea) < st.bestCost;
+    nc += __popc(__ballot_sync(kFull, cand[s]));
+  }
+  if (nc == 0) return false;
+  ctr.visits += nc;
+  NodeP cn[S];
+  float total[S], induced[S];
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    total[s] = induced[s] = kInf;
+    if (!cand[s]) continue;
+    const uint32_t xs = p.chk(st.fn[s]);
+    float4 q0, q1, q2;
+    if (s == 0 && st.haveRec) {
+      q0 = st.rec[0]; q1 = st.rec[1]; q2 = st.rec[2];
+    } else {
+      const float4 *q = reinterpret_cast<const float4 *>(p.t + xs);
+      q0 = __ldg(q); q1 = __ldg(q + 1); q2 = __ldg(q + 2);
+    }
+    Box b;
+    p.subset_aabb_from(st.fn[s], q0, q1, q2, cn[s], b);
+    const float ind = fmul(-1.0f, surface_area(b));
+    merge_into(b, nbox);
+    total[s] = fadd(st.fc[s], surface_area(b));
+    induced[s] = fadd(ind, total[s]);
+  }
+  // Best of the round: smallest total, then smallest (cost, node) of the entry.
+  uint32_t kl = 0xFFFFFFFFu;
+#pragma unroll
+  for (int s = 0; s < S; ++s)
+    if (cand[s]) kl = min(kl, f2ord(total[s]));
+  const uint32_t kmin = __reduce_min_sync(kFull, kl);
+  uint32_t rnode;
+  uint32_t tieMask = 0;  // this lane's slots that reach kmin
+#pragma unroll
+  for (int s = 0; s < S; ++s)
+    if (cand[s] && f2ord(total[s]) == kmin) tieMask |= 1u << s;
+  const uint32_t tieLanes = __ballot_sync(kFull, tieMask != 0);
+  if (__popc(tieLanes) == 1 && (S == 1 || __popc(__shfl_sync(kFull, tieMask, __ffs(tieLanes) - 1)) == 1)) {
+    uint32_t mine = kNone;
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+      if (tieMask & (1u << s)) mine = st.fn[s];
+    rnode = __shfl_sync(kFull, mine, __ffs(tieLanes) - 1);
+  } else {
+    uint32_t cl = 0xFFFFFFFFu;
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+      if (tieMask & (1u << s)) cl = min(cl, f2ord(st.fc[s]));
+    const uint32_t cmin = __reduce_min_sync(kFull, cl);
+    uint32_t nl = 0xFFFFFFFFu;
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+      if ((tieMask & (1u << s)) && f2ord(st.fc[s]) == cmin) nl = min(nl, st.fn[s]);
+    rnode = __reduce_min_sync(kFull, nl);
+  }
+  const float rbest = ord2f(kmin);
+  if (rbest < st.bestCost) {
+    st.bestCost = rbest;
+    st.best = rnode;
+  }
+  // Children of the expanded entries: the k-th expanded entry (slot-major, then lane) writes
+  // children 2k and 2k + 1 to the warp's buffer.
+  uint32_t m = 0;
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    const bool kids = cand[s] && !cn[s].isLeafFlag && fadd(induced[s], sarea) < st.bestCost;
+    const uint32_t kmask = __ballot_sync(kFull, kids);
+    const uint32_t mk = 2u * __popc(kmask);
+    if (kids) {
+      const uint32_t k = m / 2 + __popc(kmask & ltMask);
+      buf[2 * k] = make_uint2(__float_as_uint(induced[s]), cn[s].left);
+      buf[2 * k + 1] = make_uint2(__float_as_uint(induced[s]), cn[s].right);
+      if (m + mk > 32u) {  // children past slot 0: warm their records in L2
+        if (cn[s].left < p.numNodes) prefetch_node(p.t, cn[s].left);
+        if (cn[s].right < p.numNodes) prefetch_node(p.t, cn[s].right);
+      }
+    }
+    m += mk;
+  }
+  __syncwarp();
+  st.haveRec = false;
+  if (m <= kFrontierCap) {
+    st.used = (m + 31u) / 32u;
+#pragma unroll
+    for (int s = 0; s < kFrontier; ++s) {
+      const uint32_t e = (uint32_t)s * 32u + lane;
+      if ((uint32_t)s < st.used) {
+        const uint2 v = e < m ? buf[e] : make_uint2(__float_as_uint(kInf), kNone);
+        st.fc[s] = __uint_as_float(v.x);
+        st.fn[s] = v.y;
+      } else {
+        st.fc[s] = kInf;
+        st.fn[s] = kNone;
+      }
+    }
+    if (lane < m) {  // slot 0's records for the next round (an index out of range: the root's)
+      const float4 *q = reinterpret_cast<const float4 *>(p.t + (st.fn[0] < p.numNodes ? st.fn[0] : p.root));
+      st.rec[0] = __ldg(q);
+      st.rec[1] = __ldg(q + 1);
+      st.rec[2] = __ldg(q + 2);
+    }
+    st.haveRec = true;
+  } else {
+    // Overflow: sort all children and keep the 128 lowest in (cost, node) order.
+    float c8[2 * kFrontier];
+    uint32_t n8[2 * kFrontier];
+#pragma unroll
+    for (int s = 0; s < 2 * kFrontier; ++s) {
+      const uint32_t e = (uint32_t)s * 32u + lane;
+      const uint2 v = e < m ? buf[e] : make_uint2(__float_as_uint(kInf), kNone);
+      c8[s] = __uint_as_float(v.x);
+      n8[s] = v.y;
+    }
+    bitonic_sort<2 * kFrontier>(c8, n8, false, lane);
+#pragma unroll
+    for (int s = 0; s < kFrontier; ++s) {
+      st.fc[s] = c8[s];
+      st.fn[s] = n8[s];
+    }
+    ctr.overflow += m - kFrontierCap;
+    st.used = kFrontier;
+  }
+  __syncwarp();
+  return true;
 }
 
 // findNode1's cost model in batched rounds (every lane of the warp calls it with the same patch).
 __device__ uint32_t find_node_batched(const Patch &p, uint32_t n, SearchCounters &ctr) {
   const uint32_t lane = threadIdx.x & 31u;
   const float kInf = __int_as_float(0x7f800000);
-  float best_cost = kInf;
-  uint32_t best = 0;
   const Box nbox = tree_box(p.t, p.chk(n));
   const float sarea = tree_sa(p.t, p.chk(n));
-  float fc[kFrontier];
-  uint32_t fn[kFrontier];
+  BatchedSearch st;
 #pragma unroll
   for (int s = 0; s < kFrontier; ++s) {
-    fc[s] = kInf;
-    fn[s] = kNone;
+    st.fc[s] = kInf;
+    st.fn[s] = kNone;
   }
   if (lane == 0) {
-    fc[0] = 0.0f;
-    fn[0] = p.root;
+    st.fc[0] = 0.0f;
+    st.fn[0] = p.root;
   }
-  uint32_t fsize = 1;      // finite frontier entries (warp-uniform)
-  bool haveRec = false;     // slot 0's tree records are already in rec[] (warp-uniform)
-  float4 rec[3];
+  st.used = 1;
+  st.haveRec = false;
+  st.bestCost = kInf;
+  st.best = 0;
+  uint2 *buf = child_buffer();
   for (uint32_t round = 0;; ++round) {
     if (round > p.numNodes) {  // bounded: every round evaluates at least one node
       p.bad = true;
       break;
     }
-    const bool cand = fc[0] != kInf && fadd(fc[0], sarea) < best_cost;
-    const uint32_t vmask = __ballot_sync(kFull, cand);
-    if (vmask == 0) break;
-    ctr.visits += __popc(vmask);
-    NodeP cn;
-    float total = kInf, induced = kInf;
-    if (cand) {
-      Box b;
-      const uint32_t xs = p.chk(fn[0]);
-      if (!haveRec) {
-        const float4 *q = reinterpret_cast<const float4 *>(p.t + xs);
-        rec[0] = __ldg(q);
-        rec[1] = __ldg(q + 1);
-        rec[2] = __ldg(q + 2);
-      }
-      p.subset_aabb_from(fn[0], rec[0], rec[1], rec[2], cn, b);
-      induced = fmul(-1.0f, surface_area(b));
-      merge_into(b, nbox);
-      total = fadd(fc[0], surface_area(b));
-      induced = fadd(induced, total);
-    }
-    // Best of the round: smallest total, first in (cost, node) order on ties.
-    const uint32_t key = cand ? f2ord(total) : 0xFFFFFFFFu;
-    const uint32_t kmin = __reduce_min_sync(kFull, key);
-    uint32_t tie = __ballot_sync(kFull, cand && key == kmin);
-    if (__popc(tie) > 1) {
-      const bool in = (tie >> lane) & 1u;
-      const uint32_t co = in ? f2ord(fc[0]) : 0xFFFFFFFFu;
-      const uint32_t cmin = __reduce_min_sync(kFull, co);
-      const bool in2 = in && co == cmin;
-      const uint32_t nmin = __reduce_min_sync(kFull, in2 ? fn[0] : 0xFFFFFFFFu);
-      tie = __ballot_sync(kFull, in2 && fn[0] == nmin);
-    }
-    const uint32_t first = __ffs(tie) - 1;
-    const float rbest = ord2f(kmin);
-    const uint32_t rnode = __shfl_sync(kFull, fn[0], first);
-    if (rbest < best_cost) {
-      best_cost = rbest;
-      best = rnode;
-    }
-    const bool kids = cand && !cn.isLeafFlag && fadd(induced, sarea) < best_cost;
-    const uint32_t kmask = __ballot_sync(kFull, kids);
-    const uint32_t m = 2u * __popc(kmask);                 // children this round
-    const uint32_t rest = fsize - min(fsize, 32u);        // frontier entries left in slots 1..3
-    const bool unsortedNext = rest == 0 && m <= 32;
-    if (kids && !unsortedNext) {
-      if (cn.left < p.numNodes) prefetch_node(p.t, cn.left);
-      if (cn.right < p.numNodes) prefetch_node(p.t, cn.right);
-    }
-    haveRec = false;
-    if (m == 0) {
-      // Nothing to insert: the remaining frontier is already in order, shift it down a slot.
-#pragma unroll
-      for (int s = 0; s + 1 < kFrontier; ++s) {
-        fc[s] = fc[s + 1];
-        fn[s] = fn[s + 1];
-      }
-      fc[kFrontier - 1] = kInf;
-      fn[kFrontier - 1] = kNone;
-      fsize = rest;
-    } else if (m <= 32) {
-      // At most 32 children: gather them into one slot (lane j takes child j) through the warp's
-      // buffer, where the k-th lane with children (in lane order) writes children 2k and 2k + 1.
-      // If slots 1..3 are empty they are the new frontier as they are; otherwise they are sorted
-      // and merged with the rest (at most 128 entries, no overflow): child j's rank is the number
-      // of children below it in (cost, node) order (keys are distinct: a node enters the frontier
-      // once), read from the buffer as broadcasts, four at a time.
-      uint2 *buf = rank_buffer();
-      if (kids) {
-        const uint32_t k = __popc(kmask & ((1u << lane) - 1u));
-        buf[2 * k] = make_uint2(__float_as_uint(induced), cn.left);
-        buf[2 * k + 1] = make_uint2(__float_as_uint(induced), cn.right);
-      }
-      __syncwarp();
-      const uint2 own = buf[lane];
-      const float cj = lane < m ? __uint_as_float(own.x) : kInf;
-      const uint32_t nj = lane < m ? own.y : kNone;
-      if (rest == 0) {
-        // The children are the whole new frontier: they stay in slot 0 in the order gathered, and
-        // each lane loads its child's record now (an index out of range loads the root's record,
-        // as the tree path would after flagging it).
-        if (lane < m) {
-          const float4 *q = reinterpret_cast<const float4 *>(p.t + (nj < p.numNodes ? nj : p.root));
-          rec[0] = __ldg(q);
-          rec[1] = __ldg(q + 1);
-          rec[2] = __ldg(q + 2);
-        }
-        __syncwarp();
-        fc[0] = cj;
-        fn[0] = nj;
-#pragma unroll
-        for (int s = 1; s < kFrontier; ++s) {
-          fc[s] = kInf;
-          fn[s] = kNone;
-        }
-        fsize = m;
-        haveRec = true;
-        continue;
-      }
-      uint32_t rank = 0;
-      for (uint32_t i0 = 0; i0 < m; i0 += 4) {
-#pragma unroll
-        for (uint32_t q = 0; q < 4; ++q) {
-          const uint2 o = buf[(i0 + q) & 31u];
-          const float ci = __uint_as_float(o.x);
-          rank += (i0 + q < m && (ci < cj || (ci == cj && o.y < nj))) ? 1u : 0u;
-        }
-      }
-      __syncwarp();
-      // Descending (lane 31 - rank, the unused lanes fill 0 .. 31 - m), then merged.
-      buf[lane < m ? 31u - rank : lane - m] = make_uint2(__float_as_uint(cj), nj);
-      __syncwarp();
-      const uint2 e = buf[lane];
-      __syncwarp();
-      float c1[1] = {__uint_as_float(e.x)};
-      uint32_t n1[1] = {e.y};
-      if (rest <= 32) {
-        float mc[2] = {fc[1], c1[0]};
-        uint32_t mn[2] = {fn[1], n1[0]};
-        bitonic_merge<2>(mc, mn, lane);
-        fc[0] = mc[0]; fn[0] = mn[0];
-        fc[1] = mc[1]; fn[1] = mn[1];
-        fc[2] = fc[3] = kInf;
-        fn[2] = fn[3] = kNone;
-      } else {
-        float mc[4] = {fc[1], fc[2], fc[3], c1[0]};
-        uint32_t mn[4] = {fn[1], fn[2], fn[3], n1[0]};
-        bitonic_merge<4>(mc, mn, lane);
-#pragma unroll
-        for (int s = 0; s < kFrontier; ++s) {
-          fc[s] = mc[s];
-          fn[s] = mn[s];
-        }
-      }
-      fsize = rest + m;
-    } else {
-      // Wide round: sort all children (two slots) and merge into 256, keeping the lowest 128.
-      float cc[2] = {kids ? induced : kInf, kids ? induced : kInf};
-      uint32_t cnn[2] = {kids ? cn.left : kNone, kids ? cn.right : kNone};
-      bitonic_sort<2>(cc, cnn, true, lane);
-      float mc[8] = {fc[1], fc[2], fc[3], kInf, kInf, kInf, cc[0], cc[1]};
-      uint32_t mn[8] = {fn[1], fn[2], fn[3], kNone, kNone, kNone, cnn[0], cnn[1]};
-      bitonic_merge<8>(mc, mn, lane);
-#pragma unroll
-      for (int s = 0; s < kFrontier; ++s) {
-        fc[s] = mc[s];
-        fn[s] = mn[s];
-      }
-      const uint32_t total = rest + m;
-      ctr.overflow += total > 128u ? total - 128u : 0u;
-      fsize = min(total, 128u);
-    }
+    const bool more = st.used <= 1   ? batched_round<1>(p, st, nbox, sarea, buf, ctr)
+                      : st.used <= 2 ? batched_round<2>(p, st, nbox, sarea, buf, ctr)
+                                     : batched_round<kFrontier>(p, st, nbox, sarea, buf, ctr);
+    if (!more) break;
   }
   p.bad = __any_sync(kFull, p.bad);
-  return best;
+  return st.best;
 }
 
 // reinsert (Bittner13CUDA.cu:308-358).

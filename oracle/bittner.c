@@ -393,13 +393,12 @@ static int gpu_remove(bpatch *p, uint32_t x, uint32_t ins[2], uint32_t un[2], ui
 }
 
 /* Batched best-first search (the GPU kernels' default search). Same cost model and pruning as
- * findNode1, but each round evaluates the BF_K lowest-bound entries of the frontier together:
- * the frontier is ordered by (cost, node); the entries whose bound cost + SA(n) is below the best
- * total so far (a prefix) are evaluated, the best total among them (first in order on ties)
- * replaces the best if strictly smaller, every evaluated inner node whose induced cost still
- * passes the bound against the updated best pushes both children, and the frontier keeps its
- * BF_CAP lowest entries (the rest are counted as overflow). */
-#define BF_K 32
+ * findNode1, but in rounds over the whole frontier: every frontier entry whose bound cost + SA(n)
+ * is below the best total so far is evaluated; the best total among them (ties: the entry first
+ * in (cost, node) order) replaces the best if strictly smaller; every evaluated inner node whose
+ * induced cost still passes the bound against the updated best pushes both children; if more
+ * than BF_CAP children were pushed, the BF_CAP lowest in (cost, node) order are kept (the rest
+ * are counted as overflow). The frontier's order plays no other part. */
 #define BF_CAP 128
 
 typedef struct fent {
@@ -420,43 +419,42 @@ static uint32_t gpu_find_node_batched(const bpatch *p, uint32_t n, uint64_t *ove
   const orc_node *nd = &p->t[n];
   orc_aabb nbox = nd->bbox;
   float sarea = nd->surfaceArea;
-  fent f[BF_CAP + 2 * BF_K], nf[BF_CAP + 2 * BF_K];
+  fent f[BF_CAP], nf[2 * BF_CAP];
   size_t fn = 1;
   f[0].c = 0.0f;
   f[0].n = p->root;
   for (;;) {
-    size_t take = fn < BF_K ? fn : BF_K;
-    size_t nv = 0;
-    while (nv < take && f[nv].c + sarea < best_cost) nv++;
+    float tot[BF_CAP], ind[BF_CAP];
+    npatch cn[BF_CAP];
+    size_t cand[BF_CAP], nv = 0;
+    for (size_t i = 0; i < fn; ++i)
+      if (f[i].c + sarea < best_cost) cand[nv++] = i;
     if (nv == 0) break;
     if (visits) *visits += nv;
-    float tot[BF_K], ind[BF_K];
-    npatch cn[BF_K];
-    for (size_t i = 0; i < nv; ++i) {
-      cn[i] = bp_get_subset(p, f[i].n);
-      orc_aabb b = bp_get_aabb(p, f[i].n);
+    size_t bi = 0;
+    for (size_t v = 0; v < nv; ++v) {
+      const fent *e = &f[cand[v]];
+      cn[v] = bp_get_subset(p, e->n);
+      orc_aabb b = bp_get_aabb(p, e->n);
       float induced = -1.0f * orc_surface_area(&b);
       merge_into(&b, &nbox);
       float direct = orc_surface_area(&b);
-      tot[i] = f[i].c + direct;
-      ind[i] = induced + tot[i];
+      tot[v] = e->c + direct;
+      ind[v] = induced + tot[v];
+      if (v > 0 && (tot[v] < tot[bi] || (tot[v] == tot[bi] && fent_cmp(e, &f[cand[bi]]) < 0))) bi = v;
     }
-    size_t bi = 0;
-    for (size_t i = 1; i < nv; ++i)
-      if (tot[i] < tot[bi]) bi = i;
     if (tot[bi] < best_cost) {
       best_cost = tot[bi];
-      best = f[bi].n;
+      best = f[cand[bi]].n;
     }
     size_t m = 0;
-    for (size_t i = take; i < fn; ++i) nf[m++] = f[i];
-    for (size_t i = 0; i < nv; ++i) {
-      if (cn[i].isLeafFlag || !(ind[i] + sarea < best_cost)) continue;
-      nf[m].c = ind[i]; nf[m].n = cn[i].left; m++;
-      nf[m].c = ind[i]; nf[m].n = cn[i].right; m++;
+    for (size_t v = 0; v < nv; ++v) {
+      if (cn[v].isLeafFlag || !(ind[v] + sarea < best_cost)) continue;
+      nf[m].c = ind[v]; nf[m].n = cn[v].left; m++;
+      nf[m].c = ind[v]; nf[m].n = cn[v].right; m++;
     }
-    qsort(nf, m, sizeof(fent), fent_cmp);
     if (m > BF_CAP) {
+      qsort(nf, m, sizeof(fent), fent_cmp);
       *overflow += m - BF_CAP;
       m = BF_CAP;
     }
