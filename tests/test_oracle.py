@@ -239,3 +239,14 @@ def test_bittner_chunked_improves_and_stays_valid(orc):
     # deterministic
     out2, trace2, _ = orc.bittner_chunked(nodes, 10)
     assert np.array_equal(out.view(np.uint8), out2.view(np.uint8))
+
+
+def test_batched_search_reaches_the_heap_order_sah(orc):
+    """The batched search (whole-frontier rounds) finds the same optimum as the reference's
+    heap order up to ties and overflow: equal iteration counts give SAH within 0.5%."""
+    vert, faces = scenes.uniform_soup(20000, seed=21)
+    nodes, _, _ = orc.lbvh_build(vert, faces)
+    _, tb, st_b = orc.bittner_chunked(nodes, 10, search_mode=0)
+    _, th, _ = orc.bittner_chunked(nodes, 10, search_mode=1)
+    assert abs(tb[-1] / th[-1] - 1.0) <= 0.005, (tb[-1], th[-1])
+    assert tb[-1] < 0.8 * tb[0]
