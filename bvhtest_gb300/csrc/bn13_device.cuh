@@ -665,6 +665,7 @@ __device__ __forceinline__ void apply_item(bvhgb_node *t, const PatchOut &in, ui
 
 // Release a third of an item's claims and count the arrivals along one dirty path (kFixTree3_1);
 // the parent link is loaded together with the counter update, so a level costs one round trip.
+// The path's own start node gets bit 31 as well (the refit below must know its start nodes).
 __device__ __forceinline__ void count_path(const bvhgb_node *__restrict__ t, uint32_t root, uint32_t numNodes,
                                           const PatchOut &in, uint32_t j, uint32_t x, uint32_t *__restrict__ owner,
                                           uint32_t *__restrict__ counter, uint32_t *__restrict__ err) {
@@ -673,47 +674,79 @@ __device__ __forceinline__ void count_path(const bvhgb_node *__restrict__ t, uin
     if (y != kNone) owner[y] = kNone;
   }
   if (x == kNone) return;
+  uint32_t add = 0x80000001u;
   for (uint32_t steps = 0;; ++steps) {
     if (x >= numNodes || steps > numNodes) {
       atomicOr(err, kErrBadIndex);
       break;
     }
     const uint32_t px = t[x].parent;  // issued before the update; the links are final here
-    if (atomicAdd(&counter[x], 1u) != 0u) break;
+    if (atomicAdd(&counter[x], add) != 0u) break;
     if (x == root) break;
+    add = 1u;
     x = px;
   }
 }
 
 // The last path to arrive at a node recomputes its box (kFixTree3_2). A node's links do not change
-// in this launch, so they are read before its counter; after the acq_rel update only the other
-// child's box is loaded (the box of the child the path came from is still in registers).
+// in this launch, so they are read before its counter. A counter holds the arrivals still expected
+// (low 16 bits, from the count pass) and, above, how many arrivals brought a changed box: a path
+// whose node's box came out bitwise unchanged wrote nothing, so its arrival needs no release and
+// adds nothing; if no arrival at a node changed (and it is not a start node, whose children were
+// relinked), the node's box is already the union of its children's and only the climb goes on.
+// Near the root, where all paths meet, boxes rarely change, so most of a long climb costs one
+// relaxed round trip per level. Every node whose children were relinked by a patch is a start
+// node (grand parent, reused nodes; bit 31 of its counter, set by the count pass) or the parent of
+// a reused node, so a start node always reports a change. The last arrival resets the counter.
 __device__ __forceinline__ void refit_path(bvhgb_node *t, uint32_t root, uint32_t numNodes, uint32_t x,
                                           uint32_t *__restrict__ counter, uint32_t *__restrict__ err) {
   if (x == kNone) return;
   uint32_t from = kNone;  // child the path came from, whose box is 'cur'
   Box cur;
+  bool changed = true;    // the start node's children were relinked
   for (uint32_t steps = 0;; ++steps) {
     if (x >= numNodes || steps > numNodes) {
       atomicOr(err, kErrBadIndex);
       return;
     }
+    const float4 w0 = __ldcg(reinterpret_cast<const float4 *>(t + x));      // mn.xyz mx.x
     const float4 w1 = __ldcg(reinterpret_cast<const float4 *>(t + x) + 1);  // mx.y mx.z parent left
     const float4 w2 = __ldcg(reinterpret_cast<const float4 *>(t + x) + 2);  // right flags level sa
-    if (atom_add_acq_rel(&counter[x], 0xFFFFFFFFu) != 1u) return;  // not the last arrival
+    const uint32_t add = changed ? 0xFFFFu : 0xFFFFFFFFu;  // one arrival less (low 16 bits), one changed more
+    const uint32_t old = changed ? atom_add_acq_rel(&counter[x], add) : atom_add_acquire(&counter[x], add);
+    if ((old & 0xFFFFu) != 1u) return;  // not the last arrival
+    counter[x] = 0u;
     const uint32_t parent = __float_as_uint(w1.z), l = __float_as_uint(w1.w), r = __float_as_uint(w2.x);
     if ((__float_as_uint(w2.y) & 0xFFFFu) || l >= numNodes || r >= numNodes) {
       if (!(__float_as_uint(w2.y) & 0xFFFFu)) atomicOr(err, kErrBadIndex);
       return;
     }
-    Box b = from == l ? cur : load_box_cg(t + l);
-    const Box rb = from == r ? cur : load_box_cg(t + r);
-    merge_into(b, rb);
-    float4 *p = reinterpret_cast<float4 *>(t + x);
-    p[0] = make_float4(b.mn[0], b.mn[1], b.mn[2], b.mx[0]);
-    p[1] = make_float4(b.mx[1], b.mx[2], w1.z, w1.w);
-    t[x].surfaceArea = surface_area(b);
+    const bool start = (old >> 31) != 0u;  // x started a path (this one or an earlier arrival)
+    const bool anyChanged = changed || start || ((old >> 16) & 0x7FFFu) != 0u;
+    Box b;
+    b.mn[0] = w0.x; b.mn[1] = w0.y; b.mn[2] = w0.z;
+    b.mx[0] = w0.w; b.mx[1] = w1.x; b.mx[2] = w1.y;
+    bool upChanged = false;
+    if (anyChanged) {
+      Box nb = from == l ? cur : load_box_cg(t + l);
+      const Box rb = from == r ? cur : load_box_cg(t + r);
+      merge_into(nb, rb);
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        upChanged |= __float_as_uint(nb.mn[k]) != __float_as_uint(b.mn[k]) ||
+                     __float_as_uint(nb.mx[k]) != __float_as_uint(b.mx[k]);
+      if (upChanged) {
+        float4 *p = reinterpret_cast<float4 *>(t + x);
+        p[0] = make_float4(nb.mn[0], nb.mn[1], nb.mn[2], nb.mx[0]);
+        p[1] = make_float4(nb.mx[1], nb.mx[2], w1.z, w1.w);
+        t[x].surfaceArea = surface_area(nb);
+        b = nb;
+      }
+    }
     if (x == root) return;
+    // A start node may have moved (a reused node now hangs under a new parent), so its parent
+    // cannot compare against the old box: it always counts as changed.
+    changed = upChanged || start;
     from = x;
     cur = b;
     x = parent;
