@@ -472,12 +472,20 @@ __device__ __forceinline__ uint32_t rank_bin(float v) { return f2ord(v) >> 16; }
 
 // Depth by pointer jumping: after r rounds anc[x] is the 2^r-th ancestor of x, or the root, and
 // dep[x] the distance to it, so kDepthRounds rounds give min(depth, 2^kDepthRounds) exactly.
+// One coalesced pass over the nodes: the depth recursion's start, and compact copies of every
+// node's surface area and parent (bit 31: the node is a leaf) that the leaf counts and the feature
+// rows gather from (33 MB per 8M nodes each, so they stay in L2 where the 48-byte records do not).
+constexpr uint32_t kLeafBit = 0x80000000u;
 __global__ void depth_init_kernel(const bvhgb_node *__restrict__ t, uint32_t n, uint32_t root, uint32_t *__restrict__ anc,
-                                  uint32_t *__restrict__ dep) {
+                                  uint32_t *__restrict__ dep, float *__restrict__ sa, uint32_t *__restrict__ par) {
   for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
-    const uint32_t p = __ldg(&t[x].parent);
+    const float4 w1 = __ldg(reinterpret_cast<const float4 *>(t + x) + 1);  // mx.y mx.z parent left
+    const float4 w2 = __ldg(reinterpret_cast<const float4 *>(t + x) + 2);  // right flags level sa
+    const uint32_t p = __float_as_uint(w1.z);
     anc[x] = (x == root || p >= n) ? root : p;
     dep[x] = x == root ? 0u : 1u;
+    sa[x] = w2.w;
+    par[x] = (p & ~kLeafBit) | ((__float_as_uint(w2.y) & 0xFFFFu) ? kLeafBit : 0u);
   }
 }
 __global__ void depth_jump_kernel(uint32_t n, uint32_t root, const uint32_t *__restrict__ ancIn,
@@ -499,21 +507,22 @@ __global__ void depth_jump_kernel(uint32_t n, uint32_t root, const uint32_t *__r
 // receives the first's count in the same atomic, writes the parent's count and goes on. The count
 // travels in the atomic itself, so no fence or sibling load is needed; the next parent is loaded
 // before the atomic.
-__global__ void leaf_count_kernel(const bvhgb_node *__restrict__ t, uint32_t n, uint32_t root, uint32_t *cnt,
+__global__ void leaf_count_kernel(const uint32_t *__restrict__ par, uint32_t n, uint32_t root, uint32_t *cnt,
                                   unsigned long long *acc, uint32_t *err) {
   constexpr unsigned long long kArrival = 1ull << 40;
   for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
-    if (__ldg(&t[x].isLeafFlag) == 0) continue;
+    const uint32_t pv = __ldg(par + x);
+    if (!(pv & kLeafBit)) continue;
     __stcg(cnt + x, 1u);
     if (x == root) continue;
     uint32_t c = 1;
-    uint32_t y = __ldg(&t[x].parent);
+    uint32_t y = pv & ~kLeafBit;
     for (uint32_t steps = 0;; ++steps) {
       if (y >= n || steps > n) {
         atomicOr(err, kErrBadIndex);
         break;
       }
-      const uint32_t next = y == root ? root : __ldg(&t[y].parent);
+      const uint32_t next = y == root ? root : (__ldg(par + y) & ~kLeafBit);
       const unsigned long long old = atomicAdd(acc + y, kArrival | c);
       if (old == 0ull) break;  // first arrival: the sibling's climb continues
       c += (uint32_t)(old & (kArrival - 1ull));
@@ -530,9 +539,10 @@ __global__ void leaf_count_kernel(const bvhgb_node *__restrict__ t, uint32_t n, 
 __global__ void features_raw_kernel(const bvhgb_node *__restrict__ t, const uint32_t *__restrict__ inner,
                                     uint32_t numInner, uint32_t numNodes, uint32_t root,
                                     const uint32_t *__restrict__ depth, const uint32_t *__restrict__ leafCount,
+                                    const float *__restrict__ saOf, const uint32_t *__restrict__ par,
                                     float invLog2Leaves, float *__restrict__ raw, float *__restrict__ src,
                                     uint32_t *__restrict__ hist, uint32_t *__restrict__ err) {
-  const float sroot = __ldg(&t[root].surfaceArea);
+  const float sroot = __ldg(saOf + root);
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t base = blockIdx.x * blockDim.x; base < numInner; base += stride) {
@@ -546,19 +556,21 @@ __global__ void features_raw_kernel(const bvhgb_node *__restrict__ t, const uint
 #pragma unroll
         for (int k = 0; k < kMlpRaw; ++k) raw[(size_t)i * kMlpRaw + k] = 0.0f;
       } else {
-        const float sa = __ldg(&t[x].surfaceArea);
-        const uint32_t l = min(__ldg(&t[x].left), numNodes - 1), r = min(__ldg(&t[x].right), numNodes - 1);
-        const float sl = __ldg(&t[l].surfaceArea), sr = __ldg(&t[r].surfaceArea);
-        const uint32_t p = x == root ? root : min(__ldg(&t[x].parent), numNodes - 1);
-        const uint32_t g = p == root ? root : min(__ldg(&t[p].parent), numNodes - 1);
+        const float4 w1 = __ldg(reinterpret_cast<const float4 *>(t + x) + 1);  // mx.y mx.z parent left
+        const float4 w2 = __ldg(reinterpret_cast<const float4 *>(t + x) + 2);  // right flags level sa
+        const float sa = w2.w;
+        const uint32_t l = min(__float_as_uint(w1.w), numNodes - 1), r = min(__float_as_uint(w2.x), numNodes - 1);
+        const float sl = __ldg(saOf + l), sr = __ldg(saOf + r);
+        const uint32_t p = x == root ? root : min(__float_as_uint(w1.z), numNodes - 1);
+        const uint32_t g = p == root ? root : min(__ldg(par + p) & ~kLeafBit, numNodes - 1);
         const float mn = sl < sr ? sl : sr;
         const float sum = fadd(sl, sr);
         const float cost = fdiv(fmul(fmul(fmul(sa, sa), sa), 2.0f), fmul(sum, mn));  // kCalcCost
         const uint32_t d = min(depth[x], 1u << kDepthRounds);
         float f[kMlpRaw];
         f[0] = log2f(sa);
-        f[1] = fdiv(sa, __ldg(&t[p].surfaceArea));
-        f[2] = fdiv(sa, __ldg(&t[g].surfaceArea));
+        f[1] = fdiv(sa, __ldg(saOf + p));
+        f[2] = fdiv(sa, __ldg(saOf + g));
         f[3] = fdiv(sa, sum);
         f[4] = fmul((float)d, invLog2Leaves);
         f[5] = log2f((float)__ldcg(leafCount + l));
@@ -591,8 +603,17 @@ __global__ void __launch_bounds__(1024) hist_scan_kernel(uint32_t *hist) {
   const uint32_t *h = hist + blockIdx.x * kRankBins;
   uint32_t *pre = hist + (4 + blockIdx.x) * kRankBins;
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  // Each thread owns kPer consecutive bins, read (and written) as 16-byte vectors.
+  static_assert(kPer % 16 == 0, "vector access");
+  const uint4 *h4 = reinterpret_cast<const uint4 *>(h + tid * kPer);
   uint32_t local = 0;
-  for (uint32_t k = 0; k < kPer; ++k) local += h[tid * kPer + k];
+  for (uint32_t k0 = 0; k0 < kPer / 4; k0 += 4) {
+    uint4 v[4];
+#pragma unroll
+    for (uint32_t k = 0; k < 4; ++k) v[k] = h4[k0 + k];
+#pragma unroll
+    for (uint32_t k = 0; k < 4; ++k) local += v[k].x + v[k].y + v[k].z + v[k].w;
+  }
   uint32_t inc = local;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -613,9 +634,20 @@ __global__ void __launch_bounds__(1024) hist_scan_kernel(uint32_t *hist) {
   }
   __syncthreads();
   uint32_t run = warpSum[warp] + inc - local;
-  for (uint32_t k = 0; k < kPer; ++k) {
-    pre[tid * kPer + k] = run;
-    run += h[tid * kPer + k];
+  uint4 *p4 = reinterpret_cast<uint4 *>(pre + tid * kPer);
+  for (uint32_t k0 = 0; k0 < kPer / 4; k0 += 4) {
+    uint4 v[4];
+#pragma unroll
+    for (uint32_t k = 0; k < 4; ++k) v[k] = h4[k0 + k];
+#pragma unroll
+    for (uint32_t k = 0; k < 4; ++k) {
+      uint4 o;
+      o.x = run; run += v[k].x;
+      o.y = run; run += v[k].y;
+      o.z = run; run += v[k].z;
+      o.w = run; run += v[k].w;
+      p4[k0 + k] = o;
+    }
   }
 }
 
@@ -674,6 +706,8 @@ int lr_scratch_alloc(LrScratch &s, uint32_t numNodes) {
     if (e == cudaSuccess) e = cudaMalloc(&s.dep[k], 4 * n);
   }
   if (e == cudaSuccess) e = cudaMalloc(&s.leafCount, 4 * n);
+  if (e == cudaSuccess) e = cudaMalloc(&s.sa, 4 * n);
+  if (e == cudaSuccess) e = cudaMalloc(&s.par, 4 * n);
   if (e == cudaSuccess) e = cudaMalloc(&s.acc, 8 * n);
   if (e == cudaSuccess) e = cudaMalloc(&s.err, 4);
   if (e == cudaSuccess) e = cudaMalloc(&s.hist, 4ull * kRankBins * 8);
@@ -698,6 +732,10 @@ void lr_scratch_free(LrScratch &s) {
     s.anc[k] = s.dep[k] = nullptr;
   }
   cudaFree(s.leafCount);
+  cudaFree(s.sa);
+  cudaFree(s.par);
+  s.sa = nullptr;
+  s.par = nullptr;
   cudaFree(s.acc);
   cudaFree(s.err);
   cudaFree(s.hist);
@@ -719,7 +757,7 @@ int lr_features(LrScratch &s, const bvhgb_node *nodes, uint32_t numNodes, uint32
   if (numNodes > s.numNodes || numInner > s.numNodes / 2 + 1) return BVHGB_TOO_LARGE;
   if (numInner == 0) return BVHGB_OK;
   const uint32_t g = grid_for(numNodes, 256);
-  depth_init_kernel<<<g, 256, 0, st>>>(nodes, numNodes, root, s.anc[0], s.dep[0]);
+  depth_init_kernel<<<g, 256, 0, st>>>(nodes, numNodes, root, s.anc[0], s.dep[0], s.sa, s.par);
   BVHGB_LAUNCH_CHECK("lr depth init");
   int cur = 0;
   for (uint32_t r = 0; r < kDepthRounds; ++r) {
@@ -728,11 +766,11 @@ int lr_features(LrScratch &s, const bvhgb_node *nodes, uint32_t numNodes, uint32
     cur ^= 1;
   }
   BVHGB_CUDA_TRY(cudaMemsetAsync(s.acc, 0, 8ull * numNodes, st));
-  leaf_count_kernel<<<g, 256, 0, st>>>(nodes, numNodes, root, s.leafCount, s.acc, lr_error_word(s));
+  leaf_count_kernel<<<g, 256, 0, st>>>(s.par, numNodes, root, s.leafCount, s.acc, lr_error_word(s));
   BVHGB_LAUNCH_CHECK("lr leaf count");
   BVHGB_CUDA_TRY(cudaMemsetAsync(s.hist, 0, 4ull * kRankBins * 4, st));
   const uint32_t gi = grid_for(numInner, 256);
-  features_raw_kernel<<<gi, 256, 0, st>>>(nodes, inner, numInner, numNodes, root, s.dep[cur], s.leafCount,
+  features_raw_kernel<<<gi, 256, 0, st>>>(nodes, inner, numInner, numNodes, root, s.dep[cur], s.leafCount, s.sa, s.par,
                                           invLog2Leaves, s.raw, s.src, s.hist, lr_error_word(s));
   BVHGB_LAUNCH_CHECK("lr features");
   hist_scan_kernel<<<4, 1024, 0, st>>>(s.hist);

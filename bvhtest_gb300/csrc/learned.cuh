@@ -22,6 +22,8 @@ struct LrScratch {
   uint32_t numNodes = 0;
   uint32_t *anc[2] = {nullptr, nullptr}, *dep[2] = {nullptr, nullptr};
   uint32_t *leafCount = nullptr, *hist = nullptr, *err = nullptr;
+  float *sa = nullptr;        // per-node surface area (compact copy)
+  uint32_t *par = nullptr;    // per-node parent | leaf bit (compact copy)
   unsigned long long *acc = nullptr;  // leaf-count accumulators: 2^40 per arrival + the arriving count
   float *raw = nullptr, *src = nullptr;
   uint16_t *x = nullptr;  // BF16 feature rows [numInner][24]
