@@ -10,6 +10,7 @@
 //    (JCGT 2013): the far distance is scaled by 1 + 2*gamma(3), so a box that holds the closest
 //    hit is never culled; closest-hit ties resolve to the smallest primitive index;
 //  * each hit also yields (primId, t).
+#include <algorithm>
 #include <cmath>
 
 #include "common.cuh"
@@ -89,7 +90,8 @@ __device__ __forceinline__ float uniform01(uint64_t seed, uint64_t idx, uint32_t
 // primary rays only). The bounce starts on the hit point, offset along the normal that faces the
 // incoming ray; the direction follows Malley's method around that normal in the orthonormal basis
 // of Duff et al. (JCGT 2017).
-__global__ void __launch_bounds__(128) trace_bounce_kernel(const bvhgb_node *__restrict__ nodes, uint32_t numNodes,
+__global__ void __launch_bounds__(128) trace_bounce_kernel(const bvhgb_node *__restrict__ nodes,
+                                                           const TravNode *__restrict__ trav, uint32_t numNodes,
                                                            uint32_t root, const float *__restrict__ vert,
                                                            const uint32_t *__restrict__ faces, CamParams cam,
                                                            TraceParams tp, uint64_t seed, float offset,
@@ -155,13 +157,14 @@ __global__ void __launch_bounds__(128) trace_bounce_kernel(const bvhgb_node *__r
   }
   setup_ray(r);
   Hit h;
-  traverse(r, nodes, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
+  traverse_records(r, nodes, trav, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
   o.primId = h.prim;
   o.t = h.prim == kNone ? __int_as_float(0x7f800000) : h.t;
   out[pix] = o;
 }
 
-__global__ void __launch_bounds__(128) trace_image_kernel(const bvhgb_node *__restrict__ nodes, uint32_t numNodes,
+__global__ void __launch_bounds__(128) trace_image_kernel(const bvhgb_node *__restrict__ nodes,
+                                                          const TravNode *__restrict__ trav, uint32_t numNodes,
                                                           uint32_t root, const float *__restrict__ vert,
                                                           const uint32_t *__restrict__ faces, CamParams cam,
                                                           TraceParams tp, bvhgb_pixel *__restrict__ img,
@@ -172,7 +175,8 @@ __global__ void __launch_bounds__(128) trace_image_kernel(const bvhgb_node *__re
   RayPre r;
   camera_ray(cam, x, y, r);
   Hit h;
-  const uint32_t visits = traverse(r, nodes, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
+  const uint32_t visits =
+      traverse_records(r, nodes, trav, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
   bvhgb_pixel px_out;
   px_out.hit = 0;
   px_out.diffuse = 0;
@@ -193,7 +197,8 @@ __global__ void __launch_bounds__(128) trace_image_kernel(const bvhgb_node *__re
   }
 }
 
-__global__ void __launch_bounds__(128) trace_rays_kernel(const bvhgb_node *__restrict__ nodes, uint32_t numNodes,
+__global__ void __launch_bounds__(128) trace_rays_kernel(const bvhgb_node *__restrict__ nodes,
+                                                         const TravNode *__restrict__ trav, uint32_t numNodes,
                                                          uint32_t root, const float *__restrict__ vert,
                                                          const uint32_t *__restrict__ faces,
                                                          const float *__restrict__ org, const float *__restrict__ dir,
@@ -208,11 +213,47 @@ __global__ void __launch_bounds__(128) trace_rays_kernel(const bvhgb_node *__res
   }
   setup_ray(r);
   Hit h;
-  traverse(r, nodes, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
+  traverse_records(r, nodes, trav, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
   bvhgb_hit o;
   o.primId = h.prim;
   o.t = h.prim == kNone ? __int_as_float(0x7f800000) : h.t;
   hits[i] = o;
+}
+
+__global__ void build_trav_kernel(const bvhgb_node *__restrict__ nodes, uint32_t numNodes, TravNode *__restrict__ out) {
+  for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < numNodes; x += gridDim.x * blockDim.x)
+    build_trav(nodes, numNodes, x, out, &g_trace_errors);
+}
+
+// The traversal records of one trace call live in stream-ordered memory from a private pool that
+// keeps what it has (so repeated calls do not go back to the driver), one pool per device.
+cudaMemPool_t trav_pool() {
+  static cudaMemPool_t pools[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  if (!pools[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t p = nullptr;
+    if (cudaMemPoolCreate(&p, &props) != cudaSuccess) return nullptr;
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+    pools[dev] = p;
+  }
+  return pools[dev];
+}
+
+// Allocates and builds the records of a trace call on its stream; the caller frees them after its
+// kernel with cudaFreeAsync on the same stream.
+int make_trav(const bvhgb_node *nodes, uint32_t numNodes, cudaStream_t s, TravNode **out) {
+  cudaMemPool_t pool = trav_pool();
+  if (!pool) return BVHGB_CUDA_ERROR;
+  BVHGB_CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void **>(out), sizeof(TravNode) * (size_t)numNodes, pool, s));
+  build_trav_kernel<<<std::min(ceil_div(numNodes, 256), (uint32_t)sm_count() * 16), 256, 0, s>>>(nodes, numNodes, *out);
+  BVHGB_LAUNCH_CHECK("trace records");
+  return BVHGB_OK;
 }
 
 // Host mirror of the device normalise (each operation rounds once; this file's host code is
@@ -287,12 +328,18 @@ extern "C" BVHGB_API int bvhgb_trace_image(const bvhgb_node *nodes, uint32_t num
   if (!nodes || !vert || !faces || !cam || !img || numNodes == 0 || root >= numNodes) return BVHGB_INVALID_ARGUMENT;
   if (cam->width == 0 || cam->height == 0) return BVHGB_OK;
   const CamParams cp = make_cam_params(cam);
+  cudaStream_t s = as_stream(stream);
+  TravNode *trav = nullptr;
+  int st = make_trav(nodes, numNodes, s, &trav);
+  if (st) return st;
   dim3 block(16, 8);
   dim3 grid(ceil_div(cam->width, 16), ceil_div(cam->height, 8));
-  trace_image_kernel<<<grid, block, 0, as_stream(stream)>>>(nodes, numNodes, root, vert, faces, cp, make_trace_params(cfg),
-                                                            img, hits);
-  BVHGB_LAUNCH_CHECK("trace image");
-  return BVHGB_OK;
+  trace_image_kernel<<<grid, block, 0, s>>>(nodes, trav, numNodes, root, vert, faces, cp, make_trace_params(cfg), img,
+                                            hits);
+  st = check_launch("trace image");
+  count_launch();
+  cudaFreeAsync(trav, s);
+  return st;
 }
 
 extern "C" BVHGB_API int bvhgb_trace_rays(const bvhgb_node *nodes, uint32_t numNodes, uint32_t root, const float *vert,
@@ -301,10 +348,16 @@ extern "C" BVHGB_API int bvhgb_trace_rays(const bvhgb_node *nodes, uint32_t numN
   if (!nodes || !vert || !faces || numNodes == 0 || root >= numNodes) return BVHGB_INVALID_ARGUMENT;
   if (n == 0) return BVHGB_OK;
   if (!org || !dir || !hits) return BVHGB_INVALID_ARGUMENT;
-  trace_rays_kernel<<<ceil_div(n, 128), 128, 0, as_stream(stream)>>>(nodes, numNodes, root, vert, faces, org, dir, n,
-                                                                     make_trace_params(cfg), hits);
-  BVHGB_LAUNCH_CHECK("trace rays");
-  return BVHGB_OK;
+  cudaStream_t s = as_stream(stream);
+  TravNode *trav = nullptr;
+  int st = make_trav(nodes, numNodes, s, &trav);
+  if (st) return st;
+  trace_rays_kernel<<<ceil_div(n, 128), 128, 0, s>>>(nodes, trav, numNodes, root, vert, faces, org, dir, n,
+                                                     make_trace_params(cfg), hits);
+  st = check_launch("trace rays");
+  count_launch();
+  cudaFreeAsync(trav, s);
+  return st;
 }
 
 extern "C" BVHGB_API int bvhgb_trace_bounce(const bvhgb_node *nodes, uint32_t numNodes, uint32_t root, const float *vert,
@@ -316,13 +369,18 @@ extern "C" BVHGB_API int bvhgb_trace_bounce(const bvhgb_node *nodes, uint32_t nu
   if ((rayOrg == nullptr) != (rayDir == nullptr)) return BVHGB_INVALID_ARGUMENT;
   if (cam->width == 0 || cam->height == 0) return BVHGB_OK;
   const CamParams cp = make_cam_params(cam);
+  cudaStream_t s = as_stream(stream);
+  TravNode *trav = nullptr;
+  int st = make_trav(nodes, numNodes, s, &trav);
+  if (st) return st;
   dim3 block(16, 8);
   dim3 grid(ceil_div(cam->width, 16), ceil_div(cam->height, 8));
-  trace_bounce_kernel<<<grid, block, 0, as_stream(stream)>>>(nodes, numNodes, root, vert, faces, cp,
-                                                             make_trace_params(cfg), seed, offset, primary, bounce,
-                                                             rayOrg, rayDir);
-  BVHGB_LAUNCH_CHECK("trace bounce");
-  return BVHGB_OK;
+  trace_bounce_kernel<<<grid, block, 0, s>>>(nodes, trav, numNodes, root, vert, faces, cp, make_trace_params(cfg), seed,
+                                             offset, primary, bounce, rayOrg, rayDir);
+  st = check_launch("trace bounce");
+  count_launch();
+  cudaFreeAsync(trav, s);
+  return st;
 }
 
 extern "C" BVHGB_API int bvhgb_trace_read_errors(uint32_t *flags, int reset) {

@@ -201,5 +201,122 @@ __device__ __forceinline__ uint32_t traverse(const RayPre &r, const bvhgb_node *
   return visits;
 }
 
+
+// ---- traversal records --------------------------------------------------------------------------
+// Traversal record of an inner node: both children's boxes and references in 64 bytes (one aligned
+// pair of sectors), so a visit loads one record instead of the children's two 48-byte nodes, and a
+// leaf child's faces are known without loading the leaf. ref = the node id of an inner child, the
+// first face of a leaf child; count = 0 for an inner child, the leaf's face count. Built from the
+// drop-in node array before a trace (the boxes are copied bit for bit, so hits do not change).
+struct __align__(64) TravNode {
+  float4 q0;  // left mn.xyz, left mx.x
+  float4 q1;  // left mx.y mx.z, right mn.x mn.y
+  float4 q2;  // right mn.z, right mx.xyz
+  uint4 q3;   // left ref, right ref, left count, right count
+};
+
+
+__device__ __forceinline__ void build_trav(const bvhgb_node *__restrict__ nodes, uint32_t numNodes, uint32_t x,
+                                           TravNode *__restrict__ out, uint32_t *err) {
+  const float4 *p = reinterpret_cast<const float4 *>(nodes + x);
+  const float4 b = __ldg(p + 1), c = __ldg(p + 2);
+  if (__float_as_uint(c.y) & 0xFFFFu) return;  // leaves have no record
+  const uint32_t l = __float_as_uint(b.w), r = __float_as_uint(c.x);
+  TravNode t;
+  if (l >= numNodes || r >= numNodes) {  // no child can be hit: an empty box on both sides
+    atomicOr(err, kErrBadIndex);
+    const float inf = __int_as_float(0x7f800000);
+    t.q0 = make_float4(inf, inf, inf, -inf);
+    t.q1 = make_float4(-inf, -inf, inf, inf);
+    t.q2 = make_float4(inf, -inf, -inf, -inf);
+    t.q3 = make_uint4(0u, 0u, 0u, 0u);
+  } else {
+    const float4 *pl = reinterpret_cast<const float4 *>(nodes + l);
+    const float4 *pr = reinterpret_cast<const float4 *>(nodes + r);
+    const float4 la = __ldg(pl), lb = __ldg(pl + 1), lc = __ldg(pl + 2);
+    const float4 ra = __ldg(pr), rb = __ldg(pr + 1), rc = __ldg(pr + 2);
+    const bool lleaf = (__float_as_uint(lc.y) & 0xFFFFu) != 0, rleaf = (__float_as_uint(rc.y) & 0xFFFFu) != 0;
+    t.q0 = la;
+    t.q1 = make_float4(lb.x, lb.y, ra.x, ra.y);
+    t.q2 = make_float4(ra.z, ra.w, rb.x, rb.y);
+    t.q3 = make_uint4(lleaf ? __float_as_uint(lb.w) : l, rleaf ? __float_as_uint(rb.w) : r,
+                      lleaf ? __float_as_uint(lc.x) : 0u, rleaf ? __float_as_uint(rc.x) : 0u);
+  }
+  out[x] = t;
+}
+
+// Closest hit through the traversal records (same hits as traverse(): the boxes and triangle tests
+// are the same and the closest-hit rule does not depend on the order of the tests). A leaf child
+// is tested as soon as its box is hit, so the stack holds inner nodes only. Returns the number of
+// inner nodes visited.
+__device__ __forceinline__ uint32_t traverse_records(const RayPre &r, const bvhgb_node *__restrict__ nodes,
+                                                     const TravNode *__restrict__ trav, uint32_t numNodes,
+                                                     uint32_t root, const float *__restrict__ vert,
+                                                     const uint32_t *__restrict__ faces, float tmin, float tmax,
+                                                     bool cull, Hit &h, uint32_t *err) {
+  uint2 stack[kStack];
+  int sp = 0;
+  uint32_t visits = 0;
+  h.prim = kNone;
+  h.t = tmax;
+  float4 a, b, c;
+  load_node(nodes, root, a, b, c);
+  float tn;
+  if (!box_hit(r, a, b, tmin, tmax, tn)) return 0;
+  if (__float_as_uint(c.y) & 0xFFFFu) {
+    test_leaf(r, vert, faces, __float_as_uint(b.w), __float_as_uint(c.x), tmin, tmax, cull, h);
+    return 0;
+  }
+  uint32_t cur = root;
+  for (uint32_t it = 0;; ++it) {
+    if (it > numNodes) {  // a tree visits each node at most once: a cyclic (corrupted) input
+      atomicOr(err, kErrBadIndex);
+      break;
+    }
+    ++visits;
+    const float4 *q = reinterpret_cast<const float4 *>(trav + cur);
+    const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2);
+    const uint4 q3 = __ldg(reinterpret_cast<const uint4 *>(q + 3));
+    float lim = h.prim == kNone ? tmax : fmul(h.t, kBestSlack);
+    float tl, tr;
+    bool hl = box_hit(r, q0, make_float4(q1.x, q1.y, 0.0f, 0.0f), tmin, lim, tl);
+    bool hr = box_hit(r, make_float4(q1.z, q1.w, q2.x, q2.y), make_float4(q2.z, q2.w, 0.0f, 0.0f), tmin, lim, tr);
+    if (hl && q3.z) {
+      test_leaf(r, vert, faces, q3.x, q3.z, tmin, tmax, cull, h);
+      hl = false;
+    }
+    if (hr && q3.w) {
+      test_leaf(r, vert, faces, q3.y, q3.w, tmin, tmax, cull, h);
+      hr = false;
+    }
+    if (hl || hr) lim = h.prim == kNone ? tmax : fmul(h.t, kBestSlack);
+    hl = hl && tl <= lim;
+    hr = hr && tr <= lim;
+    if (hl && hr) {
+      const bool lfirst = tl <= tr;
+      if (sp < kStack) stack[sp++] = make_uint2(lfirst ? q3.y : q3.x, __float_as_uint(lfirst ? tr : tl));
+      else atomicOr(err, kErrStackOverflow);
+      cur = lfirst ? q3.x : q3.y;
+      continue;
+    }
+    if (hl || hr) {
+      cur = hl ? q3.x : q3.y;
+      continue;
+    }
+    // Pop the next subtree whose entry distance can still beat the best hit.
+    bool found = false;
+    while (sp > 0) {
+      const uint2 e = stack[--sp];
+      if (__uint_as_float(e.y) <= (h.prim == kNone ? tmax : fmul(h.t, kBestSlack))) {
+        cur = e.x;
+        found = true;
+        break;
+      }
+    }
+    if (!found) break;
+  }
+  return visits;
+}
+
 }  // namespace
 }  // namespace bvhgb
