@@ -227,6 +227,7 @@ def run_ours(args, w, rank, world, local):
     lbvh.build(vert, faces, nodes)
     torch.cuda.synchronize()
     opt = api.Bittner13GPU(nodes, num_nodes=n_nodes, profile=not args.no_kernel_events)
+    tracer = api.Tracer(n_nodes)
     cam = w["camera"]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
 
@@ -247,8 +248,9 @@ def run_ours(args, w, rank, world, local):
         marks.append(ev())
         opt.run(w["iters"])
         marks.append(ev())
-        img, hits = api.trace_image(nodes, vert, faces, cam, num_nodes=n_nodes)
-        bounce, _, _ = api.trace_bounce(nodes, vert, faces, cam, hits, seed=17, num_nodes=n_nodes)
+        tracer.update(nodes, num_nodes=n_nodes)  # traversal records of this tree, timed with the trace
+        img, hits = tracer.trace_image(vert, faces, cam)
+        bounce, _, _ = tracer.trace_bounce(vert, faces, cam, hits, seed=17)
         marks.append(ev())
         return marks, hits, bounce
 
@@ -510,14 +512,16 @@ def stress_arm(args, dev, flush, scorer):
     org_h, dir_h, sizes = scenes.stress_rays(lo, hi)
     org = torch.from_numpy(org_h).to(dev)
     dirs = torch.from_numpy(dir_h).to(dev)
-    api.trace_rays(nodes, v, f, org[:65536], dirs[:65536], num_nodes=n_nodes)  # warm-up
+    tracer = api.Tracer(n_nodes)
+    tracer.update(nodes, num_nodes=n_nodes).trace_rays(v, f, org[:65536], dirs[:65536])  # warm-up
     flush.fill_(1)
     torch.cuda.synchronize()
     marks = [ev()]
     marks[0].record()
+    tracer.update(nodes, num_nodes=n_nodes)  # the traversal records, timed with the first batch
     hits, off = [], 0
     for sz in sizes:
-        hits.append(api.trace_rays(nodes, v, f, org[off:off + sz], dirs[off:off + sz], num_nodes=n_nodes))
+        hits.append(tracer.trace_rays(v, f, org[off:off + sz], dirs[off:off + sz]))
         off += sz
         m = ev()
         m.record()
@@ -840,6 +844,7 @@ def run_phase(args, w):
     lbvh = api.LBVH(n, w["bits"], w["topo"])
     lbvh.build(vert, faces, nodes)
     opt = api.Bittner13GPU(nodes, num_nodes=2 * n - 1) if args.only == "optimize" else None
+    tracer = api.Tracer(2 * n - 1) if args.only == "trace" else None
     if opt is not None and args.scorer:
         scorer = api.Mlp.load(args.scorer)
         opt.set_scorer(scorer, args.plain_every)
@@ -855,8 +860,9 @@ def run_phase(args, w):
             opt.iteration = 0
             opt.run(w["iters"])
         else:
-            img, hits = api.trace_image(nodes, vert, faces, w["camera"], num_nodes=2 * n - 1)
-            api.trace_bounce(nodes, vert, faces, w["camera"], hits, seed=17, num_nodes=2 * n - 1)
+            tracer.update(nodes, num_nodes=2 * n - 1)
+            img, hits = tracer.trace_image(vert, faces, w["camera"])
+            tracer.trace_bounce(vert, faces, w["camera"], hits, seed=17)
         e1.record()
         torch.cuda.synchronize()
         if i >= args.warmup:

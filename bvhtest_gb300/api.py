@@ -410,6 +410,68 @@ def trace_bounce(nodes, vert, faces, camera: dict, primary_hits, seed=1, offset=
     return out, org, dirs
 
 
+class Tracer:
+    """A tracer prepared for one tree (bvhgb_tracer_*): update() builds its traversal records (64 B
+    per inner node), after which trace_image / trace_rays / trace_bounce give the same hits as the
+    module functions with one record load per visit. The node tensor must not change between
+    update() and the traces."""
+
+    def __init__(self, max_nodes: int):
+        self.lib = load()
+        h = C.c_void_p()
+        check(self.lib.bvhgb_tracer_create(int(max_nodes), C.byref(h)), "bvhgb_tracer_create")
+        self.handle = h
+        self.nodes = None
+
+    def close(self):
+        if self.handle:
+            self.lib.bvhgb_tracer_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def update(self, nodes, root=0, num_nodes=None, stream=None):
+        n = nodes.shape[0] if num_nodes is None else num_nodes
+        check(self.lib.bvhgb_tracer_update(self.handle, _ptr(nodes), n, root, _stream(stream)), "bvhgb_tracer_update")
+        self.nodes = nodes  # kept alive: the records point into it
+        return self
+
+    def trace_image(self, vert, faces, camera: dict, light=(2.0, 2.0, 2.0), face_culling=False, with_hits=True,
+                    stream=None):
+        cam = make_camera(**camera)
+        cfg = make_trace_config(light, face_culling)
+        npx = cam.width * cam.height
+        img = torch.empty(npx, dtype=torch.int32, device="cuda")
+        hits = torch.empty(npx, dtype=torch.int64, device="cuda") if with_hits else None
+        check(self.lib.bvhgb_tracer_trace_image(self.handle, _ptr(vert), _ptr(faces), C.byref(cam), C.byref(cfg),
+                                                _ptr(img), _ptr(hits), _stream(stream)), "bvhgb_tracer_trace_image")
+        return img, hits
+
+    def trace_rays(self, vert, faces, org, dirs, tmin=0.0, tmax=float("inf"), face_culling=False, stream=None):
+        cfg = make_trace_config((2.0, 2.0, 2.0), face_culling, tmin, tmax)
+        o, d = _dev_f32(org), _dev_f32(dirs)
+        hits = torch.empty(o.shape[0], dtype=torch.int64, device="cuda")
+        check(self.lib.bvhgb_tracer_trace_rays(self.handle, _ptr(vert), _ptr(faces), _ptr(o), _ptr(d), o.shape[0],
+                                               C.byref(cfg), _ptr(hits), _stream(stream)), "bvhgb_tracer_trace_rays")
+        return hits
+
+    def trace_bounce(self, vert, faces, camera: dict, primary_hits, seed=1, offset=1e-4, with_rays=False, stream=None):
+        cam = make_camera(**camera)
+        cfg = make_trace_config()
+        npx = cam.width * cam.height
+        out = torch.empty(npx, dtype=torch.int64, device="cuda")
+        org = torch.empty((npx, 3), dtype=torch.float32, device="cuda") if with_rays else None
+        dirs = torch.empty((npx, 3), dtype=torch.float32, device="cuda") if with_rays else None
+        check(self.lib.bvhgb_tracer_trace_bounce(self.handle, _ptr(vert), _ptr(faces), C.byref(cam), C.byref(cfg), seed,
+                                                 offset, _ptr(primary_hits), _ptr(out), _ptr(org), _ptr(dirs),
+                                                 _stream(stream)), "bvhgb_tracer_trace_bounce")
+        return out, org, dirs
+
+
 def trace_errors(reset=True) -> int:
     v = C.c_uint32()
     check(load().bvhgb_trace_read_errors(C.byref(v), int(reset)), "bvhgb_trace_read_errors")

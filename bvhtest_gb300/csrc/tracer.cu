@@ -90,6 +90,7 @@ __device__ __forceinline__ float uniform01(uint64_t seed, uint64_t idx, uint32_t
 // primary rays only). The bounce starts on the hit point, offset along the normal that faces the
 // incoming ray; the direction follows Malley's method around that normal in the orthonormal basis
 // of Duff et al. (JCGT 2017).
+template <bool REC>
 __global__ void __launch_bounds__(128) trace_bounce_kernel(const bvhgb_node *__restrict__ nodes,
                                                            const TravNode *__restrict__ trav, uint32_t numNodes,
                                                            uint32_t root, const float *__restrict__ vert,
@@ -157,12 +158,14 @@ __global__ void __launch_bounds__(128) trace_bounce_kernel(const bvhgb_node *__r
   }
   setup_ray(r);
   Hit h;
-  traverse_records(r, nodes, trav, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
+  if (REC) traverse_records(r, nodes, trav, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
+  else traverse(r, nodes, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
   o.primId = h.prim;
   o.t = h.prim == kNone ? __int_as_float(0x7f800000) : h.t;
   out[pix] = o;
 }
 
+template <bool REC>
 __global__ void __launch_bounds__(128) trace_image_kernel(const bvhgb_node *__restrict__ nodes,
                                                           const TravNode *__restrict__ trav, uint32_t numNodes,
                                                           uint32_t root, const float *__restrict__ vert,
@@ -176,7 +179,8 @@ __global__ void __launch_bounds__(128) trace_image_kernel(const bvhgb_node *__re
   camera_ray(cam, x, y, r);
   Hit h;
   const uint32_t visits =
-      traverse_records(r, nodes, trav, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
+      REC ? traverse_records(r, nodes, trav, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors)
+          : traverse(r, nodes, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
   bvhgb_pixel px_out;
   px_out.hit = 0;
   px_out.diffuse = 0;
@@ -197,6 +201,7 @@ __global__ void __launch_bounds__(128) trace_image_kernel(const bvhgb_node *__re
   }
 }
 
+template <bool REC>
 __global__ void __launch_bounds__(128) trace_rays_kernel(const bvhgb_node *__restrict__ nodes,
                                                          const TravNode *__restrict__ trav, uint32_t numNodes,
                                                          uint32_t root, const float *__restrict__ vert,
@@ -213,7 +218,8 @@ __global__ void __launch_bounds__(128) trace_rays_kernel(const bvhgb_node *__res
   }
   setup_ray(r);
   Hit h;
-  traverse_records(r, nodes, trav, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
+  if (REC) traverse_records(r, nodes, trav, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
+  else traverse(r, nodes, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
   bvhgb_hit o;
   o.primId = h.prim;
   o.t = h.prim == kNone ? __int_as_float(0x7f800000) : h.t;
@@ -223,37 +229,6 @@ __global__ void __launch_bounds__(128) trace_rays_kernel(const bvhgb_node *__res
 __global__ void build_trav_kernel(const bvhgb_node *__restrict__ nodes, uint32_t numNodes, TravNode *__restrict__ out) {
   for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < numNodes; x += gridDim.x * blockDim.x)
     build_trav(nodes, numNodes, x, out, &g_trace_errors);
-}
-
-// The traversal records of one trace call live in stream-ordered memory from a private pool that
-// keeps what it has (so repeated calls do not go back to the driver), one pool per device.
-cudaMemPool_t trav_pool() {
-  static cudaMemPool_t pools[64] = {};
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
-  if (!pools[dev]) {
-    cudaMemPoolProps props = {};
-    props.allocType = cudaMemAllocationTypePinned;
-    props.location.type = cudaMemLocationTypeDevice;
-    props.location.id = dev;
-    cudaMemPool_t p = nullptr;
-    if (cudaMemPoolCreate(&p, &props) != cudaSuccess) return nullptr;
-    uint64_t keep = UINT64_MAX;
-    cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
-    pools[dev] = p;
-  }
-  return pools[dev];
-}
-
-// Allocates and builds the records of a trace call on its stream; the caller frees them after its
-// kernel with cudaFreeAsync on the same stream.
-int make_trav(const bvhgb_node *nodes, uint32_t numNodes, cudaStream_t s, TravNode **out) {
-  cudaMemPool_t pool = trav_pool();
-  if (!pool) return BVHGB_CUDA_ERROR;
-  BVHGB_CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void **>(out), sizeof(TravNode) * (size_t)numNodes, pool, s));
-  build_trav_kernel<<<std::min(ceil_div(numNodes, 256), (uint32_t)sm_count() * 16), 256, 0, s>>>(nodes, numNodes, *out);
-  BVHGB_LAUNCH_CHECK("trace records");
-  return BVHGB_OK;
 }
 
 // Host mirror of the device normalise (each operation rounds once; this file's host code is
@@ -317,8 +292,70 @@ TraceParams make_trace_params(const bvhgb_trace_config *cfg) {
   return tp;
 }
 
+// The three traces, on the node array (trav == nullptr) or on a prepared tracer's records.
+int launch_image(const bvhgb_node *nodes, const TravNode *trav, uint32_t numNodes, uint32_t root, const float *vert,
+                 const uint32_t *faces, const bvhgb_camera *cam, const bvhgb_trace_config *cfg, bvhgb_pixel *img,
+                 bvhgb_hit *hits, cudaStream_t s) {
+  if (cam->width == 0 || cam->height == 0) return BVHGB_OK;
+  const CamParams cp = make_cam_params(cam);
+  dim3 block(16, 8);
+  dim3 grid(ceil_div(cam->width, 16), ceil_div(cam->height, 8));
+  if (trav)
+    trace_image_kernel<true><<<grid, block, 0, s>>>(nodes, trav, numNodes, root, vert, faces, cp, make_trace_params(cfg),
+                                                    img, hits);
+  else
+    trace_image_kernel<false><<<grid, block, 0, s>>>(nodes, trav, numNodes, root, vert, faces, cp,
+                                                     make_trace_params(cfg), img, hits);
+  BVHGB_LAUNCH_CHECK("trace image");
+  return BVHGB_OK;
+}
+
+int launch_rays(const bvhgb_node *nodes, const TravNode *trav, uint32_t numNodes, uint32_t root, const float *vert,
+                const uint32_t *faces, const float *org, const float *dir, uint32_t n, const bvhgb_trace_config *cfg,
+                bvhgb_hit *hits, cudaStream_t s) {
+  if (n == 0) return BVHGB_OK;
+  if (!org || !dir || !hits) return BVHGB_INVALID_ARGUMENT;
+  if (trav)
+    trace_rays_kernel<true><<<ceil_div(n, 128), 128, 0, s>>>(nodes, trav, numNodes, root, vert, faces, org, dir, n,
+                                                             make_trace_params(cfg), hits);
+  else
+    trace_rays_kernel<false><<<ceil_div(n, 128), 128, 0, s>>>(nodes, trav, numNodes, root, vert, faces, org, dir, n,
+                                                              make_trace_params(cfg), hits);
+  BVHGB_LAUNCH_CHECK("trace rays");
+  return BVHGB_OK;
+}
+
+int launch_bounce(const bvhgb_node *nodes, const TravNode *trav, uint32_t numNodes, uint32_t root, const float *vert,
+                  const uint32_t *faces, const bvhgb_camera *cam, const bvhgb_trace_config *cfg, uint64_t seed,
+                  float offset, const bvhgb_hit *primary, bvhgb_hit *bounce, float *rayOrg, float *rayDir,
+                  cudaStream_t s) {
+  if (!primary || !bounce || (rayOrg == nullptr) != (rayDir == nullptr)) return BVHGB_INVALID_ARGUMENT;
+  if (cam->width == 0 || cam->height == 0) return BVHGB_OK;
+  const CamParams cp = make_cam_params(cam);
+  dim3 block(16, 8);
+  dim3 grid(ceil_div(cam->width, 16), ceil_div(cam->height, 8));
+  if (trav)
+    trace_bounce_kernel<true><<<grid, block, 0, s>>>(nodes, trav, numNodes, root, vert, faces, cp,
+                                                     make_trace_params(cfg), seed, offset, primary, bounce, rayOrg,
+                                                     rayDir);
+  else
+    trace_bounce_kernel<false><<<grid, block, 0, s>>>(nodes, trav, numNodes, root, vert, faces, cp,
+                                                      make_trace_params(cfg), seed, offset, primary, bounce, rayOrg,
+                                                      rayDir);
+  BVHGB_LAUNCH_CHECK("trace bounce");
+  return BVHGB_OK;
+}
+
 }  // namespace
 }  // namespace bvhgb
+
+// A tracer prepared for one tree: its traversal records, rebuilt by bvhgb_tracer_update.
+struct bvhgb_tracer {
+  uint32_t maxNodes = 0;
+  const bvhgb_node *nodes = nullptr;
+  uint32_t numNodes = 0, root = 0;
+  bvhgb::TravNode *trav = nullptr;
+};
 
 using namespace bvhgb;
 
@@ -326,61 +363,82 @@ extern "C" BVHGB_API int bvhgb_trace_image(const bvhgb_node *nodes, uint32_t num
                                            const uint32_t *faces, const bvhgb_camera *cam, const bvhgb_trace_config *cfg,
                                            bvhgb_pixel *img, bvhgb_hit *hits, bvhgb_stream stream) {
   if (!nodes || !vert || !faces || !cam || !img || numNodes == 0 || root >= numNodes) return BVHGB_INVALID_ARGUMENT;
-  if (cam->width == 0 || cam->height == 0) return BVHGB_OK;
-  const CamParams cp = make_cam_params(cam);
-  cudaStream_t s = as_stream(stream);
-  TravNode *trav = nullptr;
-  int st = make_trav(nodes, numNodes, s, &trav);
-  if (st) return st;
-  dim3 block(16, 8);
-  dim3 grid(ceil_div(cam->width, 16), ceil_div(cam->height, 8));
-  trace_image_kernel<<<grid, block, 0, s>>>(nodes, trav, numNodes, root, vert, faces, cp, make_trace_params(cfg), img,
-                                            hits);
-  st = check_launch("trace image");
-  count_launch();
-  cudaFreeAsync(trav, s);
-  return st;
+  return launch_image(nodes, nullptr, numNodes, root, vert, faces, cam, cfg, img, hits, as_stream(stream));
 }
 
 extern "C" BVHGB_API int bvhgb_trace_rays(const bvhgb_node *nodes, uint32_t numNodes, uint32_t root, const float *vert,
                                           const uint32_t *faces, const float *org, const float *dir, uint32_t n,
                                           const bvhgb_trace_config *cfg, bvhgb_hit *hits, bvhgb_stream stream) {
   if (!nodes || !vert || !faces || numNodes == 0 || root >= numNodes) return BVHGB_INVALID_ARGUMENT;
-  if (n == 0) return BVHGB_OK;
-  if (!org || !dir || !hits) return BVHGB_INVALID_ARGUMENT;
-  cudaStream_t s = as_stream(stream);
-  TravNode *trav = nullptr;
-  int st = make_trav(nodes, numNodes, s, &trav);
-  if (st) return st;
-  trace_rays_kernel<<<ceil_div(n, 128), 128, 0, s>>>(nodes, trav, numNodes, root, vert, faces, org, dir, n,
-                                                     make_trace_params(cfg), hits);
-  st = check_launch("trace rays");
-  count_launch();
-  cudaFreeAsync(trav, s);
-  return st;
+  return launch_rays(nodes, nullptr, numNodes, root, vert, faces, org, dir, n, cfg, hits, as_stream(stream));
 }
 
 extern "C" BVHGB_API int bvhgb_trace_bounce(const bvhgb_node *nodes, uint32_t numNodes, uint32_t root, const float *vert,
                                             const uint32_t *faces, const bvhgb_camera *cam, const bvhgb_trace_config *cfg,
                                             uint64_t seed, float offset, const bvhgb_hit *primary, bvhgb_hit *bounce,
                                             float *rayOrg, float *rayDir, bvhgb_stream stream) {
-  if (!nodes || !vert || !faces || !cam || !primary || !bounce || numNodes == 0 || root >= numNodes)
-    return BVHGB_INVALID_ARGUMENT;
-  if ((rayOrg == nullptr) != (rayDir == nullptr)) return BVHGB_INVALID_ARGUMENT;
-  if (cam->width == 0 || cam->height == 0) return BVHGB_OK;
-  const CamParams cp = make_cam_params(cam);
-  cudaStream_t s = as_stream(stream);
-  TravNode *trav = nullptr;
-  int st = make_trav(nodes, numNodes, s, &trav);
-  if (st) return st;
-  dim3 block(16, 8);
-  dim3 grid(ceil_div(cam->width, 16), ceil_div(cam->height, 8));
-  trace_bounce_kernel<<<grid, block, 0, s>>>(nodes, trav, numNodes, root, vert, faces, cp, make_trace_params(cfg), seed,
-                                             offset, primary, bounce, rayOrg, rayDir);
-  st = check_launch("trace bounce");
-  count_launch();
-  cudaFreeAsync(trav, s);
-  return st;
+  if (!nodes || !vert || !faces || !cam || numNodes == 0 || root >= numNodes) return BVHGB_INVALID_ARGUMENT;
+  return launch_bounce(nodes, nullptr, numNodes, root, vert, faces, cam, cfg, seed, offset, primary, bounce, rayOrg,
+                       rayDir, as_stream(stream));
+}
+
+extern "C" BVHGB_API int bvhgb_tracer_create(uint32_t maxNodes, bvhgb_tracer **out) {
+  if (!out || maxNodes == 0) return BVHGB_INVALID_ARGUMENT;
+  *out = nullptr;
+  auto *tr = new bvhgb_tracer();
+  tr->maxNodes = maxNodes;
+  const cudaError_t e = cudaMalloc(&tr->trav, sizeof(TravNode) * (size_t)maxNodes);
+  if (e != cudaSuccess) {
+    set_last_error("bvhgb_tracer_create", e);
+    delete tr;
+    return e == cudaErrorMemoryAllocation ? BVHGB_OUT_OF_MEMORY : BVHGB_CUDA_ERROR;
+  }
+  *out = tr;
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_tracer_destroy(bvhgb_tracer *tr) {
+  if (!tr) return BVHGB_OK;
+  cudaFree(tr->trav);
+  delete tr;
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_tracer_update(bvhgb_tracer *tr, const bvhgb_node *nodes, uint32_t numNodes, uint32_t root,
+                                             bvhgb_stream stream) {
+  if (!tr || !nodes || numNodes == 0 || root >= numNodes) return BVHGB_INVALID_ARGUMENT;
+  if (numNodes > tr->maxNodes) return BVHGB_TOO_LARGE;
+  tr->nodes = nodes;
+  tr->numNodes = numNodes;
+  tr->root = root;
+  build_trav_kernel<<<std::min(ceil_div(numNodes, 256), (uint32_t)sm_count() * 16), 256, 0, as_stream(stream)>>>(
+      nodes, numNodes, tr->trav);
+  BVHGB_LAUNCH_CHECK("tracer records");
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_tracer_trace_image(const bvhgb_tracer *tr, const float *vert, const uint32_t *faces,
+                                                  const bvhgb_camera *cam, const bvhgb_trace_config *cfg,
+                                                  bvhgb_pixel *img, bvhgb_hit *hits, bvhgb_stream stream) {
+  if (!tr || !tr->nodes || !vert || !faces || !cam || !img) return BVHGB_INVALID_ARGUMENT;
+  return launch_image(tr->nodes, tr->trav, tr->numNodes, tr->root, vert, faces, cam, cfg, img, hits, as_stream(stream));
+}
+
+extern "C" BVHGB_API int bvhgb_tracer_trace_rays(const bvhgb_tracer *tr, const float *vert, const uint32_t *faces,
+                                                 const float *org, const float *dir, uint32_t n,
+                                                 const bvhgb_trace_config *cfg, bvhgb_hit *hits, bvhgb_stream stream) {
+  if (!tr || !tr->nodes || !vert || !faces) return BVHGB_INVALID_ARGUMENT;
+  return launch_rays(tr->nodes, tr->trav, tr->numNodes, tr->root, vert, faces, org, dir, n, cfg, hits,
+                     as_stream(stream));
+}
+
+extern "C" BVHGB_API int bvhgb_tracer_trace_bounce(const bvhgb_tracer *tr, const float *vert, const uint32_t *faces,
+                                                   const bvhgb_camera *cam, const bvhgb_trace_config *cfg, uint64_t seed,
+                                                   float offset, const bvhgb_hit *primary, bvhgb_hit *bounce,
+                                                   float *rayOrg, float *rayDir, bvhgb_stream stream) {
+  if (!tr || !tr->nodes || !vert || !faces || !cam) return BVHGB_INVALID_ARGUMENT;
+  return launch_bounce(tr->nodes, tr->trav, tr->numNodes, tr->root, vert, faces, cam, cfg, seed, offset, primary,
+                       bounce, rayOrg, rayDir, as_stream(stream));
 }
 
 extern "C" BVHGB_API int bvhgb_trace_read_errors(uint32_t *flags, int reset) {

@@ -143,6 +143,13 @@ PROTOS = {
     "bvhgb_trace_bounce": (I32, [VP, U32, U32, VP, VP, C.POINTER(Camera), C.POINTER(TraceConfig), U64, F32, VP, VP,
                                  VP, VP, VP]),
     "bvhgb_trace_read_errors": (I32, [C.POINTER(U32), I32]),
+    "bvhgb_tracer_create": (I32, [U32, C.POINTER(VP)]),
+    "bvhgb_tracer_destroy": (I32, [VP]),
+    "bvhgb_tracer_update": (I32, [VP, VP, U32, U32, VP]),
+    "bvhgb_tracer_trace_image": (I32, [VP, VP, VP, C.POINTER(Camera), C.POINTER(TraceConfig), VP, VP, VP]),
+    "bvhgb_tracer_trace_rays": (I32, [VP, VP, VP, VP, VP, U32, C.POINTER(TraceConfig), VP, VP]),
+    "bvhgb_tracer_trace_bounce": (I32, [VP, VP, VP, C.POINTER(Camera), C.POINTER(TraceConfig), U64, F32, VP, VP, VP,
+                                        VP, VP]),
     "bvhgb_copy_mesh_to_gpu": (I32, [VP, U32, VP, U32, VP, U32, C.POINTER(MeshRaw)]),
     "bvhgb_copy_mesh_to_host": (I32, [C.POINTER(MeshRaw), VP, VP, VP]),
     "bvhgb_copy_bvh_to_gpu": (I32, [VP, U32, U32, C.c_uint16, C.POINTER(BvhPointer)]),

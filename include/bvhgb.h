@@ -435,6 +435,27 @@ BVHGB_API int bvhgb_trace_bounce(const bvhgb_node *nodes, uint32_t numNodes, uin
                                  const uint32_t *faces, const bvhgb_camera *cam, const bvhgb_trace_config *cfg,
                                  uint64_t seed, float offset, const bvhgb_hit *primary, bvhgb_hit *bounce,
                                  float *rayOrg, float *rayDir, bvhgb_stream stream);
+/* A tracer prepared for one tree (no counterpart in the reference, whose tracer reads the node
+ * array): bvhgb_tracer_update builds traversal records (both children's boxes and references per
+ * inner node, 64 bytes each, maxNodes of them allocated at create) once, and every trace call on
+ * the tracer reuses them, loading one record per visit instead of two 48-byte nodes. The node
+ * array must stay as it was at the last update while traces run. Same hits as the calls above. */
+typedef struct bvhgb_tracer bvhgb_tracer;
+BVHGB_API int bvhgb_tracer_create(uint32_t maxNodes, bvhgb_tracer **out);
+BVHGB_API int bvhgb_tracer_destroy(bvhgb_tracer *tr);
+BVHGB_API int bvhgb_tracer_update(bvhgb_tracer *tr, const bvhgb_node *nodes, uint32_t numNodes, uint32_t root,
+                                  bvhgb_stream stream);
+BVHGB_API int bvhgb_tracer_trace_image(const bvhgb_tracer *tr, const float *vert, const uint32_t *faces,
+                                       const bvhgb_camera *cam, const bvhgb_trace_config *cfg, bvhgb_pixel *img,
+                                       bvhgb_hit *hits, bvhgb_stream stream);
+BVHGB_API int bvhgb_tracer_trace_rays(const bvhgb_tracer *tr, const float *vert, const uint32_t *faces,
+                                      const float *org, const float *dir, uint32_t n, const bvhgb_trace_config *cfg,
+                                      bvhgb_hit *hits, bvhgb_stream stream);
+BVHGB_API int bvhgb_tracer_trace_bounce(const bvhgb_tracer *tr, const float *vert, const uint32_t *faces,
+                                        const bvhgb_camera *cam, const bvhgb_trace_config *cfg, uint64_t seed,
+                                        float offset, const bvhgb_hit *primary, bvhgb_hit *bounce, float *rayOrg,
+                                        float *rayDir, bvhgb_stream stream);
+
 /* Device-side traversal error bits seen since the last reset (2 = stack overflow, 4 = bad child
  * index); synchronous. */
 BVHGB_API int bvhgb_trace_read_errors(uint32_t *flags, int reset);

@@ -135,3 +135,33 @@ def test_rays_missing_everything(gpu):
     h = gpu.hits_to_numpy(gpu.trace_rays(nodes, v, f, org, dirs))
     torch.cuda.synchronize()
     assert np.all(h["prim"] == MISS) and np.all(np.isinf(h["t"]))
+
+
+def test_prepared_tracer_gives_the_same_hits(gpu):
+    """bvhgb_tracer_*: the traversal records (both children per record) give the node-array
+    traversal's hits for primary, bounce and random rays, and again after the tree changes."""
+    import torch
+    vert, faces, v, f, nodes = _scene(gpu, 20000, seed=4, bits=63, topo="karras")
+    n_nodes = 2 * 20000 - 1
+    tr = gpu.Tracer(n_nodes).update(nodes, num_nodes=n_nodes)
+    cam = scenes.camera_default()
+    for round_ in range(2):
+        img_a, hits_a = gpu.trace_image(nodes, v, f, cam, num_nodes=n_nodes)
+        img_b, hits_b = tr.trace_image(v, f, cam)
+        bounce_a, _, _ = gpu.trace_bounce(nodes, v, f, cam, hits_a, seed=3, num_nodes=n_nodes)
+        bounce_b, _, _ = tr.trace_bounce(v, f, cam, hits_b, seed=3)
+        org, dirs = scenes.random_rays(8192, vert.min(0), vert.max(0), seed=5 + round_)
+        rays_a = gpu.trace_rays(nodes, v, f, org, dirs, num_nodes=n_nodes)
+        rays_b = tr.trace_rays(v, f, org, dirs)
+        torch.cuda.synchronize()
+        assert torch.equal(hits_a, hits_b) and torch.equal(bounce_a, bounce_b) and torch.equal(rays_a, rays_b)
+        px_a, px_b = gpu.pixels_to_numpy(img_a), gpu.pixels_to_numpy(img_b)
+        assert np.array_equal(px_a["hit"], px_b["hit"]) and np.array_equal(px_a["diffuse"], px_b["diffuse"])
+        assert (gpu.hits_to_numpy(rays_a)["prim"] != MISS).mean() > 0.05  # about 11% of these rays hit
+        if round_ == 0:  # change the tree, rebuild the records
+            opt = gpu.Bittner13GPU(nodes, num_nodes=n_nodes)
+            opt.run(3)
+            opt.close()
+            tr.update(nodes, num_nodes=n_nodes)
+    assert gpu.trace_errors() == 0
+    tr.close()
