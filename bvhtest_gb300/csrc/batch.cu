@@ -205,7 +205,7 @@ __device__ __forceinline__ MeshItem item_of(const uint32_t *__restrict__ itemMes
   return {m, q - __ldg(itemOff + m)};
 }
 
-__global__ void __launch_bounds__(kWarpItemsPerBlock * 32) batch_patch_kernel(
+__global__ void __launch_bounds__(kWarpItemsPerBlock * 32, 5) batch_patch_kernel(
     const bvhgb_node *__restrict__ nodes, const uint32_t *__restrict__ todo, const uint32_t *__restrict__ itemMesh,
     const uint32_t *__restrict__ itemOff, const uint32_t *__restrict__ chunkSize,
     const uint32_t *__restrict__ faceOff, const uint32_t *__restrict__ nodeOff,

@@ -84,7 +84,7 @@ __global__ void patch_kernel(const bvhgb_node *__restrict__ t, uint32_t root, co
 
 // One warp per batch item: the patch logic runs redundantly on every lane (same data, no
 // divergence) and the two searches are the warp-cooperative batched search; lane 0 publishes.
-__global__ void __launch_bounds__(kWarpItemsPerBlock * 32) patch_warp_kernel(
+__global__ void __launch_bounds__(kWarpItemsPerBlock * 32, 5) patch_warp_kernel(
     const bvhgb_node *__restrict__ t, uint32_t root, const uint32_t *__restrict__ todo, uint32_t numTodo,
     uint32_t chunk, uint32_t numChunks, uint32_t chunkSize, uint32_t offsetAccess, PatchOut *__restrict__ out,
     uint32_t *__restrict__ valid, uint32_t *__restrict__ toFix, uint32_t *__restrict__ owner,

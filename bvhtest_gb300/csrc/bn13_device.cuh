@@ -308,58 +308,47 @@ __device__ bool remove_node(Patch &p, uint32_t x, uint32_t ins[2], uint32_t un[2
 // entry whose bound passes (up to four per lane, their loads issued together), reduces the best
 // total (ties: the entry first in (cost, node) order) and gathers the children of the expanded
 // entries into the warp's shared buffer, which becomes the next frontier. Only when more than 128
-// children arrive are they sorted (bitonic, in registers) and the 128 lowest kept, the rest
-// counted as overflow. The records of the next round's slot 0 are loaded as soon as it is known.
+// children arrive are the 128 lowest in (cost, node) order selected (a radix selection by warp
+// ballots) and kept, the rest counted as overflow. The records of the next round's slot 0 are loaded as soon as it is known.
 // oracle/bittner.c (gpu_find_node_batched) restates the same rounds.
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 constexpr int kFrontier = 4;  // slots per lane (128 entries)
 constexpr uint32_t kFrontierCap = 32u * kFrontier;
 
-__device__ __forceinline__ bool fe_gt(float ca, uint32_t na, float cb, uint32_t nb) {
-  return ca > cb || (ca == cb && na > nb);
-}
-
-// One compare-exchange stage of a bitonic network over S slots x 32 lanes.
+// The k-th smallest (1 <= k <= number of flagged entries) of the 32-bit keys of the slots flagged
+// in 'in' (bit s: this lane's slot s), S slots per lane: a most-significant-bit-first radix
+// selection by warp ballots, starting below the bits that all flagged keys share.
 template <int S>
-__device__ __forceinline__ void bitonic_stage(float (&c)[S], uint32_t (&n)[S], int j, int k, bool descending,
-                                              uint32_t lane) {
-  if (j >= 32) {
-    const int d = j >> 5;
+__device__ __forceinline__ uint32_t warp_select_kth(const uint32_t (&key)[S], uint32_t in, uint32_t k) {
+  uint32_t lo = 0xFFFFFFFFu, hi = 0u;
 #pragma unroll
-    for (int s = 0; s < S; ++s) {
-      if (s & d) continue;
-      const int t = s + d;
-      const uint32_t e = (uint32_t)s * 32u + lane;
-      const bool asc = ((e & (uint32_t)k) == 0) != descending;
-      const bool swap = asc ? fe_gt(c[s], n[s], c[t], n[t]) : fe_gt(c[t], n[t], c[s], n[s]);
-      if (swap) {
-        const float tc = c[s]; c[s] = c[t]; c[t] = tc;
-        const uint32_t tn = n[s]; n[s] = n[t]; n[t] = tn;
-      }
+  for (int s = 0; s < S; ++s)
+    if ((in >> s) & 1u) {
+      lo = min(lo, key[s]);
+      hi = max(hi, key[s]);
     }
-  } else {
+  lo = __reduce_min_sync(kFull, lo);
+  hi = __reduce_max_sync(kFull, hi);
+  if (lo == hi) return lo;
+  const int top = 31 - __clz(lo ^ hi);
+  uint32_t res = lo & ~((2u << top) - 1u);  // 2u << 31 wraps to 0: no common bits
+  uint32_t alive = in;
+  for (int bit = top; bit >= 0; --bit) {
+    uint32_t ones = 0;  // this lane's slots whose key has the bit set
 #pragma unroll
-    for (int s = 0; s < S; ++s) {
-      const float oc = __shfl_xor_sync(kFull, c[s], j);
-      const uint32_t on = __shfl_xor_sync(kFull, n[s], j);
-      const uint32_t e = (uint32_t)s * 32u + lane;
-      const bool asc = ((e & (uint32_t)k) == 0) != descending;
-      const bool keepMin = ((lane & (uint32_t)j) == 0) == asc;
-      if (keepMin ? fe_gt(c[s], n[s], oc, on) : fe_gt(oc, on, c[s], n[s])) {
-        c[s] = oc;
-        n[s] = on;
-      }
+    for (int s = 0; s < S; ++s) ones |= ((key[s] >> bit) & 1u) << s;
+    uint32_t zeros = 0;
+#pragma unroll
+    for (int s = 0; s < S; ++s) zeros += __popc(__ballot_sync(kFull, ((alive & ~ones) >> s) & 1u));
+    if (k > zeros) {
+      k -= zeros;
+      res |= 1u << bit;
+      alive &= ones;
+    } else {
+      alive &= ~ones;
     }
   }
-}
-
-template <int S>
-__device__ __forceinline__ void bitonic_sort(float (&c)[S], uint32_t (&n)[S], bool descending, uint32_t lane) {
-#pragma unroll
-  for (int k = 2; k <= S * 32; k <<= 1) {
-#pragma unroll
-    for (int j = k >> 1; j > 0; j >>= 1) bitonic_stage<S>(c, n, j, k, descending, lane);
-  }
+  return res;
 }
 
 // Per-warp buffer of a round's children (up to 256 entries; blocks of up to kRankWarps warps).
@@ -495,21 +484,58 @@ __device__ __forceinline__ bool batched_round(const Patch &p, BatchedSearch &st,
     }
     st.haveRec = true;
   } else {
-    // Overflow: sort all children and keep the 128 lowest in (cost, node) order.
-    float c8[2 * kFrontier];
-    uint32_t n8[2 * kFrontier];
+    // Overflow: keep the 128 lowest children in (cost, node) order. The frontier is unordered, so
+    // only that set matters: select the 128th smallest cost, then, among the children at that cost
+    // (siblings share their parent's), the lowest nodes up to 128 entries; the kept entries are
+    // compacted to the front of the buffer.
+    uint32_t key[2 * kFrontier], nd[2 * kFrontier];
+    uint32_t in = 0;  // bit s: slot s holds a child
 #pragma unroll
     for (int s = 0; s < 2 * kFrontier; ++s) {
       const uint32_t e = (uint32_t)s * 32u + lane;
-      const uint2 v = e < m ? buf[e] : make_uint2(__float_as_uint(kInf), kNone);
-      c8[s] = __uint_as_float(v.x);
-      n8[s] = v.y;
+      const uint2 v = e < m ? buf[e] : make_uint2(0u, kNone);
+      in |= (e < m ? 1u : 0u) << s;
+      key[s] = f2ord(__uint_as_float(v.x));
+      nd[s] = v.y;
     }
-    bitonic_sort<2 * kFrontier>(c8, n8, false, lane);
+    __syncwarp();
+    const uint32_t tc = warp_select_kth<2 * kFrontier>(key, in, kFrontierCap);
+    uint32_t below = 0, tie = 0;
+#pragma unroll
+    for (int s = 0; s < 2 * kFrontier; ++s) {
+      below += __popc(__ballot_sync(kFull, ((in >> s) & 1u) && key[s] < tc));
+      tie |= (((in >> s) & 1u) && key[s] == tc ? 1u : 0u) << s;
+    }
+    uint32_t ties = 0;
+#pragma unroll
+    for (int s = 0; s < 2 * kFrontier; ++s) ties += __popc(__ballot_sync(kFull, (tie >> s) & 1u));
+    const uint32_t need = kFrontierCap - below;  // 1 <= need <= ties
+    uint32_t tn = 0xFFFFFFFFu;                    // largest node kept at cost tc
+    if (need < ties) {
+      if (need == 1u) {
+        uint32_t nl = 0xFFFFFFFFu;
+#pragma unroll
+        for (int s = 0; s < 2 * kFrontier; ++s)
+          if ((tie >> s) & 1u) nl = min(nl, nd[s]);
+        tn = __reduce_min_sync(kFull, nl);
+      } else {
+        tn = warp_select_kth<2 * kFrontier>(nd, tie, need);
+      }
+    }
+    uint32_t pos = 0;
+#pragma unroll
+    for (int s = 0; s < 2 * kFrontier; ++s) {
+      const bool keep = ((in >> s) & 1u) && (key[s] < tc || (((tie >> s) & 1u) && nd[s] <= tn));
+      const uint32_t km = __ballot_sync(kFull, keep);
+      if (keep) buf[pos + __popc(km & ltMask)] = make_uint2(__float_as_uint(ord2f(key[s])), nd[s]);
+      pos += __popc(km);
+    }
+    __syncwarp();
 #pragma unroll
     for (int s = 0; s < kFrontier; ++s) {
-      st.fc[s] = c8[s];
-      st.fn[s] = n8[s];
+      const uint2 v = buf[(uint32_t)s * 32u + lane];
+      st.fc[s] = __uint_as_float(v.x);
+      st.fn[s] = v.y;
     }
     ctr.overflow += m - kFrontierCap;
     st.used = kFrontier;
