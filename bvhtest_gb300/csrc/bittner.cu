@@ -48,7 +48,9 @@ __global__ void patch_kernel(const bvhgb_node *__restrict__ t, uint32_t root, co
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= chunkSize) return;
   const uint32_t pos = offsetAccess ? k * numChunks + chunk : chunk * chunkSize + k;
+  PatchData pd;
   Patch p;
+  p.d = &pd;
   p.t = t;
   p.root = root;
   p.numNodes = numNodes;
@@ -72,9 +74,9 @@ __global__ void patch_kernel(const bvhgb_node *__restrict__ t, uint32_t root, co
   toFix[3 * k + 2] = ok ? un[1] : kNone;
 #pragma unroll
   for (int s = 0; s < NSLOT; ++s) {
-    out[k].nd[s] = p.nd[s];
-    out[k].idx[s] = ok ? p.idx[s] : kNone;
-    if (ok && p.idx[s] != kNone) atomicMin(&owner[p.idx[s]], k);
+    out[k].nd[s] = p.d->nd[s];
+    out[k].idx[s] = ok ? p.d->idx[s] : kNone;
+    if (ok && p.d->idx[s] != kNone) atomicMin(&owner[p.d->idx[s]], k);
   }
   if (!ok) atomicAdd(&stats[S_INVALID], 1ull);
   if (ctr.overflow) atomicAdd(&stats[S_OVERFLOW], (unsigned long long)ctr.overflow);
@@ -226,6 +228,7 @@ __global__ void __launch_bounds__(kWarpItemsPerBlock * 32) gain_warp_kernel(
   const uint32_t lane = threadIdx.x & 31u;
   if (k >= n) return;  // whole warps leave together
   Patch p;
+  p.d = warp_patch_data();
   p.t = t;
   p.root = root;
   p.numNodes = numNodes;

@@ -60,12 +60,19 @@ __device__ __forceinline__ Box tree_box(const bvhgb_node *t, uint32_t x) {
 __device__ __forceinline__ float tree_sa(const bvhgb_node *t, uint32_t x) { return __ldg(&t[x].surfaceArea); }
 __device__ __forceinline__ bool tree_leaf(const bvhgb_node *t, uint32_t x) { return __ldg(&t[x].isLeafFlag) != 0; }
 
-// BVHPatch (BVHPatch.hpp:87-335), ENABLE_AABB_PATH = 0.
-struct Patch {
+// The storage of a BVHPatch: its node slots and patched boxes. Every lane of a warp that runs one
+// item holds the same patch, so the warp kernels keep one copy per warp in shared memory (a copy
+// per lane would not fit L1); the thread-per-item kernel keeps its own.
+struct PatchData {
   NodeP nd[NSLOT];
   uint32_t idx[NSLOT];
   uint32_t apath[4];
   Box abox[4];
+};
+
+// BVHPatch (BVHPatch.hpp:87-335), ENABLE_AABB_PATH = 0.
+struct Patch {
+  PatchData *d;
   const bvhgb_node *t;
   uint32_t root;
   uint32_t numNodes;
@@ -79,40 +86,40 @@ struct Patch {
 
   __device__ void clear() {
 #pragma unroll
-    for (int i = 0; i < NSLOT; ++i) idx[i] = kNone;
+    for (int i = 0; i < NSLOT; ++i) d->idx[i] = kNone;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) apath[i] = kNone;
+    for (int i = 0; i < 4; ++i) d->apath[i] = kNone;
   }
   __device__ uint32_t index_subset(uint32_t x) const {
-    if (idx[0] == x) return 0;
-    if (idx[1] == kNone) return kNone;
-    if (idx[1] == x) return 1;
-    if (idx[2] == x) return 2;
-    if (idx[3] == x) return 3;
+    if (d->idx[0] == x) return 0;
+    if (d->idx[1] == kNone) return kNone;
+    if (d->idx[1] == x) return 1;
+    if (d->idx[2] == x) return 2;
+    if (d->idx[3] == x) return 3;
     return kNone;
   }
   __device__ uint32_t index(uint32_t x) const {
     for (uint32_t i = 0; i < NSLOT; ++i)
-      if (idx[i] == x) return i;
+      if (d->idx[i] == x) return i;
     return kNone;
   }
   __device__ NodeP get(uint32_t x) const {
     uint32_t i = index(x);
-    return i == kNone ? tree_node(t, chk(x)) : nd[i];
+    return i == kNone ? tree_node(t, chk(x)) : d->nd[i];
   }
   __device__ NodeP get_subset(uint32_t x) const {
     uint32_t i = index_subset(x);
-    return i == kNone ? tree_node(t, chk(x)) : nd[i];
+    return i == kNone ? tree_node(t, chk(x)) : d->nd[i];
   }
   __device__ uint32_t patch_node(uint32_t x, uint32_t slot) {
-    idx[slot] = x;
-    nd[slot] = tree_node(t, chk(x));
+    d->idx[slot] = x;
+    d->nd[slot] = tree_node(t, chk(x));
     return slot;
   }
   __device__ uint32_t move(uint32_t from, uint32_t to) {
-    idx[to] = idx[from];
-    idx[from] = kNone;
-    nd[to] = nd[from];
+    d->idx[to] = d->idx[from];
+    d->idx[from] = kNone;
+    d->nd[to] = d->nd[from];
     return to;
   }
   __device__ uint32_t sibling(const NodeP &n) const {
@@ -124,7 +131,7 @@ struct Patch {
                                    Box &b) const {
     const uint32_t i = index_subset(x);
     if (i != kNone) {
-      n = nd[i];
+      n = d->nd[i];
     } else {
       n.parent = __float_as_uint(m.z);
       n.left = __float_as_uint(m.w);
@@ -134,8 +141,8 @@ struct Patch {
       n.isLeft = (uint16_t)(fl >> 16);
     }
     for (int k = 0; k < 4; ++k) {
-      if (apath[k] == x) {
-        b = abox[k];
+      if (d->apath[k] == x) {
+        b = d->abox[k];
         return;
       }
     }
@@ -144,7 +151,7 @@ struct Patch {
   }
   __device__ Box get_aabb(uint32_t x) const {
     for (int i = 0; i < 4; ++i)
-      if (apath[i] == x) return abox[i];
+      if (d->apath[i] == x) return d->abox[i];
     return tree_box(t, chk(x));
   }
   // patchAABBFrom (BVHPatch.hpp:293-316)
@@ -157,8 +164,8 @@ struct Patch {
       uint32_t sib = lastLeft ? n.right : n.left;
       Box sb = get_aabb(sib);
       merge_into(b, sb);
-      abox[pidx * 2 + i] = b;
-      apath[pidx * 2 + i] = ni;
+      d->abox[pidx * 2 + i] = b;
+      d->apath[pidx * 2 + i] = ni;
       lastLeft = n.isLeft != 0;
       if (ni == root) break;
       ni = n.parent;
@@ -276,23 +283,23 @@ __device__ uint32_t find_node(const Patch &p, uint32_t n, const Heap &pq, uint32
 __device__ bool remove_node(Patch &p, uint32_t x, uint32_t ins[2], uint32_t un[2], uint32_t &g_out) {
   if (tree_leaf(p.t, p.chk(x)) || x == p.root) return false;
   const uint32_t sn = p.patch_node(x, P_NODE);
-  const uint32_t s = p.sibling(p.nd[sn]);
-  const uint32_t pi = p.nd[sn].parent;
+  const uint32_t s = p.sibling(p.d->nd[sn]);
+  const uint32_t pi = p.d->nd[sn].parent;
   if (pi == p.root) return false;
   const uint32_t ss = p.patch_node(s, P_SIBLING);
   const uint32_t sp = p.patch_node(pi, P_PARENT);
-  const uint32_t gi = p.nd[sp].parent;
+  const uint32_t gi = p.d->nd[sp].parent;
   const uint32_t sg = p.patch_node(gi, P_GRAND_PARENT);
-  if (p.nd[sp].isLeft) {
-    p.nd[sg].left = s;
-    p.nd[ss].isLeft = 1;
+  if (p.d->nd[sp].isLeft) {
+    p.d->nd[sg].left = s;
+    p.d->nd[ss].isLeft = 1;
   } else {
-    p.nd[sg].right = s;
-    p.nd[ss].isLeft = 0;
+    p.d->nd[sg].right = s;
+    p.d->nd[ss].isLeft = 0;
   }
-  p.nd[ss].parent = gi;
+  p.d->nd[ss].parent = gi;
   p.patch_aabb_from(gi, 0);
-  const uint32_t l = p.nd[sn].left, r = p.nd[sn].right;
+  const uint32_t l = p.d->nd[sn].left, r = p.d->nd[sn].right;
   if (tree_sa(p.t, p.chk(l)) > tree_sa(p.t, p.chk(r))) { ins[0] = l; ins[1] = r; }
   else { ins[0] = r; ins[1] = l; }
   un[0] = x;
@@ -547,6 +554,7 @@ __device__ __forceinline__ bool batched_round(const Patch &p, BatchedSearch &st,
 // findNode1's cost model in batched rounds (every lane of the warp calls it with the same patch).
 __device__ uint32_t find_node_batched(const Patch &p, uint32_t n, SearchCounters &ctr) {
   const uint32_t lane = threadIdx.x & 31u;
+  __syncwarp();  // the warp's patch writes are visible to every lane
   const float kInf = __int_as_float(0x7f800000);
   const Box nbox = tree_box(p.t, p.chk(n));
   const float sarea = tree_sa(p.t, p.chk(n));
@@ -575,6 +583,7 @@ __device__ uint32_t find_node_batched(const Patch &p, uint32_t n, SearchCounters
                                      : batched_round<kFrontier>(p, st, nbox, sarea, buf, ctr);
     if (!more) break;
   }
+  __syncwarp();  // every lane is done reading the patch before it changes again
   p.bad = __any_sync(kFull, p.bad);
   return st.best;
 }
@@ -592,24 +601,24 @@ __device__ bool reinsert(Patch &p, uint32_t x, uint32_t unused, bool update, con
   else sb = p.move(bpi, update ? P_1ST_BEST : P_2ND_BEST);
   const uint32_t sx = p.patch_node(x, update ? P_1ST_INSERT : P_2ND_INSERT);
   const uint32_t su = update ? P_NODE : P_PARENT;
-  const uint32_t ri = p.nd[sb].parent;
+  const uint32_t ri = p.d->nd[sb].parent;
   const uint32_t rpi = p.index(ri);
   const uint32_t sr = rpi == kNone ? p.patch_node(ri, update ? P_1ST_ROOT : P_2ND_ROOT)
                                    : p.move(rpi, update ? P_1ST_ROOT : P_2ND_ROOT);
-  if (p.nd[sb].isLeft) {
-    p.nd[sr].left = unused;
-    p.nd[su].isLeft = 1;
+  if (p.d->nd[sb].isLeft) {
+    p.d->nd[sr].left = unused;
+    p.d->nd[su].isLeft = 1;
   } else {
-    p.nd[sr].right = unused;
-    p.nd[su].isLeft = 0;
+    p.d->nd[sr].right = unused;
+    p.d->nd[su].isLeft = 0;
   }
-  p.nd[su].parent = ri;
-  p.nd[su].left = best;
-  p.nd[su].right = x;
-  p.nd[sb].parent = unused;
-  p.nd[sb].isLeft = 1;
-  p.nd[sx].parent = unused;
-  p.nd[sx].isLeft = 0;
+  p.d->nd[su].parent = ri;
+  p.d->nd[su].left = best;
+  p.d->nd[su].right = x;
+  p.d->nd[sb].parent = unused;
+  p.d->nd[sb].isLeft = 1;
+  p.d->nd[sx].parent = unused;
+  p.d->nd[sx].isLeft = 0;
   if (update) p.patch_aabb_from(unused, 1);
   return true;
 }
@@ -621,6 +630,12 @@ __device__ bool reinsert(Patch &p, uint32_t x, uint32_t unused, bool update, con
 
 constexpr int kWarpItemsPerBlock = 4;
 
+// The patch storage of this warp (blocks of kWarpItemsPerBlock warps).
+__device__ __forceinline__ PatchData *warp_patch_data() {
+  __shared__ PatchData pd[kWarpItemsPerBlock];
+  return &pd[(threadIdx.x >> 5) & (kWarpItemsPerBlock - 1)];
+}
+
 // kRemoveAndReinsert for one item on a whole warp (batched search); lane 0 publishes.
 __device__ __forceinline__ void warp_patch_item(const bvhgb_node *__restrict__ t, uint32_t root, uint32_t numNodes,
                                                 uint32_t node, bool ok, uint32_t rank, PatchOut *__restrict__ out,
@@ -629,6 +644,7 @@ __device__ __forceinline__ void warp_patch_item(const bvhgb_node *__restrict__ t
                                                 uint32_t *__restrict__ err) {
   const uint32_t lane = threadIdx.x & 31u;
   Patch p;
+  p.d = warp_patch_data();
   p.t = t;
   p.root = root;
   p.numNodes = numNodes;
@@ -641,6 +657,7 @@ __device__ __forceinline__ void warp_patch_item(const bvhgb_node *__restrict__ t
   ok = ok && reinsert<true>(p, ins[0], un[0], true, unused, 0, ctr);
   ok = ok && reinsert<true>(p, ins[1], un[1], false, unused, 0, ctr);
   if (p.bad) ok = false;
+  __syncwarp();
   if (lane != 0) return;
   if (p.bad) atomicOr(err, kErrBadIndex);
   *valid = ok ? 1u : 0u;
@@ -649,9 +666,9 @@ __device__ __forceinline__ void warp_patch_item(const bvhgb_node *__restrict__ t
   toFix3[2] = ok ? un[1] : kNone;
 #pragma unroll
   for (int s = 0; s < NSLOT; ++s) {
-    out->nd[s] = p.nd[s];
-    out->idx[s] = ok ? p.idx[s] : kNone;
-    if (ok && p.idx[s] != kNone) atomicMin(&owner[p.idx[s]], rank);
+    out->nd[s] = p.d->nd[s];
+    out->idx[s] = ok ? p.d->idx[s] : kNone;
+    if (ok && p.d->idx[s] != kNone) atomicMin(&owner[p.d->idx[s]], rank);
   }
   if (!ok) atomicAdd(&stats[S_INVALID], 1ull);
   if (ctr.overflow) atomicAdd(&stats[S_OVERFLOW], (unsigned long long)ctr.overflow);
