@@ -470,36 +470,39 @@ __device__ __forceinline__ float clamp64(float v) { return fminf(fmaxf(v, -64.0f
 __device__ __forceinline__ float nan0(float v) { return isnan(v) ? 0.0f : v; }
 __device__ __forceinline__ uint32_t rank_bin(float v) { return f2ord(v) >> 16; }
 
-// Depth by pointer jumping: after r rounds anc[x] is the 2^r-th ancestor of x, or the root, and
-// dep[x] the distance to it, so kDepthRounds rounds give min(depth, 2^kDepthRounds) exactly.
+// Depth by pointer jumping on ad[x] = distance << 32 | ancestor: each round replaces a node's
+// ancestor a by a's own (ad[a] read whole, so the pair is always an ancestor and its distance,
+// whichever round wrote it). A round reaches at least as far as a synchronous one, so after r
+// rounds a node's ancestor is the root or at least 2^r levels up, and kDepthRounds rounds give
+// min(depth, 2^kDepthRounds) exactly. Only inner nodes jump (a leaf is nobody's ancestor and its
+// depth is not a feature); a node whose ancestor is the root is done.
 // One coalesced pass over the nodes: the depth recursion's start, and compact copies of every
 // node's surface area and parent (bit 31: the node is a leaf) that the leaf counts and the feature
 // rows gather from (33 MB per 8M nodes each, so they stay in L2 where the 48-byte records do not).
 constexpr uint32_t kLeafBit = 0x80000000u;
-__global__ void depth_init_kernel(const bvhgb_node *__restrict__ t, uint32_t n, uint32_t root, uint32_t *__restrict__ anc,
-                                  uint32_t *__restrict__ dep, float *__restrict__ sa, uint32_t *__restrict__ par) {
+__global__ void depth_init_kernel(const bvhgb_node *__restrict__ t, uint32_t n, uint32_t root,
+                                  unsigned long long *__restrict__ ad, float *__restrict__ sa,
+                                  uint32_t *__restrict__ par) {
   for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
     const float4 w1 = __ldg(reinterpret_cast<const float4 *>(t + x) + 1);  // mx.y mx.z parent left
     const float4 w2 = __ldg(reinterpret_cast<const float4 *>(t + x) + 2);  // right flags level sa
     const uint32_t p = __float_as_uint(w1.z);
-    anc[x] = (x == root || p >= n) ? root : p;
-    dep[x] = x == root ? 0u : 1u;
+    const uint32_t a = (x == root || p >= n) ? root : p;
+    ad[x] = ((unsigned long long)(x == root ? 0u : 1u) << 32) | a;
     sa[x] = w2.w;
     par[x] = (p & ~kLeafBit) | ((__float_as_uint(w2.y) & 0xFFFFu) ? kLeafBit : 0u);
   }
 }
-__global__ void depth_jump_kernel(uint32_t n, uint32_t root, const uint32_t *__restrict__ ancIn,
-                                  const uint32_t *__restrict__ depIn, uint32_t *__restrict__ ancOut,
-                                  uint32_t *__restrict__ depOut) {
-  for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
-    const uint32_t a = ancIn[x];
-    if (a == root) {
-      ancOut[x] = a;
-      depOut[x] = depIn[x];
-    } else {
-      ancOut[x] = ancIn[a];
-      depOut[x] = depIn[x] + depIn[a];
-    }
+__global__ void depth_jump_kernel(const uint32_t *__restrict__ inner, uint32_t numInner, uint32_t n, uint32_t root,
+                                  unsigned long long *ad) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < numInner; i += gridDim.x * blockDim.x) {
+    const uint32_t x = __ldg(inner + i);
+    if (x >= n) continue;  // flagged by the feature rows
+    const unsigned long long v = __ldcg(ad + x);
+    const uint32_t a = (uint32_t)v;
+    if (a == root || a >= n) continue;
+    const unsigned long long w = __ldcg(ad + a);
+    __stcg(ad + x, (((v >> 32) + (w >> 32)) << 32) | (w & 0xFFFFFFFFull));
   }
 }
 // Leaf counts bottom-up. A leaf starts a climb with count 1; at each parent the two arrivals add
@@ -533,16 +536,31 @@ __global__ void leaf_count_kernel(const uint32_t *__restrict__ par, uint32_t n, 
   }
 }
 
-// Raw features and the four rank histograms. The loop is warp-uniform so that the lanes of a warp
-// that fall into the same histogram bin add their count with one atomic (the values of neighbouring
-// nodes are alike, so a few bins are hot).
+__device__ __forceinline__ uint32_t bf16_bits(float v) {
+  return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v));
+}
+__device__ __forceinline__ uint32_t bf16_pair(float lo, float hi) { return bf16_bits(lo) | (bf16_bits(hi) << 16); }
+
+// The rank histograms: kHistCopies copies of the four count histograms (a block adds into copy
+// blockIdx % kHistCopies, so that the few hot bins are not one address for the whole grid), summed
+// into copy 0 before the scan, then the four exclusive prefixes.
+constexpr uint32_t kHistCopies = 16;
+constexpr size_t kHistPrefix = (size_t)kHistCopies * 4 * kRankBins;  // offset of the prefixes
+constexpr size_t kHistWords = kHistPrefix + 4 * kRankBins;
+
+// Raw features and the four rank histograms. A feature row is three 16-byte blocks: features 0-7 and
+// the zero padding 16-23 are final here and stored at once; the middle block (features 8-9 and
+// the four ranks) waits for the histograms, so features 8-9 and the rank bins go to pend[i]. The
+// loop is warp-uniform so that the lanes of a warp that fall into the same histogram bin add their
+// count with one atomic (the values of neighbouring nodes are alike, so a few bins are hot).
 __global__ void features_raw_kernel(const bvhgb_node *__restrict__ t, const uint32_t *__restrict__ inner,
                                     uint32_t numInner, uint32_t numNodes, uint32_t root,
-                                    const uint32_t *__restrict__ depth, const uint32_t *__restrict__ leafCount,
+                                    const unsigned long long *__restrict__ depth, const uint32_t *__restrict__ leafCount,
                                     const float *__restrict__ saOf, const uint32_t *__restrict__ par,
-                                    float invLog2Leaves, float *__restrict__ raw, float *__restrict__ src,
+                                    float invLog2Leaves, uint16_t *__restrict__ rows, uint4 *__restrict__ pend,
                                     uint32_t *__restrict__ hist, uint32_t *__restrict__ err) {
   const float sroot = __ldg(saOf + root);
+  uint32_t *hc = hist + (size_t)(blockIdx.x % kHistCopies) * 4 * kRankBins;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t base = blockIdx.x * blockDim.x; base < numInner; base += stride) {
@@ -550,11 +568,12 @@ __global__ void features_raw_kernel(const bvhgb_node *__restrict__ t, const uint
     const bool live = i < numInner;
     float s4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     if (live) {
+      float f[kMlpRaw];
+#pragma unroll
+      for (int k = 0; k < kMlpRaw; ++k) f[k] = 0.0f;
       const uint32_t x = __ldg(inner + i);
       if (x >= numNodes) {  // not a node: a zero row, flagged
         atomicOr(err, kErrBadIndex);
-#pragma unroll
-        for (int k = 0; k < kMlpRaw; ++k) raw[(size_t)i * kMlpRaw + k] = 0.0f;
       } else {
         const float4 w1 = __ldg(reinterpret_cast<const float4 *>(t + x) + 1);  // mx.y mx.z parent left
         const float4 w2 = __ldg(reinterpret_cast<const float4 *>(t + x) + 2);  // right flags level sa
@@ -566,8 +585,7 @@ __global__ void features_raw_kernel(const bvhgb_node *__restrict__ t, const uint
         const float mn = sl < sr ? sl : sr;
         const float sum = fadd(sl, sr);
         const float cost = fdiv(fmul(fmul(fmul(sa, sa), sa), 2.0f), fmul(sum, mn));  // kCalcCost
-        const uint32_t d = min(depth[x], 1u << kDepthRounds);
-        float f[kMlpRaw];
+        const uint32_t d = (uint32_t)min(depth[x] >> 32, 1ull << kDepthRounds);
         f[0] = log2f(sa);
         f[1] = fdiv(sa, __ldg(saOf + p));
         f[2] = fdiv(sa, __ldg(saOf + g));
@@ -579,29 +597,52 @@ __global__ void features_raw_kernel(const bvhgb_node *__restrict__ t, const uint
         f[8] = log2f(fdiv(sa, mn));
         f[9] = log2f(cost);
 #pragma unroll
-        for (int k = 0; k < kMlpRaw; ++k) raw[(size_t)i * kMlpRaw + k] = clamp64(f[k]);
+        for (int k = 0; k < kMlpRaw; ++k) f[k] = clamp64(f[k]);
         s4[0] = nan0(cost);
         s4[1] = nan0(fdiv(sa, mn));
         s4[2] = nan0(fdiv(sa, sum));
         s4[3] = nan0(sa);
       }
-      *reinterpret_cast<float4 *>(src + (size_t)i * 4) = make_float4(s4[0], s4[1], s4[2], s4[3]);
+      static_assert(kMlpRaw == 10 && kIn == 24, "row blocks: features 0-7, 8-15 (8-9 raw, 10-13 ranks), 16-23");
+      uint4 *o = reinterpret_cast<uint4 *>(rows + (size_t)i * kIn);
+      o[0] = make_uint4(bf16_pair(f[0], f[1]), bf16_pair(f[2], f[3]), bf16_pair(f[4], f[5]), bf16_pair(f[6], f[7]));
+      o[2] = make_uint4(0u, 0u, 0u, 0u);
+      pend[i] = make_uint4(rank_bin(s4[0]) | (rank_bin(s4[1]) << 16), rank_bin(s4[2]) | (rank_bin(s4[3]) << 16),
+                           bf16_pair(f[8], f[9]), 0u);
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const uint32_t bin = live ? rank_bin(s4[q]) : 0xFFFFFFFFu;
       const uint32_t peers = __match_any_sync(0xFFFFFFFFu, bin);
-      if (live && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(hist + q * kRankBins + bin, (uint32_t)__popc(peers));
+      if (live && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(hc + q * kRankBins + bin, (uint32_t)__popc(peers));
     }
   }
 }
 
-// Exclusive prefix of each of the four histograms into the second half (one block each).
+// Copy 0 of the count histograms += the other copies.
+__global__ void hist_reduce_kernel(uint32_t *hist) {
+  constexpr uint32_t n4 = kRankBins;  // 16-byte vectors per copy (4 histograms)
+  uint4 *h = reinterpret_cast<uint4 *>(hist);
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n4; j += gridDim.x * blockDim.x) {
+    uint4 a = h[j];
+#pragma unroll
+    for (uint32_t c = 1; c < kHistCopies; ++c) {
+      const uint4 b = h[(size_t)c * n4 + j];
+      a.x += b.x;
+      a.y += b.y;
+      a.z += b.z;
+      a.w += b.w;
+    }
+    h[j] = a;
+  }
+}
+
+// Exclusive prefix of each of the four histograms (copy 0) into the prefix area (one block each).
 __global__ void __launch_bounds__(1024) hist_scan_kernel(uint32_t *hist) {
   constexpr uint32_t kPer = kRankBins / 1024;
   __shared__ uint32_t warpSum[32];
   const uint32_t *h = hist + blockIdx.x * kRankBins;
-  uint32_t *pre = hist + (4 + blockIdx.x) * kRankBins;
+  uint32_t *pre = hist + kHistPrefix + blockIdx.x * kRankBins;
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   // Each thread owns kPer consecutive bins, read (and written) as 16-byte vectors.
   static_assert(kPer % 16 == 0, "vector access");
@@ -651,36 +692,22 @@ __global__ void __launch_bounds__(1024) hist_scan_kernel(uint32_t *hist) {
   }
 }
 
-__device__ __forceinline__ uint32_t bf16_bits(float v) {
-  return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v));
-}
-
-__global__ void features_pack_kernel(const float *__restrict__ raw, const float *__restrict__ src,
-                                     const uint32_t *__restrict__ hist, uint32_t numInner, uint16_t *__restrict__ x) {
+// The middle block of each row: features 8-9 (from pend) and the four ranks (mid-rank of the row's
+// bin: the values below it plus half of those in it, over the row count).
+__global__ void features_pack_kernel(const uint4 *__restrict__ pend, const uint32_t *__restrict__ hist,
+                                     uint32_t numInner, uint16_t *__restrict__ x) {
   const float fn = (float)numInner;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < numInner; i += gridDim.x * blockDim.x) {
-    float f[kIn];
-#pragma unroll
-    for (int k = 0; k < kMlpRaw; ++k) f[k] = raw[(size_t)i * kMlpRaw + k];
-    const float4 s4 = *reinterpret_cast<const float4 *>(src + (size_t)i * 4);
-    const float sv[4] = {s4.x, s4.y, s4.z, s4.w};
+    const uint4 pd = pend[i];
+    const uint32_t bins[4] = {pd.x & 0xFFFFu, pd.x >> 16, pd.y & 0xFFFFu, pd.y >> 16};
+    float r[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const uint32_t b = rank_bin(sv[q]);
-      const float below = (float)hist[(4 + q) * kRankBins + b];
-      const float own = (float)hist[q * kRankBins + b];
-      f[kMlpRaw + q] = fdiv(fadd(below, fmul(0.5f, own)), fn);
+      const float below = (float)hist[kHistPrefix + q * kRankBins + bins[q]];
+      const float own = (float)hist[q * kRankBins + bins[q]];
+      r[q] = fdiv(fadd(below, fmul(0.5f, own)), fn);
     }
-#pragma unroll
-    for (int k = kMlpRaw + 4; k < kIn; ++k) f[k] = 0.0f;
-    uint4 *o = reinterpret_cast<uint4 *>(x + (size_t)i * kIn);
-#pragma unroll
-    for (int w = 0; w < 3; ++w) {
-      uint32_t u[4];
-#pragma unroll
-      for (int h = 0; h < 4; ++h) u[h] = bf16_bits(f[w * 8 + h * 2]) | (bf16_bits(f[w * 8 + h * 2 + 1]) << 16);
-      o[w] = make_uint4(u[0], u[1], u[2], u[3]);
-    }
+    reinterpret_cast<uint4 *>(x + (size_t)i * kIn)[1] = make_uint4(pd.z, bf16_pair(r[0], r[1]), bf16_pair(r[2], r[3]), 0u);
   }
 }
 
@@ -701,18 +728,14 @@ int lr_scratch_alloc(LrScratch &s, uint32_t numNodes) {
   lr_scratch_free(s);
   const size_t n = std::max(numNodes, 1u), ni = n / 2 + 1;
   cudaError_t e = cudaSuccess;
-  for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
-    e = cudaMalloc(&s.anc[k], 4 * n);
-    if (e == cudaSuccess) e = cudaMalloc(&s.dep[k], 4 * n);
-  }
+  e = cudaMalloc(&s.ad, 8 * n);
   if (e == cudaSuccess) e = cudaMalloc(&s.leafCount, 4 * n);
   if (e == cudaSuccess) e = cudaMalloc(&s.sa, 4 * n);
   if (e == cudaSuccess) e = cudaMalloc(&s.par, 4 * n);
   if (e == cudaSuccess) e = cudaMalloc(&s.acc, 8 * n);
   if (e == cudaSuccess) e = cudaMalloc(&s.err, 4);
-  if (e == cudaSuccess) e = cudaMalloc(&s.hist, 4ull * kRankBins * 8);
-  if (e == cudaSuccess) e = cudaMalloc(&s.raw, 4 * kMlpRaw * ni);
-  if (e == cudaSuccess) e = cudaMalloc(&s.src, 16 * ni);
+  if (e == cudaSuccess) e = cudaMalloc(&s.hist, 4 * kHistWords);
+  if (e == cudaSuccess) e = cudaMalloc(&s.pend, 16 * ni);
   if (e == cudaSuccess) e = cudaMalloc(&s.x, 2ull * kIn * ni);
   if (e == cudaSuccess) e = cudaMalloc(&s.y, 4 * ni);
   if (e == cudaSuccess) e = cudaMemset(s.err, 0, 4);
@@ -726,11 +749,8 @@ int lr_scratch_alloc(LrScratch &s, uint32_t numNodes) {
 }
 
 void lr_scratch_free(LrScratch &s) {
-  for (int k = 0; k < 2; ++k) {
-    cudaFree(s.anc[k]);
-    cudaFree(s.dep[k]);
-    s.anc[k] = s.dep[k] = nullptr;
-  }
+  cudaFree(s.ad);
+  s.ad = nullptr;
   cudaFree(s.leafCount);
   cudaFree(s.sa);
   cudaFree(s.par);
@@ -739,13 +759,13 @@ void lr_scratch_free(LrScratch &s) {
   cudaFree(s.acc);
   cudaFree(s.err);
   cudaFree(s.hist);
-  cudaFree(s.raw);
-  cudaFree(s.src);
+  cudaFree(s.pend);
   cudaFree(s.x);
   cudaFree(s.y);
   s.leafCount = s.hist = s.err = nullptr;
   s.acc = nullptr;
-  s.raw = s.src = s.y = nullptr;
+  s.pend = nullptr;
+  s.y = nullptr;
   s.x = nullptr;
   s.numNodes = 0;
 }
@@ -757,25 +777,25 @@ int lr_features(LrScratch &s, const bvhgb_node *nodes, uint32_t numNodes, uint32
   if (numNodes > s.numNodes || numInner > s.numNodes / 2 + 1) return BVHGB_TOO_LARGE;
   if (numInner == 0) return BVHGB_OK;
   const uint32_t g = grid_for(numNodes, 256);
-  depth_init_kernel<<<g, 256, 0, st>>>(nodes, numNodes, root, s.anc[0], s.dep[0], s.sa, s.par);
+  depth_init_kernel<<<g, 256, 0, st>>>(nodes, numNodes, root, s.ad, s.sa, s.par);
   BVHGB_LAUNCH_CHECK("lr depth init");
-  int cur = 0;
+  const uint32_t gi = grid_for(numInner, 256);
   for (uint32_t r = 0; r < kDepthRounds; ++r) {
-    depth_jump_kernel<<<g, 256, 0, st>>>(numNodes, root, s.anc[cur], s.dep[cur], s.anc[cur ^ 1], s.dep[cur ^ 1]);
+    depth_jump_kernel<<<gi, 256, 0, st>>>(inner, numInner, numNodes, root, s.ad);
     BVHGB_LAUNCH_CHECK("lr depth jump");
-    cur ^= 1;
   }
   BVHGB_CUDA_TRY(cudaMemsetAsync(s.acc, 0, 8ull * numNodes, st));
   leaf_count_kernel<<<g, 256, 0, st>>>(s.par, numNodes, root, s.leafCount, s.acc, lr_error_word(s));
   BVHGB_LAUNCH_CHECK("lr leaf count");
-  BVHGB_CUDA_TRY(cudaMemsetAsync(s.hist, 0, 4ull * kRankBins * 4, st));
-  const uint32_t gi = grid_for(numInner, 256);
-  features_raw_kernel<<<gi, 256, 0, st>>>(nodes, inner, numInner, numNodes, root, s.dep[cur], s.leafCount, s.sa, s.par,
-                                          invLog2Leaves, s.raw, s.src, s.hist, lr_error_word(s));
+  BVHGB_CUDA_TRY(cudaMemsetAsync(s.hist, 0, 4 * kHistPrefix, st));
+  features_raw_kernel<<<gi, 256, 0, st>>>(nodes, inner, numInner, numNodes, root, s.ad, s.leafCount, s.sa, s.par,
+                                          invLog2Leaves, s.x, s.pend, s.hist, lr_error_word(s));
   BVHGB_LAUNCH_CHECK("lr features");
+  hist_reduce_kernel<<<grid_for(kRankBins, 256), 256, 0, st>>>(s.hist);
+  BVHGB_LAUNCH_CHECK("lr rank reduce");
   hist_scan_kernel<<<4, 1024, 0, st>>>(s.hist);
   BVHGB_LAUNCH_CHECK("lr rank scan");
-  features_pack_kernel<<<gi, 256, 0, st>>>(s.raw, s.src, s.hist, numInner, s.x);
+  features_pack_kernel<<<gi, 256, 0, st>>>(s.pend, s.hist, numInner, s.x);
   BVHGB_LAUNCH_CHECK("lr features pack");
   return BVHGB_OK;
 }

@@ -20,12 +20,12 @@ constexpr float kTargetEps = 0.16f;           // target = sign(g) ln(1 + |g| num
 // Device scratch for the features of one tree (sized for numNodes nodes).
 struct LrScratch {
   uint32_t numNodes = 0;
-  uint32_t *anc[2] = {nullptr, nullptr}, *dep[2] = {nullptr, nullptr};
+  unsigned long long *ad = nullptr;  // depth pointer jumping: distance << 32 | ancestor
   uint32_t *leafCount = nullptr, *hist = nullptr, *err = nullptr;
   float *sa = nullptr;        // per-node surface area (compact copy)
   uint32_t *par = nullptr;    // per-node parent | leaf bit (compact copy)
   unsigned long long *acc = nullptr;  // leaf-count accumulators: 2^40 per arrival + the arriving count
-  float *raw = nullptr, *src = nullptr;
+  uint4 *pend = nullptr;   // per row: the four rank bins (16 bits each) and features 8-9 (BF16)
   uint16_t *x = nullptr;  // BF16 feature rows [numInner][24]
   float *y = nullptr;     // scorer output per inner node
 };
