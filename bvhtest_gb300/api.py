@@ -117,6 +117,20 @@ class LBVH:
         return k, idx
 
 
+def select_smallest_pairs(keys: torch.Tensor, vals: torch.Tensor, k: int, stream=None) -> torch.Tensor:
+    """Values of the k smallest keys (int32 tensors, keys read as unsigned) in stable ascending order:
+    the first k values of radix_sort_pairs(keys, vals)."""
+    lib = load()
+    n = keys.shape[0]
+    need = C.c_size_t(0)
+    check(lib.bvhgb_select_smallest_pairs(None, C.byref(need), None, None, None, n, k, None), "select size")
+    temp = torch.empty(max(need.value, 1), dtype=torch.uint8, device="cuda")
+    out = torch.empty(k, dtype=vals.dtype, device="cuda")
+    check(lib.bvhgb_select_smallest_pairs(_ptr(temp), C.byref(need), _ptr(keys), _ptr(vals), _ptr(out), n, k,
+                                          _stream(stream)), "bvhgb_select_smallest_pairs")
+    return out
+
+
 def radix_sort_pairs(keys: torch.Tensor, vals: torch.Tensor, begin_bit=0, end_bit=None, stream=None):
     """Stable ascending sort of (key, value) pairs; keys int32/int64 tensors read as unsigned."""
     lib = load()
@@ -215,8 +229,9 @@ class Bittner13GPU:
         return out
 
     def selection(self, stream=None) -> torch.Tensor:
-        """Node order of the most recent selection (int32, device copy, batch position order)."""
-        out = torch.empty(self.num_inner, dtype=torch.int32, device="cuda")
+        """Node order of the most recent selection (int32, device copy, batch position order): the
+        first min(batch_size, num_inner) entries, the ones the chunks process."""
+        out = torch.empty(min(self.batch_size, self.num_inner), dtype=torch.int32, device="cuda")
         check(self.lib.bvhgb_bn13_read_selection(self.ws, _ptr(out), out.shape[0], _stream(stream)),
               "bvhgb_bn13_read_selection")
         return out

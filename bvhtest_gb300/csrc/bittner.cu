@@ -266,7 +266,7 @@ using namespace bvhgb;
 struct bvhgb_bn13_workspace {
   bvhgb_bn13_config cfg{};
   uint32_t numNodes = 0, root = 0, numInner = 0, numChunks = 0, chunkSize = 0;
-  uint32_t *inner = nullptr, *keys = nullptr, *vals = nullptr, *keysSorted = nullptr, *todo = nullptr;
+  uint32_t *inner = nullptr, *keys = nullptr, *vals = nullptr, *todo = nullptr;
   void *sortTemp = nullptr;
   PatchOut *patches = nullptr;
   uint32_t *valid = nullptr, *toFix = nullptr, *owner = nullptr, *counter = nullptr, *err = nullptr;
@@ -290,6 +290,12 @@ bool learned_iteration(const bvhgb_bn13_workspace *ws, uint64_t it) {
   return ws->plainEvery == 0 || it % ws->plainEvery != ws->plainEvery - 1;
 }
 
+// Entries of the selection the chunks read: position chunk * chunkSize + k (or k * numChunks +
+// chunk) for k < chunkSize, so the first numChunks * chunkSize (at most every inner node).
+uint32_t selection_count(const bvhgb_bn13_workspace *ws) {
+  return (uint32_t)std::min<uint64_t>((uint64_t)ws->numChunks * ws->chunkSize, ws->numInner);
+}
+
 void drop_graphs(bvhgb_bn13_workspace *ws) {
   for (auto &g : ws->graph) {
     if (g) cudaGraphExecDestroy(g);
@@ -310,7 +316,9 @@ int select_kind(bvhgb_bn13_workspace *ws, const bvhgb_node *nodes, bool learned,
     cost_kernel<<<grid, 256, 0, s>>>(nodes, ws->inner, ws->numInner, ws->keys, ws->vals);
     BVHGB_LAUNCH_CHECK("bn13 cost");
   }
-  return sort_pairs(ws->sortTemp, ws->keys, ws->keysSorted, ws->vals, ws->todo, ws->numInner, 4, 0, 32, s);
+  // bn13_selectNodes sorts every inner node (Bittner13CUDA.cu:659-726); the chunks read only the
+  // first selection_count entries, which a stable selection gives in the same order.
+  return select_smallest(ws->sortTemp, ws->keys, ws->vals, ws->numInner, selection_count(ws), ws->todo, s);
 }
 
 int select_nodes(bvhgb_bn13_workspace *ws, const bvhgb_node *nodes, cudaStream_t s) {
@@ -451,11 +459,10 @@ extern "C" BVHGB_API int bvhgb_bn13_create(const bvhgb_node *nodes, uint32_t num
   ws->numInner = (uint32_t)inner.size();
   const size_t ni = inner.size() ? inner.size() : 1;
   const size_t cs = ws->chunkSize ? ws->chunkSize : 1;
-  const size_t sortBytes = sort_temp_bytes(ws->numInner, 4, 0, 32);
+  const size_t sortBytes = select_temp_bytes(ws->numInner, selection_count(ws));
   if (e == cudaSuccess) e = cudaMalloc(&ws->inner, 4 * ni);
   if (e == cudaSuccess) e = cudaMalloc(&ws->keys, 4 * ni);
   if (e == cudaSuccess) e = cudaMalloc(&ws->vals, 4 * ni);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->keysSorted, 4 * ni);
   if (e == cudaSuccess) e = cudaMalloc(&ws->todo, 4 * ni);
   if (e == cudaSuccess) e = cudaMalloc(&ws->sortTemp, sortBytes ? sortBytes : 256);
   if (e == cudaSuccess) e = cudaMalloc(&ws->patches, sizeof(PatchOut) * cs);
@@ -500,7 +507,6 @@ extern "C" BVHGB_API int bvhgb_bn13_destroy(bvhgb_bn13_workspace *ws) {
   cudaFree(ws->inner);
   cudaFree(ws->keys);
   cudaFree(ws->vals);
-  cudaFree(ws->keysSorted);
   cudaFree(ws->todo);
   cudaFree(ws->sortTemp);
   cudaFree(ws->patches);
@@ -639,9 +645,9 @@ extern "C" BVHGB_API int bvhgb_bn13_set_iteration(bvhgb_bn13_workspace *ws, uint
 extern "C" BVHGB_API int bvhgb_bn13_read_selection(const bvhgb_bn13_workspace *ws, uint32_t *out, uint32_t capacity,
                                                   bvhgb_stream stream) {
   if (!ws || !out) return BVHGB_INVALID_ARGUMENT;
-  if (capacity < ws->numInner) return BVHGB_TOO_LARGE;
-  if (ws->numInner)
-    BVHGB_CUDA_TRY(cudaMemcpyAsync(out, ws->todo, 4ull * ws->numInner, cudaMemcpyDeviceToDevice, as_stream(stream)));
+  const uint32_t n = selection_count(ws);
+  if (capacity < n) return BVHGB_TOO_LARGE;
+  if (n) BVHGB_CUDA_TRY(cudaMemcpyAsync(out, ws->todo, 4ull * n, cudaMemcpyDeviceToDevice, as_stream(stream)));
   return BVHGB_OK;
 }
 

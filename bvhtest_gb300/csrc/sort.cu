@@ -370,6 +370,258 @@ int sort_pairs(void *temp, const void *keysIn, void *keysOut, const uint32_t *va
                              valsIn, valsOut, n, beginBit, endBit, s);
 }
 
+
+// ---- stable selection of the k smallest keys ------------------------------------------------------
+//
+// The first k pairs of a stable ascending sort of (keys, vals), without sorting all n: a radix
+// selection finds the k-th smallest key T (three histogram passes over 11, 11 and 10 bits, each
+// counting only the keys that match the digits found so far), a stable compaction keeps the keys
+// below T and, of those equal to T, the first ones in index order up to k in all, and the k kept
+// pairs are sorted. The compaction keeps index order, so the stable sort of the kept pairs is the
+// prefix of the stable sort of all pairs.
+namespace {
+
+constexpr uint32_t kSelBins = 2048;
+constexpr uint32_t kSelTile = 4096;        // keys per compaction tile (256 threads x 16)
+__host__ __device__ constexpr uint32_t sel_shift(int pass) { return pass == 0 ? 21u : pass == 1 ? 10u : 0u; }
+__host__ __device__ constexpr uint32_t sel_bits(int pass) { return pass == 2 ? 10u : 11u; }
+
+struct SelState {
+  uint32_t prefix;  // the digits of T found so far
+  uint32_t below;   // keys below every key with that prefix
+};
+
+struct SelLayout {
+  size_t state, hist, tileLt, tileEq, keys, vals, keysOut, sortTemp, total;
+  uint32_t tiles;
+};
+
+SelLayout make_sel_layout(uint32_t n, uint32_t k) {
+  SelLayout L{};
+  auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
+  L.tiles = ceil_div(max(n, 1u), kSelTile);
+  size_t o = 0;
+  L.state = o; o = up(o + sizeof(SelState));
+  L.hist = o; o = up(o + 4ull * kSelBins);
+  L.tileLt = o; o = up(o + 4ull * L.tiles);
+  L.tileEq = o; o = up(o + 4ull * L.tiles);
+  L.keys = o; o = up(o + 4ull * k);
+  L.vals = o; o = up(o + 4ull * k);
+  L.keysOut = o; o = up(o + 4ull * k);
+  L.sortTemp = o; o = up(o + sort_temp_bytes(k, 4, 0, 32));
+  L.total = o;
+  return L;
+}
+
+// Histogram of digit 'pass' of the keys whose higher digits equal the prefix found so far (the lanes
+// of a warp with the same bin add together; the block's counts go out once).
+__global__ void __launch_bounds__(512) select_hist_kernel(const uint32_t *__restrict__ keys, uint32_t n,
+                                                          const SelState *__restrict__ st, uint32_t *__restrict__ hist,
+                                                          int pass) {
+  __shared__ uint32_t sh[kSelBins];
+  for (uint32_t b = threadIdx.x; b < kSelBins; b += blockDim.x) sh[b] = 0;
+  __syncthreads();
+  const uint32_t shift = sel_shift(pass), mask = (1u << sel_bits(pass)) - 1u, hi = shift + sel_bits(pass);
+  const uint32_t prefix = pass ? st->prefix : 0u;
+  const uint32_t lane = threadIdx.x & 31u;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {  // warp-uniform
+    const uint32_t i = base + threadIdx.x;
+    uint32_t bin = 0xFFFFFFFFu;
+    if (i < n) {
+      const uint32_t key = __ldg(keys + i);
+      if (pass == 0 || (key >> hi) == prefix) bin = (key >> shift) & mask;
+    }
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, bin);
+    if (bin != 0xFFFFFFFFu && (peers & ((1u << lane) - 1u)) == 0u) atomicAdd(&sh[bin], (uint32_t)__popc(peers));
+  }
+  __syncthreads();
+  for (uint32_t b = threadIdx.x; b < kSelBins; b += blockDim.x)
+    if (sh[b]) atomicAdd(&hist[b], sh[b]);
+}
+
+// Block-wide exclusive sum (blocks of up to 1024 threads); *total receives the sum.
+__device__ __forceinline__ uint32_t block_exclusive_sum(uint32_t v, uint32_t *warpSums, uint32_t &total) {
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, warps = (blockDim.x + 31u) >> 5;
+  uint32_t inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+    if (lane >= (uint32_t)o) inc += t;
+  }
+  if (lane == 31u) warpSums[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t w = lane < warps ? warpSums[lane] : 0u;
+    uint32_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+      if (lane >= (uint32_t)o) wi += t;
+    }
+    warpSums[lane] = wi - w;
+    if (lane == 31u) warpSums[32] = wi;
+  }
+  __syncthreads();
+  total = warpSums[32];
+  const uint32_t r = warpSums[warp] + inc - v;
+  __syncthreads();  // warpSums may be reused
+  return r;
+}
+
+// The bin of digit 'pass' that holds the k-th smallest key: the prefix and the count below it
+// advance; the histogram is cleared for the next pass. One block of 1024 threads, 2 bins each.
+__global__ void __launch_bounds__(1024) select_find_kernel(SelState *st, uint32_t *hist, uint32_t k, int pass) {
+  __shared__ uint32_t warpSums[33];
+  const uint32_t b0 = 2u * threadIdx.x;
+  const uint32_t h0 = hist[b0], h1 = hist[b0 + 1];
+  const uint32_t below = pass ? st->below : 0u, prefix = pass ? st->prefix : 0u;
+  uint32_t total;
+  const uint32_t ex = block_exclusive_sum(h0 + h1, warpSums, total);
+  const uint32_t need = k - below;  // rank (from 1) of the wanted key among those with the prefix
+  int bin = -1;
+  uint32_t exb = 0;
+  if (ex < need && need <= ex + h0) {
+    bin = (int)b0;
+    exb = ex;
+  } else if (ex + h0 < need && need <= ex + h0 + h1) {
+    bin = (int)b0 + 1;
+    exb = ex + h0;
+  }
+  __syncthreads();  // every thread has read the state
+  if (bin >= 0) {
+    st->prefix = (prefix << sel_bits(pass)) | (uint32_t)bin;
+    st->below = below + exb;
+  }
+  hist[b0] = 0u;
+  hist[b0 + 1] = 0u;
+}
+
+// Per tile: keys below T and keys equal to T.
+__global__ void __launch_bounds__(256) select_count_kernel(const uint32_t *__restrict__ keys, uint32_t n,
+                                                           const SelState *__restrict__ st, uint32_t *__restrict__ tileLt,
+                                                           uint32_t *__restrict__ tileEq) {
+  __shared__ uint32_t warpSums[33];
+  const uint32_t T = st->prefix;
+  const size_t base = (size_t)blockIdx.x * kSelTile;
+  uint32_t lt = 0, eq = 0;
+  for (uint32_t j = threadIdx.x; j < kSelTile; j += blockDim.x) {
+    const size_t i = base + j;
+    if (i < n) {
+      const uint32_t key = __ldg(keys + i);
+      lt += key < T ? 1u : 0u;
+      eq += key == T ? 1u : 0u;
+    }
+  }
+  uint32_t totLt, totEq;
+  block_exclusive_sum(lt, warpSums, totLt);
+  block_exclusive_sum(eq, warpSums, totEq);
+  if (threadIdx.x == 0) {
+    tileLt[blockIdx.x] = totLt;
+    tileEq[blockIdx.x] = totEq;
+  }
+}
+
+// Exclusive prefix of both tile counts, in place (one block, any number of tiles).
+__global__ void __launch_bounds__(1024) select_scan_kernel(uint32_t *tileLt, uint32_t *tileEq, uint32_t tiles) {
+  __shared__ uint32_t warpSums[33];
+  uint32_t carryLt = 0, carryEq = 0;
+  for (uint32_t c = 0; c < tiles; c += blockDim.x) {
+    const uint32_t t = c + threadIdx.x;
+    const uint32_t lt = t < tiles ? tileLt[t] : 0u, eq = t < tiles ? tileEq[t] : 0u;
+    uint32_t sumLt, sumEq;
+    const uint32_t exLt = block_exclusive_sum(lt, warpSums, sumLt);
+    const uint32_t exEq = block_exclusive_sum(eq, warpSums, sumEq);
+    if (t < tiles) {
+      tileLt[t] = carryLt + exLt;
+      tileEq[t] = carryEq + exEq;
+    }
+    carryLt += sumLt;
+    carryEq += sumEq;
+  }
+}
+
+// The kept pairs in index order: key < T, or key == T among the first (k - below) such keys. Each
+// thread walks 16 consecutive keys; a key's place is (keys below T before it) + min(keys equal to
+// T before it, k - below).
+__global__ void __launch_bounds__(256) select_scatter_kernel(const uint32_t *__restrict__ keys,
+                                                             const uint32_t *__restrict__ vals, uint32_t n, uint32_t k,
+                                                             const SelState *__restrict__ st,
+                                                             const uint32_t *__restrict__ offLt,
+                                                             const uint32_t *__restrict__ offEq,
+                                                             uint32_t *__restrict__ outKeys,
+                                                             uint32_t *__restrict__ outVals) {
+  __shared__ uint32_t warpSums[33];
+  constexpr uint32_t kPer = kSelTile / 256;
+  const uint32_t T = st->prefix, need = k - st->below;
+  const size_t first = (size_t)blockIdx.x * kSelTile + (size_t)threadIdx.x * kPer;
+  uint32_t key[kPer];
+  uint32_t lt = 0, eq = 0;
+#pragma unroll
+  for (uint32_t j = 0; j < kPer; ++j) {
+    key[j] = first + j < n ? __ldg(keys + first + j) : 0xFFFFFFFFu;
+    const bool live = first + j < n;
+    lt += live && key[j] < T ? 1u : 0u;
+    eq += live && key[j] == T ? 1u : 0u;
+  }
+  uint32_t totLt, totEq;
+  uint32_t ltBefore = offLt[blockIdx.x] + block_exclusive_sum(lt, warpSums, totLt);
+  uint32_t eqBefore = offEq[blockIdx.x] + block_exclusive_sum(eq, warpSums, totEq);
+#pragma unroll
+  for (uint32_t j = 0; j < kPer; ++j) {
+    if (first + j >= n) break;
+    if (key[j] < T) {
+      const uint32_t pos = ltBefore + min(eqBefore, need);
+      if (pos < k) {  // always, unless the keys changed between the passes
+        outKeys[pos] = key[j];
+        outVals[pos] = __ldg(vals + first + j);
+      }
+      ++ltBefore;
+    } else if (key[j] == T) {
+      const uint32_t pos = ltBefore + eqBefore;
+      if (eqBefore < need && pos < k) {
+        outKeys[pos] = key[j];
+        outVals[pos] = __ldg(vals + first + j);
+      }
+      ++eqBefore;
+    }
+  }
+}
+
+}  // namespace
+
+size_t select_temp_bytes(uint32_t n, uint32_t k) { return make_sel_layout(n, min(k, n)).total; }
+
+int select_smallest(void *temp, const uint32_t *keys, const uint32_t *vals, uint32_t n, uint32_t k, uint32_t *valsOut,
+                    cudaStream_t s, uint32_t tileKeys) {
+  k = min(k, n);
+  if (k == 0) return BVHGB_OK;
+  const SelLayout L = make_sel_layout(n, k);
+  char *t = static_cast<char *>(temp);
+  SelState *st = reinterpret_cast<SelState *>(t + L.state);
+  uint32_t *hist = reinterpret_cast<uint32_t *>(t + L.hist);
+  uint32_t *tileLt = reinterpret_cast<uint32_t *>(t + L.tileLt);
+  uint32_t *tileEq = reinterpret_cast<uint32_t *>(t + L.tileEq);
+  uint32_t *ck = reinterpret_cast<uint32_t *>(t + L.keys);
+  uint32_t *cv = reinterpret_cast<uint32_t *>(t + L.vals);
+  uint32_t *ko = reinterpret_cast<uint32_t *>(t + L.keysOut);
+  if (k == n) return sort_pairs(t + L.sortTemp, keys, ko, vals, valsOut, n, 4, 0, 32, s, tileKeys);
+  BVHGB_CUDA_TRY(cudaMemsetAsync(hist, 0, 4ull * kSelBins, s));
+  const uint32_t hgrid = min(ceil_div(n, 512u * 4u), (uint32_t)sm_count() * 2);
+  for (int pass = 0; pass < 3; ++pass) {
+    select_hist_kernel<<<hgrid, 512, 0, s>>>(keys, n, st, hist, pass);
+    BVHGB_LAUNCH_CHECK("select histogram");
+    select_find_kernel<<<1, kSelBins / 2, 0, s>>>(st, hist, k, pass);
+    BVHGB_LAUNCH_CHECK("select find");
+  }
+  select_count_kernel<<<L.tiles, 256, 0, s>>>(keys, n, st, tileLt, tileEq);
+  BVHGB_LAUNCH_CHECK("select count");
+  select_scan_kernel<<<1, 1024, 0, s>>>(tileLt, tileEq, L.tiles);
+  BVHGB_LAUNCH_CHECK("select scan");
+  select_scatter_kernel<<<L.tiles, 256, 0, s>>>(keys, vals, n, k, st, tileLt, tileEq, ck, cv);
+  BVHGB_LAUNCH_CHECK("select scatter");
+  return sort_pairs(t + L.sortTemp, ck, ko, cv, valsOut, k, 4, 0, 32, s, tileKeys);
+}
+
 }  // namespace bvhgb
 
 extern "C" BVHGB_API int bvhgb_radix_sort_pairs(void *temp, size_t *tempBytes, const void *keysIn, void *keysOut,
@@ -387,6 +639,20 @@ extern "C" BVHGB_API int bvhgb_radix_sort_pairs(void *temp, size_t *tempBytes, c
   if (*tempBytes < need || (n && (!keysIn || !keysOut || !valsIn || !valsOut))) return BVHGB_INVALID_ARGUMENT;
   return bvhgb::sort_pairs(temp, keysIn, keysOut, valsIn, valsOut, n, keyBytes, beginBit, endBit,
                            bvhgb::as_stream(stream));
+}
+
+extern "C" BVHGB_API int bvhgb_select_smallest_pairs(void *temp, size_t *tempBytes, const uint32_t *keys,
+                                                     const uint32_t *vals, uint32_t *valsOut, uint32_t n, uint32_t k,
+                                                     bvhgb_stream stream) {
+  if (!tempBytes || k > n) return BVHGB_INVALID_ARGUMENT;
+  if (n >= (1u << 30)) return BVHGB_TOO_LARGE;
+  const size_t need = bvhgb::select_temp_bytes(n, k);
+  if (!temp) {
+    *tempBytes = need;
+    return BVHGB_OK;
+  }
+  if (*tempBytes < need || (k && (!keys || !vals || !valsOut))) return BVHGB_INVALID_ARGUMENT;
+  return bvhgb::select_smallest(temp, keys, vals, n, k, valsOut, bvhgb::as_stream(stream));
 }
 
 extern "C" BVHGB_API int bvhgb_sort_set_default_tile(uint32_t tileKeys, uint32_t *previous) {

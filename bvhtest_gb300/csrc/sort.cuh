@@ -19,4 +19,10 @@ constexpr uint32_t kSortTileDefault = 8192;
 bool sort_tile_valid(uint32_t tileKeys);
 int sort_pairs(void *temp, const void *keysIn, void *keysOut, const uint32_t *valsIn, uint32_t *valsOut, uint32_t n,
                uint32_t keyBytes, uint32_t beginBit, uint32_t endBit, cudaStream_t s, uint32_t tileKeys = 0);
+// The values of the first k pairs of a stable ascending sort of (keys, vals), 32-bit keys, in that
+// order, into valsOut[0, k) (k <= n), without sorting all n pairs; temp must hold
+// select_temp_bytes(n, k) bytes.
+size_t select_temp_bytes(uint32_t n, uint32_t k);
+int select_smallest(void *temp, const uint32_t *keys, const uint32_t *vals, uint32_t n, uint32_t k, uint32_t *valsOut,
+                    cudaStream_t s, uint32_t tileKeys = 0);
 }  // namespace bvhgb

@@ -97,6 +97,7 @@ PROTOS = {
     "bvhgb_lbvh_read_keys": (I32, [VP, I32, VP, VP, U32, VP]),
     "bvhgb_lbvh_read_errors": (I32, [VP, C.POINTER(U32), VP]),
     "bvhgb_radix_sort_pairs": (I32, [VP, C.POINTER(SZ), VP, VP, VP, VP, U32, U32, U32, U32, VP]),
+    "bvhgb_select_smallest_pairs": (I32, [VP, C.POINTER(SZ), VP, VP, VP, U32, U32, VP]),
     "bvhgb_sort_set_default_tile": (I32, [U32, C.POINTER(U32)]),
     "bvhgb_calc_sah": (I32, [VP, U32, U32, C.POINTER(C.c_double), VP]),
     "bvhgb_bn13_create": (I32, [VP, U32, U32, C.POINTER(Bn13Config), C.POINTER(VP), VP]),

@@ -179,6 +179,13 @@ BVHGB_API int bvhgb_radix_sort_pairs(void *temp, size_t *tempBytes, const void *
                                      const uint32_t *valsIn, uint32_t *valsOut, uint32_t n, uint32_t keyBytes,
                                      uint32_t beginBit, uint32_t endBit, bvhgb_stream stream);
 
+/* The values of the k smallest of n 32-bit keys in stable ascending order (the first k values of
+ * bvhgb_radix_sort_pairs over all 32 bits) into valsOut, without sorting all n pairs (k <= n). The
+ * optimizer's selection uses it. temp == NULL: *tempBytes receives the scratch size. No counterpart
+ * in the reference (its selection sorts every inner node, Bittner13CUDA.cu:659-726). */
+BVHGB_API int bvhgb_select_smallest_pairs(void *temp, size_t *tempBytes, const uint32_t *keys, const uint32_t *vals,
+                                          uint32_t *valsOut, uint32_t n, uint32_t k, bvhgb_stream stream);
+
 /* Keys per CTA of the onesweep passes (2048, 4096 or 8192) for sorts that are not given one: the
  * LBVH build's and the optimizer's selection sort, launched (or captured into a graph) after the
  * call. tileKeys = 0 only reads the setting. *previous (may be NULL) receives the old value. The
@@ -322,8 +329,9 @@ BVHGB_API int bvhgb_bn13_set_iteration(bvhgb_bn13_workspace *ws, uint64_t iterat
  * batch position order) for the following bvhgb_bn13_chunk calls; a later select overwrites it. */
 BVHGB_API int bvhgb_bn13_set_selection(bvhgb_bn13_workspace *ws, const uint32_t *order, uint32_t n,
                                        bvhgb_stream stream);
-/* Copies the most recent selection order (numInner node ids, batch position order) into out
- * (device, capacity entries) on 'stream'. */
+/* Copies the most recent selection order into out (device, capacity entries) on 'stream': the
+ * first min(bvhgb_bn13_batch_size, numInner) node ids in batch position order, which are the ones
+ * the chunks process (the reference sorts every inner node; only this prefix is ever read). */
 BVHGB_API int bvhgb_bn13_read_selection(const bvhgb_bn13_workspace *ws, uint32_t *out, uint32_t capacity,
                                         bvhgb_stream stream);
 

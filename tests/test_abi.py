@@ -47,6 +47,8 @@ def test_argument_errors_without_gpu():
     assert lib.bvhgb_lbvh_create(1 << 30, C.byref(cfg), C.byref(ws)) == 11
     need = C.c_size_t(0)
     assert lib.bvhgb_radix_sort_pairs(None, C.byref(need), None, None, None, None, 10, 3, 0, 8, None) == 8
+    assert lib.bvhgb_select_smallest_pairs(None, C.byref(need), None, None, None, 10, 11, None) == 8  # k > n
+    assert lib.bvhgb_select_smallest_pairs(None, None, None, None, None, 10, 5, None) == 8
     assert lib.bvhgb_trace_rays(None, 0, 0, None, None, None, None, 0, None, None, None) == 8
     assert lib.bvhgb_bn13_create(None, 0, 0, None, None, None) == 8
 

@@ -176,3 +176,29 @@ def test_sort_default_tile_gives_the_same_order(gpu, tile):
     assert np.array_equal(ko.cpu().numpy().view(np.uint64), keys[order])
     with pytest.raises(gpu.BvhgbError):
         gpu.sort_default_tile(1000)
+
+
+@pytest.mark.parametrize("n,k,kind", [(1, 1, "random"), (5000, 1, "random"), (5000, 4999, "ties"),
+                                      (5000, 5000, "random"), (100003, 1000, "ties"), (100003, 77777, "equal"),
+                                      (4194303, 83872, "random"), (4194303, 83872, "ties"), (1000000, 83872, "few")])
+def test_select_smallest_is_the_stable_sort_prefix(gpu, n, k, kind):
+    """The k smallest keys' values in stable ascending order equal the first k of the full stable sort,
+    with runs of equal keys cut at k in index order."""
+    import torch
+    g = np.random.default_rng(n + k)
+    if kind == "random":
+        keys = g.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32)
+    elif kind == "ties":
+        keys = g.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32)
+        keys[: n // 2] = keys[0]
+    elif kind == "equal":
+        keys = np.full(n, 0x3F800000, np.uint32)
+    else:  # few distinct values that share their high digits
+        keys = (g.integers(0, 4, n).astype(np.uint32) << 21) | g.integers(0, 3, n).astype(np.uint32)
+    vals = g.permutation(n).astype(np.uint32)
+    kt = torch.from_numpy(keys.view(np.int32)).cuda()
+    vt = torch.from_numpy(vals.view(np.int32)).cuda()
+    out = gpu.select_smallest_pairs(kt, vt, k)
+    torch.cuda.synchronize()
+    want = vals[np.argsort(keys, kind="stable")[:k]]
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), want)
