@@ -40,6 +40,27 @@ __device__ __forceinline__ float gelu_grad(float z) {
 }
 __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 
+// Inference GELU: tanh(u) = 1 - 2 / (1 + e^(2u)), e^(2u) = 2^(2u / ln 2) from the hardware's
+// approximate base-2 exponential and 1 / (1 + e^(2u)) from its approximate reciprocal (relative
+// errors near 2^-22 each), which leaves an absolute error of about 2e-7, far below the BF16 step
+// the activations are rounded to; the infinite or zero exponential saturates it to +-1. Training
+// keeps tanhf (its gradients are checked against float64).
+__device__ __forceinline__ float tanh_fast(float u) {
+  float e, r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(u * 2.8853900817779268f));
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(1.0f + e));
+  return fmaf(-2.0f, r, 1.0f);
+}
+__device__ __forceinline__ float gelu_fast(float z) {
+  const float u = kGeluC * (z + kGeluA * z * z * z);
+  return 0.5f * z * (1.0f + tanh_fast(u));
+}
+// Two values to BF16 in one conversion, packed low | high << 16.
+__device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi) {
+  const __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t *>(&p);
+}
+
 __device__ __forceinline__ void load_row(const uint16_t *__restrict__ x, size_t row, float in[kIn]) {
   const uint4 *p = reinterpret_cast<const uint4 *>(x + row * kIn);
 #pragma unroll
@@ -246,9 +267,9 @@ __global__ void __launch_bounds__(128, 4) mlp_forward_tc_kernel(const __nv_bfloa
 #pragma unroll
         for (int h = 0; h < 4; ++h) {
           const int j0 = 32 * half + 8 * c + 2 * h;
-          const float g0 = gelu(v[8 * c + 2 * h] + sm.b1f[j0]), g1 = gelu(v[8 * c + 2 * h + 1] + sm.b1f[j0 + 1]);
-          u[h] = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(g0)) |
-                 ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(g1)) << 16);
+          const float g0 = gelu_fast(v[8 * c + 2 * h] + sm.b1f[j0]);
+          const float g1 = gelu_fast(v[8 * c + 2 * h + 1] + sm.b1f[j0 + 1]);
+          u[h] = bf16x2_bits(g0, g1);
         }
         *reinterpret_cast<uint4 *>(sm.a2 + core_off(tid, 32 * half + 8 * c, kH)) = make_uint4(u[0], u[1], u[2], u[3]);
       }
@@ -277,7 +298,12 @@ __global__ void __launch_bounds__(128, 4) mlp_forward_tc_kernel(const __nv_bfloa
       float v[32];
       tc_ld32(tmem + lanebase + 64u + 32u * half, v);
 #pragma unroll
-      for (int i = 0; i < 32; ++i) out += sm.w3f[32 * half + i] * bf16r(gelu(v[i] + sm.b2f[32 * half + i]));
+      for (int i = 0; i < 32; i += 2) {
+        const uint32_t u = bf16x2_bits(gelu_fast(v[i] + sm.b2f[32 * half + i]),
+                                       gelu_fast(v[i + 1] + sm.b2f[32 * half + i + 1]));
+        out += sm.w3f[32 * half + i] * __uint_as_float(u << 16);
+        out += sm.w3f[32 * half + i + 1] * __uint_as_float(u & 0xFFFF0000u);
+      }
     }
     if (live) {
       y[row] = out;

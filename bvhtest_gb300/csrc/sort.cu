@@ -431,6 +431,7 @@ __global__ void __launch_bounds__(512) select_hist_kernel(const uint32_t *__rest
       const uint32_t key = __ldg(keys + i);
       if (pass == 0 || (key >> hi) == prefix) bin = (key >> shift) & mask;
     }
+    if (__ballot_sync(0xFFFFFFFFu, bin != 0xFFFFFFFFu) == 0u) continue;  // after the first pass, most warps
     const uint32_t peers = __match_any_sync(0xFFFFFFFFu, bin);
     if (bin != 0xFFFFFFFFu && (peers & ((1u << lane) - 1u)) == 0u) atomicAdd(&sh[bin], (uint32_t)__popc(peers));
   }
@@ -549,16 +550,28 @@ __global__ void __launch_bounds__(256) select_scatter_kernel(const uint32_t *__r
                                                              const uint32_t *__restrict__ offLt,
                                                              const uint32_t *__restrict__ offEq,
                                                              uint32_t *__restrict__ outKeys,
-                                                             uint32_t *__restrict__ outVals) {
+                                                             uint32_t *__restrict__ outVals, bool vec) {
   __shared__ uint32_t warpSums[33];
   constexpr uint32_t kPer = kSelTile / 256;
   const uint32_t T = st->prefix, need = k - st->below;
   const size_t first = (size_t)blockIdx.x * kSelTile + (size_t)threadIdx.x * kPer;
   uint32_t key[kPer];
+  if (vec && first + kPer <= n) {  // 16-byte loads: keys 16-byte aligned, first a multiple of 16 keys
+#pragma unroll
+    for (uint32_t j = 0; j < kPer; j += 4) {
+      const uint4 q = __ldg(reinterpret_cast<const uint4 *>(keys + first + j));
+      key[j] = q.x;
+      key[j + 1] = q.y;
+      key[j + 2] = q.z;
+      key[j + 3] = q.w;
+    }
+  } else {
+#pragma unroll
+    for (uint32_t j = 0; j < kPer; ++j) key[j] = first + j < n ? __ldg(keys + first + j) : 0xFFFFFFFFu;
+  }
   uint32_t lt = 0, eq = 0;
 #pragma unroll
   for (uint32_t j = 0; j < kPer; ++j) {
-    key[j] = first + j < n ? __ldg(keys + first + j) : 0xFFFFFFFFu;
     const bool live = first + j < n;
     lt += live && key[j] < T ? 1u : 0u;
     eq += live && key[j] == T ? 1u : 0u;
@@ -617,8 +630,12 @@ int select_smallest(void *temp, const uint32_t *keys, const uint32_t *vals, uint
   BVHGB_LAUNCH_CHECK("select count");
   select_scan_kernel<<<1, 1024, 0, s>>>(tileLt, tileEq, L.tiles);
   BVHGB_LAUNCH_CHECK("select scan");
-  select_scatter_kernel<<<L.tiles, 256, 0, s>>>(keys, vals, n, k, st, tileLt, tileEq, ck, cv);
+  const bool vec = (reinterpret_cast<uintptr_t>(keys) & 15u) == 0u;
+  select_scatter_kernel<<<L.tiles, 256, 0, s>>>(keys, vals, n, k, st, tileLt, tileEq, ck, cv, vec);
   BVHGB_LAUNCH_CHECK("select scatter");
+  // A few hundred thousand kept pairs fill few CTAs at the large tiles: the smallest tile spreads
+  // them wider (the order does not depend on the tile).
+  if (tileKeys == 0 && k <= (1u << 18)) tileKeys = 2048;
   return sort_pairs(t + L.sortTemp, ck, ko, cv, valsOut, k, 4, 0, 32, s, tileKeys);
 }
 

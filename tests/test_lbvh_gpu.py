@@ -202,3 +202,19 @@ def test_select_smallest_is_the_stable_sort_prefix(gpu, n, k, kind):
     torch.cuda.synchronize()
     want = vals[np.argsort(keys, kind="stable")[:k]]
     assert np.array_equal(out.cpu().numpy().view(np.uint32), want)
+
+
+def test_select_smallest_on_an_unaligned_key_array(gpu):
+    """Keys that start 4 bytes past a 16-byte boundary take the scalar loads: same result."""
+    import torch
+    g = np.random.default_rng(77)
+    n, k = 300001, 5000
+    keys = g.integers(0, 1 << 32, n + 1, dtype=np.uint64).astype(np.uint32)
+    vals = g.permutation(n + 1).astype(np.uint32)
+    kt = torch.from_numpy(keys.view(np.int32)).cuda()[1:]
+    vt = torch.from_numpy(vals.view(np.int32)).cuda()[1:]
+    assert kt.data_ptr() % 16 == 4
+    out = gpu.select_smallest_pairs(kt, vt, k)
+    torch.cuda.synchronize()
+    want = vals[1:][np.argsort(keys[1:], kind="stable")[:k]]
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), want)
