@@ -417,23 +417,35 @@ SelLayout make_sel_layout(uint32_t n, uint32_t k) {
 // of a warp with the same bin add together; the block's counts go out once).
 __global__ void __launch_bounds__(512) select_hist_kernel(const uint32_t *__restrict__ keys, uint32_t n,
                                                           const SelState *__restrict__ st, uint32_t *__restrict__ hist,
-                                                          int pass) {
+                                                          int pass, bool vec) {
   __shared__ uint32_t sh[kSelBins];
   for (uint32_t b = threadIdx.x; b < kSelBins; b += blockDim.x) sh[b] = 0;
   __syncthreads();
   const uint32_t shift = sel_shift(pass), mask = (1u << sel_bits(pass)) - 1u, hi = shift + sel_bits(pass);
   const uint32_t prefix = pass ? st->prefix : 0u;
   const uint32_t lane = threadIdx.x & 31u;
-  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {  // warp-uniform
-    const uint32_t i = base + threadIdx.x;
-    uint32_t bin = 0xFFFFFFFFu;
-    if (i < n) {
-      const uint32_t key = __ldg(keys + i);
-      if (pass == 0 || (key >> hi) == prefix) bin = (key >> shift) & mask;
+  // Four keys per thread and trip (one 16-byte load when the keys are 16-byte aligned).
+  for (size_t base = (size_t)blockIdx.x * blockDim.x * 4; base < n; base += (size_t)gridDim.x * blockDim.x * 4) {
+    const size_t i0 = base + 4 * (size_t)threadIdx.x;  // warp-uniform loop
+    uint32_t k4[4];
+    if (vec && i0 + 4 <= n) {
+      const uint4 q = __ldg(reinterpret_cast<const uint4 *>(keys + i0));
+      k4[0] = q.x;
+      k4[1] = q.y;
+      k4[2] = q.z;
+      k4[3] = q.w;
+    } else {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) k4[j] = i0 + j < n ? __ldg(keys + i0 + j) : 0u;
     }
-    if (__ballot_sync(0xFFFFFFFFu, bin != 0xFFFFFFFFu) == 0u) continue;  // after the first pass, most warps
-    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, bin);
-    if (bin != 0xFFFFFFFFu && (peers & ((1u << lane) - 1u)) == 0u) atomicAdd(&sh[bin], (uint32_t)__popc(peers));
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      uint32_t bin = 0xFFFFFFFFu;
+      if (i0 + j < n && (pass == 0 || (k4[j] >> hi) == prefix)) bin = (k4[j] >> shift) & mask;
+      if (__ballot_sync(0xFFFFFFFFu, bin != 0xFFFFFFFFu) == 0u) continue;  // after the first pass, most warps
+      const uint32_t peers = __match_any_sync(0xFFFFFFFFu, bin);
+      if (bin != 0xFFFFFFFFu && (peers & ((1u << lane) - 1u)) == 0u) atomicAdd(&sh[bin], (uint32_t)__popc(peers));
+    }
   }
   __syncthreads();
   for (uint32_t b = threadIdx.x; b < kSelBins; b += blockDim.x)
@@ -619,9 +631,10 @@ int select_smallest(void *temp, const uint32_t *keys, const uint32_t *vals, uint
   uint32_t *ko = reinterpret_cast<uint32_t *>(t + L.keysOut);
   if (k == n) return sort_pairs(t + L.sortTemp, keys, ko, vals, valsOut, n, 4, 0, 32, s, tileKeys);
   BVHGB_CUDA_TRY(cudaMemsetAsync(hist, 0, 4ull * kSelBins, s));
-  const uint32_t hgrid = min(ceil_div(n, 512u * 4u), (uint32_t)sm_count() * 2);
+  const bool vec = (reinterpret_cast<uintptr_t>(keys) & 15u) == 0u;
+  const uint32_t hgrid = min(ceil_div(n, 512u * 4u), (uint32_t)sm_count() * 4);
   for (int pass = 0; pass < 3; ++pass) {
-    select_hist_kernel<<<hgrid, 512, 0, s>>>(keys, n, st, hist, pass);
+    select_hist_kernel<<<hgrid, 512, 0, s>>>(keys, n, st, hist, pass, vec);
     BVHGB_LAUNCH_CHECK("select histogram");
     select_find_kernel<<<1, kSelBins / 2, 0, s>>>(st, hist, k, pass);
     BVHGB_LAUNCH_CHECK("select find");
@@ -630,7 +643,6 @@ int select_smallest(void *temp, const uint32_t *keys, const uint32_t *vals, uint
   BVHGB_LAUNCH_CHECK("select count");
   select_scan_kernel<<<1, 1024, 0, s>>>(tileLt, tileEq, L.tiles);
   BVHGB_LAUNCH_CHECK("select scan");
-  const bool vec = (reinterpret_cast<uintptr_t>(keys) & 15u) == 0u;
   select_scatter_kernel<<<L.tiles, 256, 0, s>>>(keys, vals, n, k, st, tileLt, tileEq, ck, cv, vec);
   BVHGB_LAUNCH_CHECK("select scatter");
   // A few hundred thousand kept pairs fill few CTAs at the large tiles: the smallest tile spreads
