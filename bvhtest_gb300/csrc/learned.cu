@@ -339,10 +339,13 @@ constexpr size_t kTrainSmem = sizeof(float) * (kWPad + kIn * kStride + 3 * kH * 
 __global__ void __launch_bounds__(kTile) mlp_train_kernel(const __nv_bfloat16 *__restrict__ w,
                                                           const uint16_t *__restrict__ x, const float *__restrict__ tgt,
                                                           const uint32_t *__restrict__ index, uint32_t n, float scaleN,
-                                                          float *__restrict__ grad, float *__restrict__ lossBase,
+                                                          float *__restrict__ part, float *__restrict__ lossBase,
                                                           const uint32_t *__restrict__ stepDev, uint32_t step0,
                                                           uint32_t lossCap) {
   extern __shared__ __align__(16) float sm[];
+  // This tile's gradient: every parameter's sum over the tile is stored once, in the tile's own row
+  // (grad_reduce_kernel adds the rows in a fixed order, so training repeats bit for bit).
+  float *grad = part + (size_t)blockIdx.x * kMlpParams;
   float *W = sm;
   float *X = W + kWPad;
   float *Z1 = X + kIn * kStride;  // pre-activations of layer 1, later their gradients
@@ -395,14 +398,14 @@ __global__ void __launch_bounds__(kTile) mlp_train_kernel(const __nv_bfloat16 *_
     for (int q = lane; q < kTile; q += 32) g += dY[q] * bf16r(gelu(Z2[j * kStride + q]));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xFFFFFFFFu, g, o);
-    if (lane == 0) atomicAdd(grad + oW3 + j, g);
+    if (lane == 0) grad[oW3 + j] = g;
   }
   if (warp == 0) {
     float g = 0.0f;
     for (int q = lane; q < kTile; q += 32) g += dY[q];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xFFFFFFFFu, g, o);
-    if (lane == 0) atomicAdd(grad + oB3, g);
+    if (lane == 0) grad[oB3] = g;
   }
   __syncthreads();
   // dZ2 = dY W3 gelu'(Z2); dZ1 = (W2^T dZ2) gelu'(Z1), one column per thread
@@ -426,9 +429,9 @@ __global__ void __launch_bounds__(kTile) mlp_train_kernel(const __nv_bfloat16 *_
       g2b += d2 * a1b[q];
       g1 += d1 * xk[q];
     }
-    atomicAdd(grad + oW2 + j * kH + lane, g2a);
-    atomicAdd(grad + oW2 + j * kH + lane + 32, g2b);
-    if (lane < (uint32_t)kIn) atomicAdd(grad + oW1 + j * kIn + lane, g1);
+    grad[oW2 + j * kH + lane] = g2a;
+    grad[oW2 + j * kH + lane + 32] = g2b;
+    if (lane < (uint32_t)kIn) grad[oW1 + j * kIn + lane] = g1;
     float b2 = 0.0f, b1 = 0.0f;
     for (int q = lane; q < kTile; q += 32) {
       b2 += dz2[q];
@@ -440,10 +443,19 @@ __global__ void __launch_bounds__(kTile) mlp_train_kernel(const __nv_bfloat16 *_
       b1 += __shfl_xor_sync(0xFFFFFFFFu, b1, o);
     }
     if (lane == 0) {
-      atomicAdd(grad + oB2 + j, b2);
-      atomicAdd(grad + oB1 + j, b1);
+      grad[oB2 + j] = b2;
+      grad[oB1 + j] = b1;
     }
   }
+}
+
+// g = the sum of the tiles' gradient rows, in tile order.
+__global__ void grad_reduce_kernel(const float *__restrict__ part, uint32_t tiles, float *__restrict__ g) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)kMlpParams) return;
+  float acc = 0.0f;
+  for (uint32_t b = 0; b < tiles; ++b) acc += part[(size_t)b * kMlpParams + i];
+  g[i] = acc;
 }
 
 // AdamW (Loshchilov and Hutter) on all parameters in one block: moments, bias correction with the
@@ -837,6 +849,8 @@ struct bvhgb_mlp {
   uint32_t *err = nullptr;  // error bits of the inference kernel (kErrTimeout)
   uint32_t *idx = nullptr;
   uint32_t idxCap = 0, lossCap = 0;
+  float *part = nullptr;  // per-tile gradient rows [partCap][kMlpParams]
+  uint32_t partCap = 0;
 };
 
 struct bvhgb_lr_features_ctx {
@@ -860,6 +874,16 @@ int ensure_train_attr() {
     BVHGB_CUDA_TRY(cudaFuncSetAttribute(mlp_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem));
     done = true;
   }
+  return BVHGB_OK;
+}
+
+int ensure_part(bvhgb_mlp *m, uint32_t tiles) {
+  if (m->partCap >= tiles && m->part) return BVHGB_OK;
+  cudaFree(m->part);
+  m->part = nullptr;
+  m->partCap = 0;
+  BVHGB_CUDA_TRY(cudaMalloc(&m->part, 4ull * kMlpParams * std::max(tiles, 1u)));
+  m->partCap = std::max(tiles, 1u);
   return BVHGB_OK;
 }
 
@@ -919,6 +943,7 @@ extern "C" BVHGB_API int bvhgb_mlp_destroy(bvhgb_mlp *m) {
   if (!m) return BVHGB_OK;
   cudaFree(m->p);
   cudaFree(m->g);
+  cudaFree(m->part);
   cudaFree(m->m);
   cudaFree(m->v);
   cudaFree(m->loss);
@@ -962,15 +987,17 @@ extern "C" BVHGB_API int bvhgb_mlp_forward(const bvhgb_mlp *m, const uint16_t *x
 extern "C" BVHGB_API int bvhgb_mlp_gradient(bvhgb_mlp *m, const uint16_t *x, const float *t, uint32_t n,
                                             float *gradHost, float *lossHost, bvhgb_stream stream) {
   if (!m || !x || !t || n == 0) return BVHGB_INVALID_ARGUMENT;
+  const uint32_t tiles = ceil_div(n, kTile);
   int st = ensure_train_attr();
   if (!st) st = ensure_loss(m, 1);
+  if (!st) st = ensure_part(m, tiles);
   if (st) return st;
   cudaStream_t s = as_stream(stream);
-  BVHGB_CUDA_TRY(cudaMemsetAsync(m->g, 0, 4 * kMlpParams, s));
   BVHGB_CUDA_TRY(cudaMemsetAsync(m->loss, 0, 4, s));
-  mlp_train_kernel<<<ceil_div(n, kTile), kTile, kTrainSmem, s>>>(m->pb, x, t, nullptr, n, (float)n, m->g, m->loss,
-                                                                  nullptr, 0, 1);
+  mlp_train_kernel<<<tiles, kTile, kTrainSmem, s>>>(m->pb, x, t, nullptr, n, (float)n, m->part, m->loss, nullptr, 0, 1);
   BVHGB_LAUNCH_CHECK("mlp gradient");
+  grad_reduce_kernel<<<ceil_div((uint32_t)kMlpParams, 256u), 256, 0, s>>>(m->part, tiles, m->g);
+  BVHGB_LAUNCH_CHECK("mlp gradient reduce");
   if (gradHost) BVHGB_CUDA_TRY(cudaMemcpyAsync(gradHost, m->g, 4 * kMlpParams, cudaMemcpyDeviceToHost, s));
   if (lossHost) BVHGB_CUDA_TRY(cudaMemcpyAsync(lossHost, m->loss, 4, cudaMemcpyDeviceToHost, s));
   BVHGB_CUDA_TRY(cudaMemsetAsync(m->g, 0, 4 * kMlpParams, s));
@@ -983,8 +1010,10 @@ extern "C" BVHGB_API int bvhgb_mlp_train(bvhgb_mlp *m, const uint16_t *x, const 
                                          float *lossHistory, bvhgb_stream stream) {
   if (!m || !x || !t || numSamples == 0 || batch == 0) return BVHGB_INVALID_ARGUMENT;
   if (steps == 0) return BVHGB_OK;
+  const uint32_t tiles = ceil_div(batch, kTile);
   int st = ensure_train_attr();
   if (!st) st = ensure_loss(m, steps);
+  if (!st) st = ensure_part(m, tiles);
   if (st) return st;
   cudaStream_t s = as_stream(stream);
   if (m->idxCap < batch) {
@@ -1008,8 +1037,9 @@ extern "C" BVHGB_API int bvhgb_mlp_train(bvhgb_mlp *m, const uint16_t *x, const 
   cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     batch_index_kernel<<<ceil_div(batch, 256), 256, 0, cap>>>(m->idx, batch, numSamples, seed, m->stepDev);
-    mlp_train_kernel<<<ceil_div(batch, kTile), kTile, kTrainSmem, cap>>>(m->pb, x, t, m->idx, batch, (float)batch,
-                                                                          m->g, m->loss, m->stepDev, step0, steps);
+    mlp_train_kernel<<<tiles, kTile, kTrainSmem, cap>>>(m->pb, x, t, m->idx, batch, (float)batch, m->part, m->loss,
+                                                         m->stepDev, step0, steps);
+    grad_reduce_kernel<<<ceil_div((uint32_t)kMlpParams, 256u), 256, 0, cap>>>(m->part, tiles, m->g);
     adamw_kernel<<<1, 1024, 0, cap>>>(m->p, m->pb, m->g, m->m, m->v, m->stepDev, lr, weightDecay);
     e = cudaStreamEndCapture(cap, &graph);
   }
@@ -1022,7 +1052,7 @@ extern "C" BVHGB_API int bvhgb_mlp_train(bvhgb_mlp *m, const uint16_t *x, const 
     return BVHGB_CUDA_ERROR;
   }
   for (uint32_t k = 0; k < steps && e == cudaSuccess; ++k) e = cudaGraphLaunch(exec, s);
-  count_launch(3u * steps);  // (the capture itself recorded none: its launches are not counted)
+  count_launch(4u * steps);  // (the capture itself recorded none: its launches are not counted)
   if (e == cudaSuccess && lossHistory) e = cudaMemcpyAsync(lossHistory, m->loss, 4ull * steps, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   cudaGraphExecDestroy(exec);

@@ -131,6 +131,20 @@ def test_training_reduces_loss(gpu):
     assert hist[-50:].mean() < 0.2 * hist[:10].mean()
 
 
+def test_training_repeats_bit_for_bit(gpu):
+    """The tiles' gradients are summed in a fixed order: the same data, initial weights and seed give
+    the same weights, so a scorer trained in a run is the same scorer every run."""
+    import torch
+    xf, xt = _rand_rows(20000, 6)
+    t = torch.from_numpy((np.tanh(xf[:, 0]) - 0.3 * xf[:, 3]).astype(np.float32)).cuda()
+    got = []
+    for _ in range(2):
+        m = gpu.Mlp(seed=12)
+        m.train(xt, t, 200, batch=4096, lr=2e-3, weight_decay=1e-4, seed=5)
+        got.append(m.params())
+    assert np.array_equal(got[0].view(np.uint32), got[1].view(np.uint32))
+
+
 def test_learned_selection_iteration_matches_oracle(gpu, orc):
     import torch
     _, _, nodes = _tree(gpu, 16384, seed=33)
