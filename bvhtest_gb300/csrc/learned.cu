@@ -1,7 +1,7 @@
 // Learned reinsertion scorer: node features, the 24 -> 64 -> 64 -> 1 GELU MLP (BF16 weights,
 // inputs and activations, FP32 accumulation) and its training kernels. The reference has no learned
 // part; its node selection is the inefficiency of lib/builder/Bittner13CUDA.cu:480-500, which stays
-// the default (bittner.cu) and judges the scorer through the SAH it reaches.
+// the default (bittner.cu) and evaluates the scorer by the SAH it reaches.
 //
 // Layout in HBM: feature rows are 24 BF16 values (48 bytes, three 16-byte words) per inner node in
 // the order of the optimizer's ascending inner-node list; parameters are one FP32 master array of
