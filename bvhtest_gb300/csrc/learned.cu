@@ -510,10 +510,13 @@ __device__ __forceinline__ uint32_t rank_bin(float v) { return f2ord(v) >> 16; }
 
 // Depth by pointer jumping on ad[x] = distance << 32 | ancestor: each round replaces a node's
 // ancestor a by a's own (ad[a] read whole, so the pair is always an ancestor and its distance,
-// whichever round wrote it). A round reaches at least as far as a synchronous one, so after r
-// rounds a node's ancestor is the root or at least 2^r levels up, and kDepthRounds rounds give
+// whichever round wrote it). A round follows kDepthHops pointers beyond the node's own: if every
+// pointer reached R levels when the round began, the node now reaches at least (kDepthHops + 1) R,
+// so after kDepthLaunches rounds it is the root or 4^4 = 256 levels up, and the features get
 // min(depth, 2^kDepthRounds) exactly. Only inner nodes jump (a leaf is nobody's ancestor and its
 // depth is not a feature); a node whose ancestor is the root is done.
+constexpr int kDepthHops = 3, kDepthLaunches = 4;
+static_assert(kDepthHops == 3 && kDepthLaunches == 4 && kDepthRounds == 8, "(hops + 1)^launches >= 2^rounds");
 // One coalesced pass over the nodes: the depth recursion's start, and compact copies of every
 // node's surface area and parent (bit 31: the node is a leaf) that the leaf counts and the feature
 // rows gather from (33 MB per 8M nodes each, so they stay in L2 where the 48-byte records do not).
@@ -537,10 +540,16 @@ __global__ void depth_jump_kernel(const uint32_t *__restrict__ inner, uint32_t n
     const uint32_t x = __ldg(inner + i);
     if (x >= n) continue;  // flagged by the feature rows
     const unsigned long long v = __ldcg(ad + x);
-    const uint32_t a = (uint32_t)v;
+    uint32_t a = (uint32_t)v, d = (uint32_t)(v >> 32);
     if (a == root || a >= n) continue;
-    const unsigned long long w = __ldcg(ad + a);
-    __stcg(ad + x, (((v >> 32) + (w >> 32)) << 32) | (w & 0xFFFFFFFFull));
+#pragma unroll
+    for (int h = 0; h < kDepthHops; ++h) {
+      const unsigned long long w = __ldcg(ad + a);
+      d += (uint32_t)(w >> 32);
+      a = (uint32_t)w;
+      if (a == root || a >= n) break;
+    }
+    __stcg(ad + x, ((unsigned long long)d << 32) | a);
   }
 }
 // Leaf counts bottom-up. A leaf starts a climb with count 1; at each parent the two arrivals add
@@ -818,7 +827,7 @@ int lr_features(LrScratch &s, const bvhgb_node *nodes, uint32_t numNodes, uint32
   depth_init_kernel<<<g, 256, 0, st>>>(nodes, numNodes, root, s.ad, s.sa, s.par);
   BVHGB_LAUNCH_CHECK("lr depth init");
   const uint32_t gi = grid_for(numInner, 256);
-  for (uint32_t r = 0; r < kDepthRounds; ++r) {
+  for (int r = 0; r < kDepthLaunches; ++r) {
     depth_jump_kernel<<<gi, 256, 0, st>>>(inner, numInner, numNodes, root, s.ad);
     BVHGB_LAUNCH_CHECK("lr depth jump");
   }

@@ -14,7 +14,7 @@ constexpr int kMlpHidden = 64;
 constexpr int kMlpParams = BVHGB_MLP_PARAMS;  // W1[64][24] b1[64] W2[64][64] b2[64] W3[64] b3
 constexpr int kMlpRaw = 10;                   // raw (non-rank) features
 constexpr uint32_t kRankBins = 65536;         // rank histogram bins (top 16 bits of the ordered image)
-constexpr uint32_t kDepthRounds = 8;          // pointer-jumping rounds: depth is exact up to 256
+constexpr uint32_t kDepthRounds = 8;          // depth features are exact up to 2^8 = 256 levels
 constexpr float kTargetEps = 0.16f;           // target = sign(g) ln(1 + |g| numLeaves / kTargetEps)
 
 // Device scratch for the features of one tree (sized for numNodes nodes).
