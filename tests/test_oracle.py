@@ -250,3 +250,22 @@ def test_batched_search_reaches_the_heap_order_sah(orc):
     _, th, _ = orc.bittner_chunked(nodes, 10, search_mode=1)
     assert abs(tb[-1] / th[-1] - 1.0) <= 0.005, (tb[-1], th[-1])
     assert tb[-1] < 0.8 * tb[0]
+
+
+@pytest.mark.parametrize("offset_access", [False, True])
+def test_ordered_iteration_reads_only_the_batch_prefix(orc, offset_access):
+    """A chunked iteration processes the positions below numChunks * chunkSize of its order (in
+    chunk-major or strided batch order), so that prefix gives the same tree as the whole order:
+    the GPU selection keeps only the prefix."""
+    vert, faces = scenes.uniform_soup(6000, seed=4)
+    nodes, _, _ = orc.lbvh_build(vert, faces)
+    inner = np.nonzero(nodes["isLeafFlag"] == 0)[0].astype(np.uint32)
+    order = np.random.default_rng(3).permutation(inner).astype(np.uint32)
+    k = int(0.01 * nodes.shape[0]) // 32 * 32
+    assert 0 < k < order.shape[0]
+    a = np.ascontiguousarray(nodes.copy())
+    b = np.ascontiguousarray(nodes.copy())
+    sa = orc.bittner_iteration_ordered(a, order, offset_access=offset_access)
+    sb = orc.bittner_iteration_ordered(b, order[:k], offset_access=offset_access)
+    assert sa == sb and sa["items"] == k
+    assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
