@@ -67,3 +67,29 @@ def test_struct_layouts():
 def test_node_offsets(field, off):
     from bvhtest_gb300 import native
     assert native.NODE_DTYPE.fields[field][1] == off
+
+
+def test_every_entry_rejects_null_handles_without_crashing():
+    """Every exported function called with null pointers and zero sizes returns a status: invalid
+    argument for a missing handle or buffer, OK where null is allowed (destroy, queries), a CUDA
+    error where the device itself is needed. Nothing dereferences the null."""
+    from bvhtest_gb300 import native
+    lib = native.load()
+    allowed_ok = {"bvhgb_sort_set_default_tile"}  # tileKeys = 0 with a null 'previous' only reads
+    for name in sorted(native.PROTOS):
+        f = getattr(lib, name)
+        args = []
+        for t in f.argtypes or []:
+            if t in (C.c_float, C.c_double):
+                args.append(0.0)
+            elif t in (C.c_void_p, C.c_char_p) or (isinstance(t, type) and issubclass(t, C._Pointer)):
+                args.append(None)
+            else:
+                args.append(0)
+        r = f(*args)
+        if f.restype is not C.c_int32 or not f.argtypes:
+            continue  # counters, strings, sizes; bvhgb_device_sync needs a device
+        if name.endswith("_destroy") or name in allowed_ok:
+            assert r == 0, name
+        else:
+            assert r == 8, (name, r)  # BVHGB_INVALID_ARGUMENT
