@@ -143,3 +143,24 @@ def test_learned_scorer_option(tmp_path, gpu):
     cfg2 = _config(tmp_path, [{"cmd": "load"}, {"cmd": "copyToGPU"}, {"cmd": "LBVH"},
                               {"cmd": "bittner13GPU", "options": {"maxNumStepps": 1, "learnedScorer": "missing.f32"}}])
     assert _run(cfg2) == 2  # IO_ERROR stops the input
+
+
+def test_malformed_configs_report_errors_without_crashing(tmp_path):
+    """Bad JSON, a missing config file or input mesh give an error status; an unknown command is
+    skipped with a warning; wrongly typed sections run nothing. None of them crashes the process."""
+    cases = {
+        "bad": ("{ not json", lambda r: r != 0),
+        "missing_input": (json.dumps({"baseConfig": {"name": "x", "basePath": str(tmp_path), "input": ["nope"]},
+                                      "commands": [{"cmd": "load"}]}), lambda r: r == 2),
+        "unknown": (json.dumps({"baseConfig": {"name": "x", "basePath": str(tmp_path), "input": []},
+                                "commands": [{"cmd": "frobnicate"}]}), lambda r: r == 0),
+        "types": (json.dumps({"baseConfig": {"name": 5, "basePath": 7, "input": "scene"},
+                              "commands": {"cmd": "load"}}), lambda r: r == 0),
+        "array": ("[]", lambda r: r == 0),
+    }
+    for name, (text, ok) in cases.items():
+        p = tmp_path / f"{name}.json"
+        p.write_text(text)
+        r = _run(p)
+        assert ok(r), (name, r)
+    assert _run(tmp_path / "no_such_config.json") != 0
