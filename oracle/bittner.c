@@ -4,7 +4,8 @@
  *  - orc_bittner_chunked: the chunked parallel GPU algorithm, lib/builder/Bittner13CUDA.cu:141-772
  *                         with lib/base/BVHPatch.hpp:87-335, items of a chunk evaluated against
  *                         the chunk-start tree, conflicts resolved by batch rank.
- * Parity unpinned: see oracle.h.
+ * Both are pinned to the reference's own code (oracle.h): orc_bittner_seq to Bittner13.cpp, the
+ * chunked form with Bittner13Par's rules to Bittner13Par.cpp.
  */
 #include "oracle.h"
 
@@ -215,19 +216,14 @@ int orc_bittner_seq(orc_node *t, uint32_t n_nodes, uint32_t *root, uint32_t iter
   uint32_t k = (uint32_t)((batch_percent / 100.0f) * (float)n_nodes);
   const uint32_t cap = 16384; /* Bittner13::QUEUE_SIZE */
   hitem *pq = malloc(sizeof(hitem) * cap);
-  cost_item *todo = malloc(sizeof(cost_item) * n_nodes);
+  uint32_t *todo = malloc(sizeof(uint32_t) * (n_nodes ? n_nodes : 1));
   if (sah_trace) sah_trace[0] = orc_sah(t, n_nodes, *root);
   for (uint32_t it = 0; it < iters; ++it) {
-#pragma omp parallel for schedule(static)
-    for (int64_t j = 0; j < (int64_t)n_nodes; ++j) {
-      todo[j].idx = (uint32_t)j;
-      todo[j].cost = orc_inefficiency(t, (uint32_t)j);
-    }
-    /* nth_element + sort of the first k (Bittner13.cpp:282-283); ties broken by index. */
-    qsort(todo, n_nodes, sizeof(cost_item), cmp_cost_desc);
-    for (uint32_t j = 0; j < k && j < n_nodes; ++j) {
+    /* nth_element + sort of the first k (Bittner13.cpp:258-283), with the same library calls. */
+    const uint32_t m = orc_std_select(t, n_nodes, k, 1, todo);
+    for (uint32_t j = 0; j < m; ++j) {
       uint32_t ins[2], un[2];
-      if (!seq_remove(t, *root, todo[j].idx, ins, un)) continue;
+      if (!seq_remove(t, *root, todo[j], ins, un)) continue;
       seq_reinsert(t, root, ins[0], un[0], pq, cap);
       seq_reinsert(t, root, ins[1], un[1], pq, cap);
     }
@@ -625,9 +621,18 @@ static void run_iteration(orc_node *t, uint32_t root, const uint32_t *order, uin
       w->fix[3 * k + 1] = un[0];
       w->fix[3 * k + 2] = un[1];
     }
-    /* Conflict rule: claim every patched node with the item's rank; lowest rank wins. */
+    /* Conflict rule 0: claim every patched node with the item's rank; lowest rank wins.
+     * Rule 1: in batch order, an item takes its nodes only if none is taken yet. */
     for (uint32_t k = 0; k < csize; ++k) {
       if (!w->valid[k]) continue;
+      if (cfg->conflict_rule == 1) {
+        int free_all = 1;
+        for (int s = 0; s < NNODE; ++s) {
+          uint32_t x = w->patches[k].idx[s];
+          if (x != NONE && w->owner[x] != NONE) free_all = 0;
+        }
+        if (!free_all) continue;
+      }
       for (int s = 0; s < NNODE; ++s) {
         uint32_t x = w->patches[k].idx[s];
         if (x != NONE && k < w->owner[x]) w->owner[x] = k;
@@ -686,24 +691,32 @@ int orc_bittner_chunked(orc_node *t, uint32_t n_nodes, uint32_t root, uint32_t i
   for (uint32_t i = 0, j = 0; i < n_nodes; ++i) if (!t[i].isLeafFlag) inner[j++] = i;
   cost_item *todo = malloc(sizeof(cost_item) * (n_inner ? n_inner : 1));
   uint32_t *order = malloc(sizeof(uint32_t) * (n_inner ? n_inner : 1));
+  uint32_t *order_all = cfg->std_select ? malloc(sizeof(uint32_t) * (n_nodes ? n_nodes : 1)) : NULL;
   chunk_work w;
   chunk_work_init(&w, n_nodes, csize, cap);
 
   if (sah_trace) sah_trace[0] = orc_sah(t, n_nodes, root);
   for (uint32_t it = 0; it < iters; ++it) {
-    /* bn13_selectNodes (:659-726): kCalcCost + stable descending sort of (cost, node). */
-    for (uint32_t j = 0; j < n_inner; ++j) {
-      todo[j].idx = inner[j];
-      todo[j].cost = orc_inefficiency(t, inner[j]);
+    uint32_t n_order = n_inner;
+    if (cfg->std_select) {
+      /* Bittner13Par.cpp:421-437: nth_element + sort of the chunk-rounded batch over all nodes. */
+      n_order = orc_std_select(t, n_nodes, numc * csize, 1, order_all);
+      run_iteration(t, root, order_all, n_order, numc, csize, cap, cfg, &w, &st);
+    } else {
+      /* bn13_selectNodes (:659-726): kCalcCost + stable descending sort of (cost, node). */
+      for (uint32_t j = 0; j < n_inner; ++j) {
+        todo[j].idx = inner[j];
+        todo[j].cost = orc_inefficiency(t, inner[j]);
+      }
+      qsort(todo, n_inner, sizeof(cost_item), cmp_cost_desc);
+      for (uint32_t j = 0; j < n_inner; ++j) order[j] = todo[j].idx;
+      run_iteration(t, root, order, n_order, numc, csize, cap, cfg, &w, &st);
     }
-    qsort(todo, n_inner, sizeof(cost_item), cmp_cost_desc);
-    for (uint32_t j = 0; j < n_inner; ++j) order[j] = todo[j].idx;
-    run_iteration(t, root, order, n_inner, numc, csize, cap, cfg, &w, &st);
     if (sah_trace) sah_trace[it + 1] = orc_sah(t, n_nodes, root);
   }
   chunk_work_free(&w, &st);
   if (stats) *stats = st;
-  free(inner); free(todo); free(order);
+  free(inner); free(todo); free(order); free(order_all);
   (void)cmp_u32;
   return 0;
 }

@@ -5,11 +5,20 @@
  * and the cpu_baseline / --impl reference legs of bench.py load it. The product (the CUDA
  * library under bvhtest_gb300/) never links or calls it and has no CPU fallback.
  *
- * Parity status: UNPINNED. The reference (mensinda/BVHTest) ships no tests, golden vectors or
- * fixtures, and it cannot be compiled here (its glm/cub/fmt/spdlog submodules are empty and glm
- * is not installed). Every function below is a plain-C restatement of the reference file:line
- * it cites, pinned only by hand-derived known-answer tests (tests/golden/) and by the
- * reference's own runtime invariants (lib/misc/Validate.cpp), which are restated here too.
+ * Parity status: PINNED where the reference has CPU code, through the reference's own sources.
+ * oracle/build_ref.py compiles lib/builder/Bittner13.cpp, Bittner13Par.cpp, lib/base/BVH.cpp,
+ * lib/misc/Camera.cpp, lib/tracer/CPUTracer.cpp, BruteForceTracer.cpp, Median.cpp and Wald07.cpp
+ * (with stand-ins, written here, for its empty math/format/log submodules) into oracle/_ref, and
+ * tests/test_ref_pin.py checks: orc_bittner_seq == Bittner13 and orc_bittner_chunked with
+ * {heap search, conflict_rule 1, std_select 1} == Bittner13Par, byte for byte on the trees (also on
+ * the large scene, whose inefficiencies tie); orc_sah == BVH::calcSAH up to its float summation;
+ * orc_camera_rays == Camera::genRays; orc_trace_cpu_reference == CPUTracer (hit mask, visit counts,
+ * shading bytes); orc_trace_brute's hit mask == BruteForceTracer's. tests/golden/ref_pin.npz keeps
+ * those outputs for machines without the reference. UNPINNED: the LBVH steps (the reference has
+ * them only as CUDA kernels, which cannot run here) and the GPU kernels' deterministic conflict
+ * rule (conflict_rule 0; the reference's GPU rule is first-come and not deterministic); they rest
+ * on hand-derived known answers (tests/golden/) and the reference's runtime invariants
+ * (lib/misc/Validate.cpp restated here).
  *
  * Floating point: compiled with -ffp-contract=off so that every a*b+c rounds twice, matching
  * the product kernels, which spell out __fmul_rn/__fadd_rn. The reference's GPU build let nvcc
@@ -107,7 +116,20 @@ typedef struct orc_bn13_cfg {
   uint32_t offset_access;/* offsetAccess */
   uint32_t heap_cap;     /* B&B heap capacity (the reference uses 4096) */
   uint32_t search_mode;  /* 0: batched best-first (32 per round, frontier 128); 1: findNode1 heap */
+  uint32_t conflict_rule;/* 0: an item is applied iff it holds the lowest batch rank on every node it
+                          *    patches, failed items' claims included (the GPU kernels);
+                          * 1: items are taken in batch order and an item is applied iff none of its
+                          *    nodes was taken by an earlier applied item (Bittner13Par.cpp:470-495,
+                          *    where a failed item releases what it claimed) */
+  uint32_t std_select;   /* 0: inner nodes by descending inefficiency, ties by node index (GPU
+                          *    kernels); 1: the reference CPU optimizers' nth_element + sort order
+                          *    (orc_std_select) */
 } orc_bn13_cfg;
+
+/* Batch selection of Bittner13.cpp:258-283 / Bittner13Par.cpp:421-437 with the same standard-
+ * library calls (ties come out in the reference's order): writes the first k nodes by descending
+ * inefficiency to order_out and returns k. */
+uint32_t orc_std_select(const orc_node *nodes, uint32_t n_nodes, uint32_t k, int do_sort, uint32_t *order_out);
 
 typedef struct orc_bn13_stats {
   uint64_t items;        /* batch items considered */

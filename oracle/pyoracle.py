@@ -30,7 +30,8 @@ class Camera(C.Structure):
 
 class Bn13Cfg(C.Structure):
     _fields_ = [("num_chunks", C.c_uint32), ("batch_percent", C.c_float), ("offset_access", C.c_uint32),
-                ("heap_cap", C.c_uint32), ("search_mode", C.c_uint32)]
+                ("heap_cap", C.c_uint32), ("search_mode", C.c_uint32), ("conflict_rule", C.c_uint32),
+                ("std_select", C.c_uint32)]
 
 
 class Bn13Stats(C.Structure):
@@ -143,11 +144,13 @@ def bittner_seq(nodes, iters, batch_percent=1.0, root=0):
 
 
 def bittner_chunked(nodes, iters, num_chunks=32, batch_percent=1.0, offset_access=False, heap_cap=4096, root=0,
-                    search_mode=0):
-    """search_mode 0: batched best-first search (GPU default); 1: the reference's heap order."""
+                    search_mode=0, conflict_rule=0, std_select=0):
+    """search_mode 0: batched best-first search (GPU default); 1: the reference's heap order.
+    conflict_rule 0: lowest batch rank claims (GPU kernels); 1: Bittner13Par's first-come rule.
+    std_select 0: stable inefficiency order (GPU kernels); 1: the reference CPU optimizers' order."""
     nodes = np.ascontiguousarray(nodes).copy()
     trace = np.zeros(iters + 1, np.float64)
-    cfg = Bn13Cfg(num_chunks, batch_percent, int(offset_access), heap_cap, search_mode)
+    cfg = Bn13Cfg(num_chunks, batch_percent, int(offset_access), heap_cap, search_mode, conflict_rule, std_select)
     st = Bn13Stats()
     lib().orc_bittner_chunked(_p(nodes), C.c_uint32(nodes.shape[0]), C.c_uint32(root), C.c_uint32(iters),
                               C.byref(cfg), _p(trace), C.byref(st))
