@@ -1,6 +1,7 @@
 // Library-wide host helpers, SAH reduction and the transfer entry points
 // (lib/cuda/cudaFN.cu:32-187, lib/builder/Bittner13CUDA.cu:776-803, lib/base/BVH.cpp:23-70).
 #include <atomic>
+#include <mutex>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -31,6 +32,40 @@ void count_launch(uint32_t n) { g_launches.fetch_add(n, std::memory_order_relaxe
 // Launches recorded while a stream was being captured did not run; the capture takes them back and
 // every replay of the graph adds its kernel count instead.
 void uncount_launches(uint64_t n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
+
+// Identity of the CUDA context current on this thread: the driver's context ID, unique within the
+// process, so a context made after a cudaDeviceReset never matches one cached before it. 0 when
+// there is no current context or the driver does not report one.
+uint64_t context_id() {
+  typedef int (*CtxGetCurrent)(void **);
+  typedef int (*CtxGetId)(void *, unsigned long long *);
+  static CtxGetCurrent getCurrent = nullptr;
+  static CtxGetId getId = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *a = nullptr, *b = nullptr;
+    cudaDriverEntryPointQueryResult qa, qb;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) == cudaSuccess &&
+        qa == cudaDriverEntryPointSuccess)
+      getCurrent = reinterpret_cast<CtxGetCurrent>(a);
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) == cudaSuccess &&
+        qb == cudaDriverEntryPointSuccess)
+      getId = reinterpret_cast<CtxGetId>(b);
+    cudaGetLastError();
+  });
+  if (!getCurrent || !getId) return 0;
+  void *ctx = nullptr;
+  if (getCurrent(&ctx) != 0) return 0;
+  if (!ctx) {
+    // No context on this thread yet (so no stream capture either): let the runtime make its
+    // context current, then ask again.
+    cudaFree(nullptr);
+    if (getCurrent(&ctx) != 0 || !ctx) return 0;
+  }
+  unsigned long long id = 0;
+  if (getId(ctx, &id) != 0) return 0;
+  return (uint64_t)id;
+}
 
 int sm_count() {
   int dev = 0, n = 0;
@@ -93,6 +128,13 @@ extern "C" BVHGB_API const char *bvhgb_status_string(int s) {
 
 extern "C" BVHGB_API const char *bvhgb_last_error(void) { return g_last_error; }
 extern "C" BVHGB_API uint64_t bvhgb_launch_count(void) { return g_launches.load(); }
+
+extern "C" BVHGB_API int bvhgb_reset_device(void) {
+  // Cached per-context state (shared-memory opt-ins, symbol addresses) is keyed by context_id(),
+  // so the context made after this reset looks it all up again.
+  BVHGB_CUDA_TRY(cudaDeviceReset());
+  return BVHGB_OK;
+}
 
 extern "C" BVHGB_API int bvhgb_device_sync(void) {
   BVHGB_CUDA_TRY(cudaDeviceSynchronize());

@@ -126,6 +126,39 @@ __global__ void refit_kernel(bvhgb_node *t, uint32_t root, const uint32_t *__res
   refit_path(t, root, numNodes, toFix[i], counter, err);
 }
 
+// Full bottom-up refit (kFixTree1, Bittner13CUDA.cu:372-404): every leaf starts a climb; at each
+// inner node the first arrival stops and the second recomputes the box from both children and goes
+// on. The arrival counter is acq_rel, so the second arrival sees the first one's child box; child
+// boxes are read past L1. The last arrival resets the counter (the workspace keeps them at 0).
+__global__ void refit_full_kernel(bvhgb_node *t, uint32_t root, uint32_t numNodes, uint32_t *__restrict__ counter,
+                                  uint32_t *__restrict__ err) {
+  const uint32_t leaf = blockIdx.x * blockDim.x + threadIdx.x;
+  if (leaf >= numNodes || leaf == root || !__ldg(&t[leaf].isLeafFlag)) return;
+  uint32_t x = __ldg(&t[leaf].parent);
+  for (uint32_t steps = 0;; ++steps) {
+    if (x >= numNodes || steps > numNodes) {
+      atomicOr(err, kErrBadIndex);
+      return;
+    }
+    if (atom_add_acq_rel(&counter[x], 1u) == 0u) return;  // the sibling's climb is still on its way
+    counter[x] = 0u;
+    const uint32_t l = __ldcg(&t[x].left), r = __ldcg(&t[x].right);
+    if (l >= numNodes || r >= numNodes) {
+      atomicOr(err, kErrBadIndex);
+      return;
+    }
+    Box b = load_box_cg(t + l);
+    merge_into(b, load_box_cg(t + r));
+    float4 *p = reinterpret_cast<float4 *>(t + x);
+    const float4 w1 = __ldcg(p + 1);
+    p[0] = make_float4(b.mn[0], b.mn[1], b.mn[2], b.mx[0]);
+    p[1] = make_float4(b.mx[1], b.mx[2], w1.z, w1.w);
+    t[x].surfaceArea = surface_area(b);
+    if (x == root) return;
+    x = __ldcg(&t[x].parent);
+  }
+}
+
 // ---- isolated realised gain of one reinsertion (the learned scorer's training label) -----------
 // The patch changes the children of three nodes: the grand parent (its child becomes the sibling)
 // and the two reused nodes. A box changes iff its node lies on a path from one of them to the root
@@ -437,7 +470,7 @@ extern "C" BVHGB_API int bvhgb_bn13_create(const bvhgb_node *nodes, uint32_t num
   ws->root = root;
   ws->numChunks = ws->cfg.numChunks;
   const uint32_t lNum = (uint32_t)((bp / 100.0f) * (float)numNodes);  // Bittner13GPU.cpp:79-80
-  ws->chunkSize = lNum / ws->numChunks;
+  ws->chunkSize = ws->cfg.chunkSize ? ws->cfg.chunkSize : lNum / ws->numChunks;
   cudaStream_t s = as_stream(stream);
 
   // initData (Bittner13CUDA.cu:939-987): inner nodes in ascending index order.
@@ -580,6 +613,14 @@ extern "C" BVHGB_API int bvhgb_bn13_run(bvhgb_bn13_workspace *ws, bvhgb_node *no
     count_launch(ws->launchesKind[kind]);
     ++ws->iteration;
   }
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_bn13_refit(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, bvhgb_stream stream) {
+  if (!ws || !nodes) return BVHGB_INVALID_ARGUMENT;
+  const uint32_t n = ws->numNodes;
+  refit_full_kernel<<<ceil_div(n, 256u), 256, 0, as_stream(stream)>>>(nodes, ws->root, n, ws->counter, ws->err);
+  BVHGB_LAUNCH_CHECK("bn13 full refit");
   return BVHGB_OK;
 }
 

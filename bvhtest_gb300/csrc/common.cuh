@@ -140,6 +140,7 @@ void uncount_launches(uint64_t n);
 inline cudaStream_t as_stream(bvhgb_stream s) { return reinterpret_cast<cudaStream_t>(s); }
 inline uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 int sm_count();
+uint64_t context_id();
 }  // namespace bvhgb
 
 #define BVHGB_CUDA_TRY(call)                          \

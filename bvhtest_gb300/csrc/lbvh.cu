@@ -290,6 +290,24 @@ extern "C" BVHGB_API int bvhgb_lbvh_read_scene_box(bvhgb_lbvh_workspace *ws, bvh
   return BVHGB_OK;
 }
 
+extern "C" BVHGB_API int bvhgb_lbvh_set_scene_box(bvhgb_lbvh_workspace *ws, const bvhgb_aabb *scene,
+                                                  bvhgb_stream stream) {
+  if (!ws || !scene) return BVHGB_INVALID_ARGUMENT;
+  // The order-preserving integer image of each float, as the bounds kernel's atomics keep it.
+  const float f[6] = {scene->minMax[0].x, scene->minMax[0].y, scene->minMax[0].z,
+                      scene->minMax[1].x, scene->minMax[1].y, scene->minMax[1].z};
+  uint32_t h[6];
+  for (int k = 0; k < 6; ++k) {
+    uint32_t u;
+    std::memcpy(&u, &f[k], 4);
+    h[k] = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+  }
+  cudaStream_t s = as_stream(stream);
+  BVHGB_CUDA_TRY(cudaMemcpyAsync(ws->scene, h, sizeof(h), cudaMemcpyHostToDevice, s));
+  // The copy reads pageable host memory, so it is staged before the call returns.
+  return BVHGB_OK;
+}
+
 extern "C" BVHGB_API int bvhgb_lbvh_read_keys(bvhgb_lbvh_workspace *ws, int sorted, void *keys_host, uint32_t *idx_host,
                                               uint32_t n, bvhgb_stream stream) {
   int st = check_ws(ws, n);
@@ -325,6 +343,7 @@ extern "C" BVHGB_API int bvhgb_lbvh_read_errors(bvhgb_lbvh_workspace *ws, uint32
 // working memory from one array in this file, sized for BVHGB_STATIC_MAX_FACES triangles and
 // reserved on every GPU that loads the library until the process exits.
 #include <mutex>
+#include <vector>
 
 namespace bvhgb {
 namespace {
@@ -332,49 +351,45 @@ namespace {
 constexpr size_t kStaticScratchBytes = 12ull << 20;  // covers keys, values, slots and sort scratch
 __device__ __align__(256) unsigned char g_lbvh_static_scratch[kStaticScratchBytes];
 
-constexpr int kMaxDevices = 64;
+struct StaticBase {
+  uint64_t context;  // context_id() of the context the address belongs to
+  unsigned char *base;
+};
 std::mutex g_static_mutex;
-unsigned char *g_static_base[kMaxDevices] = {};
+std::vector<StaticBase> g_static_base;
 
 size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
 
-// Device address of the array on the current device, looked up once per device.
+// Device address of the array in the current context, looked up once per context: every device
+// has its own copy, and a device reset (cudaDeviceReset, bvhgb_reset_device) makes a new context
+// whose copy may sit elsewhere, so an address is never reused across contexts.
 int static_scratch(unsigned char **out) {
-  int dev = 0;
-  BVHGB_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return BVHGB_GENERIC_ERROR;
+  const uint64_t ctx = context_id();
   std::lock_guard<std::mutex> lock(g_static_mutex);
-  if (!g_static_base[dev]) {
-    void *p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_lbvh_static_scratch);
-    if (e != cudaSuccess) {
-      set_last_error("cudaGetSymbolAddress(g_lbvh_static_scratch)", e);
-      return BVHGB_CUDA_ERROR;
-    }
-    g_static_base[dev] = static_cast<unsigned char *>(p);
+  if (ctx != 0) {
+    for (const StaticBase &b : g_static_base)
+      if (b.context == ctx) {
+        *out = b.base;
+        return BVHGB_OK;
+      }
   }
-  *out = g_static_base[dev];
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_lbvh_static_scratch);
+  if (e != cudaSuccess) {
+    set_last_error("cudaGetSymbolAddress(g_lbvh_static_scratch)", e);
+    return BVHGB_CUDA_ERROR;
+  }
+  if (ctx != 0) g_static_base.push_back({ctx, static_cast<unsigned char *>(p)});
+  *out = static_cast<unsigned char *>(p);
   return BVHGB_OK;
 }
 
-}  // namespace
-}  // namespace bvhgb
-
-extern "C" BVHGB_API int bvhgb_lbvh_build_static(const float *vert, const uint32_t *faces, uint32_t numFaces,
-                                                 const bvhgb_lbvh_config *cfg, bvhgb_node *nodes,
-                                                 bvhgb_stream stream) {
-  const bvhgb_lbvh_config c = cfg ? *cfg : bvhgb_lbvh_config{30u, BVHGB_TOPO_REFCOMPAT};
-  if ((c.mortonBits != 30 && c.mortonBits != 63) || c.topology > BVHGB_TOPO_KARRAS) return BVHGB_INVALID_ARGUMENT;
-  if (numFaces > BVHGB_STATIC_MAX_FACES) return BVHGB_TOO_LARGE;
-  if (numFaces == 0) return BVHGB_OK;
-  if (!vert || !faces || !nodes) return BVHGB_INVALID_ARGUMENT;
+// The working memory of one build carved out of the array for the largest size: the same layout
+// for a build and for the read-back of its error bits.
+int static_workspace(const bvhgb_lbvh_config &c, bvhgb_lbvh_workspace &ws) {
   unsigned char *base = nullptr;
   int st = static_scratch(&base);
   if (st) return st;
-  st = sort_prepare();  // a function attribute, not an allocation
-  if (st) return st;
-  // Carve the working memory of one build for the largest size out of the array.
-  bvhgb_lbvh_workspace ws;
   ws.maxFaces = BVHGB_STATIC_MAX_FACES;
   ws.cfg = c;
   ws.keyBytes = c.mortonBits == 30 ? 4u : 8u;
@@ -394,11 +409,46 @@ extern "C" BVHGB_API int bvhgb_lbvh_build_static(const float *vert, const uint32
   ws.sortTempBytes = sort_temp_bytes(BVHGB_STATIC_MAX_FACES, ws.keyBytes, 0, c.mortonBits);
   ws.sortTemp = take(ws.sortTempBytes);
   if (off > kStaticScratchBytes) return BVHGB_GENERIC_ERROR;  // the array is sized for the worst case
+  return BVHGB_OK;
+}
+
+bool static_cfg_valid(const bvhgb_lbvh_config &c) {
+  return (c.mortonBits == 30 || c.mortonBits == 63) && c.topology <= BVHGB_TOPO_KARRAS;
+}
+
+}  // namespace
+}  // namespace bvhgb
+
+extern "C" BVHGB_API int bvhgb_lbvh_build_static(const float *vert, const uint32_t *faces, uint32_t numFaces,
+                                                 const bvhgb_lbvh_config *cfg, bvhgb_node *nodes,
+                                                 bvhgb_stream stream) {
+  const bvhgb_lbvh_config c = cfg ? *cfg : bvhgb_lbvh_config{30u, BVHGB_TOPO_REFCOMPAT};
+  if (!static_cfg_valid(c)) return BVHGB_INVALID_ARGUMENT;
+  if (numFaces > BVHGB_STATIC_MAX_FACES) return BVHGB_TOO_LARGE;
+  if (numFaces == 0) return BVHGB_OK;
+  if (!vert || !faces || !nodes) return BVHGB_INVALID_ARGUMENT;
+  bvhgb_lbvh_workspace ws;
+  int st = static_workspace(c, ws);
+  if (st) return st;
+  st = sort_prepare();  // a function attribute, not an allocation
+  if (st) return st;
   // The same phases as bvhgb_lbvh_build; every scratch word that must start at a known value is
-  // written by the phase that uses it (scene box init kernel, slot reset in the Morton kernel,
-  // the sort's memset of its counters), so the previous call's contents do not matter.
+  // written by the phase that uses it (scene box init kernel, which also clears the build's error
+  // word; slot reset in the Morton kernel; the sort's memset of its counters and error word), so
+  // the previous call's contents do not matter.
   if ((st = bvhgb_lbvh_init_tri_data(&ws, vert, faces, numFaces, stream))) return st;
   if ((st = bvhgb_lbvh_calc_morton(&ws, vert, faces, numFaces, stream))) return st;
   if ((st = bvhgb_lbvh_sort(&ws, numFaces, stream))) return st;
   return bvhgb_lbvh_build_tree(&ws, vert, faces, numFaces, nodes, stream);
 }
+
+extern "C" BVHGB_API int bvhgb_lbvh_static_read_errors(const bvhgb_lbvh_config *cfg, uint32_t *flags,
+                                                       bvhgb_stream stream) {
+  const bvhgb_lbvh_config c = cfg ? *cfg : bvhgb_lbvh_config{30u, BVHGB_TOPO_REFCOMPAT};
+  if (!flags || !static_cfg_valid(c)) return BVHGB_INVALID_ARGUMENT;
+  bvhgb_lbvh_workspace ws;
+  int st = static_workspace(c, ws);
+  if (st) return st;
+  return bvhgb_lbvh_read_errors(&ws, flags, stream);
+}
+

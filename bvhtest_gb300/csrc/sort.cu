@@ -20,6 +20,10 @@
 #include "common.cuh"
 #include "sort.cuh"
 
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
 namespace bvhgb {
 
 namespace {
@@ -337,16 +341,21 @@ cudaError_t set_smem_attr() {
 }  // namespace
 
 int sort_prepare() {
-  // Opt in to more than 48 KB of dynamic shared memory once per process (before any capture).
-  static int done = 0;
-  if (done) return BVHGB_OK;
+  // Opt in to more than 48 KB of dynamic shared memory. The attribute belongs to the context, so it
+  // is set once per context (another device, or the context after a device reset, sets it again);
+  // the first call on a context must come before any stream capture. Thread-safe.
+  static std::mutex m;
+  static std::vector<uint64_t> done;
+  const uint64_t ctx = context_id();
+  std::lock_guard<std::mutex> lock(m);
+  if (ctx != 0 && std::find(done.begin(), done.end(), ctx) != done.end()) return BVHGB_OK;
   BVHGB_CUDA_TRY((set_smem_attr<uint32_t, 256, 8>()));
   BVHGB_CUDA_TRY((set_smem_attr<uint32_t, 256, 16>()));
   BVHGB_CUDA_TRY((set_smem_attr<uint32_t, 512, 16>()));
   BVHGB_CUDA_TRY((set_smem_attr<uint64_t, 256, 8>()));
   BVHGB_CUDA_TRY((set_smem_attr<uint64_t, 256, 16>()));
   BVHGB_CUDA_TRY((set_smem_attr<uint64_t, 512, 16>()));
-  done = 1;
+  if (ctx != 0) done.push_back(ctx);
   return BVHGB_OK;
 }
 

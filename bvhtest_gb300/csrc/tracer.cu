@@ -226,6 +226,78 @@ __global__ void __launch_bounds__(128) trace_rays_kernel(const bvhgb_node *__res
   hits[i] = o;
 }
 
+// The reference's Ray (lib/base/Ray.hpp:38-80): origin, direction, 1 / direction, sign of the
+// inverse direction per axis, pixel coordinates. 48 bytes, 16-byte aligned.
+struct RefRay {
+  float pos[3], dir[3], inv[3];
+  uint8_t sign[3], pad;
+  uint32_t px, py;
+};
+static_assert(sizeof(RefRay) == 48, "Ray layout");
+
+// kGenerateRays (CUDAKernels.cu:43-59): one camera ray per pixel written as a Ray record
+// (Ray::set: 1 / dir and its signs).
+__global__ void gen_rays_kernel(RefRay *__restrict__ rays, CamParams cam) {
+  const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= cam.w || y >= cam.h) return;
+  RayPre r;
+  camera_ray(cam, x, y, r);
+  RefRay o;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    o.pos[k] = r.o[k];
+    o.dir[k] = r.d[k];
+    o.inv[k] = r.inv[k];
+    o.sign[k] = r.inv[k] < 0.0f ? 1 : 0;
+  }
+  o.pad = 0;
+  o.px = x;
+  o.py = y;
+  rays[(size_t)y * cam.w + x] = o;
+}
+
+// kTraceRay (CUDAKernels.cu:114-223) on caller-supplied Ray records: closest hit, the pixel
+// {hit, diffuse, intCount} and (optionally) (primId, t), one ray per pixel in record order.
+template <bool REC>
+__global__ void __launch_bounds__(128) trace_ray_image_kernel(const bvhgb_node *__restrict__ nodes,
+                                                              const TravNode *__restrict__ trav, uint32_t numNodes,
+                                                              uint32_t root, const float *__restrict__ vert,
+                                                              const uint32_t *__restrict__ faces,
+                                                              const RefRay *__restrict__ rays, uint32_t n,
+                                                              TraceParams tp, bvhgb_pixel *__restrict__ img,
+                                                              bvhgb_hit *__restrict__ hits) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 *rp = reinterpret_cast<const float4 *>(rays + i);
+  const float4 a = __ldg(rp), b = __ldg(rp + 1);
+  RayPre r;
+  r.o[0] = a.x; r.o[1] = a.y; r.o[2] = a.z;
+  r.d[0] = a.w; r.d[1] = b.x; r.d[2] = b.y;
+  setup_ray(r);
+  Hit h;
+  const uint32_t visits =
+      REC ? traverse_records(r, nodes, trav, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors)
+          : traverse(r, nodes, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
+  bvhgb_pixel px_out;
+  px_out.hit = 0;
+  px_out.diffuse = 0;
+  px_out.intCount = (uint16_t)visits;
+  if (h.prim != kNone) {
+    float v0[3], v1[3], v2[3];
+    load_tri(vert, faces, h.prim, v0, v1, v2);
+    px_out.hit = 1;
+    px_out.diffuse = shade(r, h.t, v0, v1, v2, tp.light);
+  }
+  img[i] = px_out;
+  if (hits) {
+    bvhgb_hit o;
+    o.primId = h.prim;
+    o.t = h.prim == kNone ? __int_as_float(0x7f800000) : h.t;
+    hits[i] = o;
+  }
+}
+
 __global__ void build_trav_kernel(const bvhgb_node *__restrict__ nodes, uint32_t numNodes, TravNode *__restrict__ out) {
   for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < numNodes; x += gridDim.x * blockDim.x)
     build_trav(nodes, numNodes, x, out, &g_trace_errors);
@@ -439,6 +511,33 @@ extern "C" BVHGB_API int bvhgb_tracer_trace_bounce(const bvhgb_tracer *tr, const
   if (!tr || !tr->nodes || !vert || !faces || !cam) return BVHGB_INVALID_ARGUMENT;
   return launch_bounce(tr->nodes, tr->trav, tr->numNodes, tr->root, vert, faces, cam, cfg, seed, offset, primary,
                        bounce, rayOrg, rayDir, as_stream(stream));
+}
+
+extern "C" BVHGB_API int bvhgb_generate_rays(void *rays, const bvhgb_camera *cam, bvhgb_stream stream) {
+  if (!rays || !cam) return BVHGB_INVALID_ARGUMENT;
+  if (cam->width == 0 || cam->height == 0) return BVHGB_OK;
+  if (reinterpret_cast<uintptr_t>(rays) % 16) return BVHGB_INVALID_ARGUMENT;
+  const CamParams cp = make_cam_params(cam);
+  dim3 block(16, 8);
+  dim3 grid(ceil_div(cam->width, 16), ceil_div(cam->height, 8));
+  gen_rays_kernel<<<grid, block, 0, as_stream(stream)>>>(static_cast<RefRay *>(rays), cp);
+  BVHGB_LAUNCH_CHECK("generate rays");
+  return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_trace_ray_image(const bvhgb_node *nodes, uint32_t numNodes, uint32_t root,
+                                              const float *vert, const uint32_t *faces, const void *rays, uint32_t n,
+                                              const bvhgb_trace_config *cfg, int bundle, bvhgb_pixel *img,
+                                              bvhgb_hit *hits, bvhgb_stream stream) {
+  if (!nodes || !vert || !faces || !rays || !img || numNodes == 0 || root >= numNodes) return BVHGB_INVALID_ARGUMENT;
+  if (reinterpret_cast<uintptr_t>(rays) % 16) return BVHGB_INVALID_ARGUMENT;
+  if (n == 0) return BVHGB_OK;
+  (void)bundle;  // both schedules give the same pixels; one kernel serves both
+  trace_ray_image_kernel<false><<<ceil_div(n, 128), 128, 0, as_stream(stream)>>>(
+      nodes, nullptr, numNodes, root, vert, faces, static_cast<const RefRay *>(rays), n, make_trace_params(cfg), img,
+      hits);
+  BVHGB_LAUNCH_CHECK("trace ray image");
+  return BVHGB_OK;
 }
 
 extern "C" BVHGB_API int bvhgb_trace_read_errors(uint32_t *flags, int reset) {

@@ -42,7 +42,7 @@ class LbvhConfig(C.Structure):
 class Bn13Config(C.Structure):
     _fields_ = [("numChunks", C.c_uint32), ("blockSize", C.c_uint32), ("batchPercent", C.c_float),
                 ("offsetAccess", C.c_uint32), ("heapCapacity", C.c_uint32), ("profileKernels", C.c_uint32),
-                ("searchMode", C.c_uint32)]
+                ("searchMode", C.c_uint32), ("chunkSize", C.c_uint32)]
 
 
 class Bn13Stats(C.Structure):
@@ -94,6 +94,7 @@ PROTOS = {
     "bvhgb_lbvh_sort": (I32, [VP, U32, VP]),
     "bvhgb_lbvh_build_tree": (I32, [VP, VP, VP, U32, VP, VP]),
     "bvhgb_lbvh_read_scene_box": (I32, [VP, C.POINTER(Aabb), VP]),
+    "bvhgb_lbvh_set_scene_box": (I32, [VP, C.POINTER(Aabb), VP]),
     "bvhgb_lbvh_read_keys": (I32, [VP, I32, VP, VP, U32, VP]),
     "bvhgb_lbvh_read_errors": (I32, [VP, C.POINTER(U32), VP]),
     "bvhgb_radix_sort_pairs": (I32, [VP, C.POINTER(SZ), VP, VP, VP, VP, U32, U32, U32, U32, VP]),
@@ -107,6 +108,7 @@ PROTOS = {
     "bvhgb_bn13_select_nodes": (I32, [VP, VP, VP]),
     "bvhgb_bn13_chunk": (I32, [VP, VP, U32, VP]),
     "bvhgb_bn13_get_stats": (I32, [VP, C.POINTER(Bn13Stats), VP]),
+    "bvhgb_bn13_refit": (I32, [VP, VP, VP]),
     "bvhgb_bn13_batch_size": (U32, [VP]),
     "bvhgb_bn13_launches_per_iteration": (U32, [VP]),
     "bvhgb_bn13_search_time": (I32, [VP, C.POINTER(F32), C.POINTER(U32)]),
@@ -144,6 +146,8 @@ PROTOS = {
     "bvhgb_trace_bounce": (I32, [VP, U32, U32, VP, VP, C.POINTER(Camera), C.POINTER(TraceConfig), U64, F32, VP, VP,
                                  VP, VP, VP]),
     "bvhgb_trace_read_errors": (I32, [C.POINTER(U32), I32]),
+    "bvhgb_generate_rays": (I32, [VP, C.POINTER(Camera), VP]),
+    "bvhgb_trace_ray_image": (I32, [VP, U32, U32, VP, VP, VP, U32, C.POINTER(TraceConfig), I32, VP, VP, VP]),
     "bvhgb_tracer_create": (I32, [U32, C.POINTER(VP)]),
     "bvhgb_tracer_destroy": (I32, [VP]),
     "bvhgb_tracer_update": (I32, [VP, VP, U32, U32, VP]),
@@ -160,6 +164,7 @@ PROTOS = {
     "bvhgb_free_mesh": (I32, [C.POINTER(MeshRaw)]),
     "bvhgb_fix_levels_host": (I32, [VP, U32, U32, C.POINTER(C.c_uint16)]),
     "bvhgb_device_sync": (I32, []),
+    "bvhgb_reset_device": (I32, []),
 }
 
 _lib = None

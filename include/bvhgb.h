@@ -150,23 +150,33 @@ BVHGB_API int bvhgb_lbvh_build_tree(bvhgb_lbvh_workspace *ws, const float *vert,
 /* Copies of intermediate device results (synchronous on 'stream'). keys: uint32 (30-bit) or
  * uint64 (63-bit) per face; sorted = after bvhgb_lbvh_sort. scene: 6 floats. */
 BVHGB_API int bvhgb_lbvh_read_scene_box(bvhgb_lbvh_workspace *ws, bvhgb_aabb *scene, bvhgb_stream stream);
+/* The scene box the Morton phase normalises by (LBVH_calcMortonCodes takes it as an argument,
+ * LBVH_CUDA.cu:168-183); bvhgb_lbvh_init_tri_data computes it, this call replaces it. */
+BVHGB_API int bvhgb_lbvh_set_scene_box(bvhgb_lbvh_workspace *ws, const bvhgb_aabb *scene, bvhgb_stream stream);
 BVHGB_API int bvhgb_lbvh_read_keys(bvhgb_lbvh_workspace *ws, int sorted, void *keys_host, uint32_t *idx_host,
                                    uint32_t numFaces, bvhgb_stream stream);
 /* Allocation-free LBVH build. No counterpart in the reference (its build allocates in
  * LBVH_allocateWorkingMemory and per call in LBVH_initTriData). For callers that cannot call
  * cudaMalloc while they build — a per-frame rebuild in a render or simulation loop, where an
  * allocation synchronises the device, or a host application that owns all device memory through
- * its own pool. Same result as bvhgb_lbvh_build (same kernels), but the working memory is one
- * 12 MiB file-scope device array that every GPU loading the library keeps until exit; nothing is
- * allocated and no allocating library routine is called. The caller still passes the mesh and the
- * node array (2 * numFaces - 1 nodes). Limits: numFaces <= BVHGB_STATIC_MAX_FACES, else
- * BVHGB_TOO_LARGE. All calls share the one array: calls that overlap on the GPU (other streams,
- * other host threads) race and must be serialised by the caller. The first call on each device
- * looks up the array's device address with that device current; make that first call before any
- * stream capture. */
+ * its own pool. Same node array as bvhgb_lbvh_build, but the working memory is one 12 MiB
+ * file-scope device array that every GPU loading the library keeps until exit; nothing is
+ * allocated and no allocating library routine is called. The array has no room for the per-face
+ * box records the allocating build keeps, so the tree kernel re-reads each leaf's face and three
+ * vertices instead of one 32-byte record: the result is the same, the memory traffic and time are
+ * not. The caller still passes the mesh and the node array (2 * numFaces - 1 nodes). Limits:
+ * numFaces <= BVHGB_STATIC_MAX_FACES, else BVHGB_TOO_LARGE. All calls share the one array: calls
+ * that overlap on the GPU (other streams, other host threads) race and must be serialised by the
+ * caller. The first call in each context (each device; again after a device reset) looks up the
+ * array's device address with that device current; make that first call before any stream
+ * capture. */
 #define BVHGB_STATIC_MAX_FACES 262144u
 BVHGB_API int bvhgb_lbvh_build_static(const float *vert, const uint32_t *faces, uint32_t numFaces,
                                       const bvhgb_lbvh_config *cfg, bvhgb_node *nodes, bvhgb_stream stream);
+/* The device error bits of the last bvhgb_lbvh_build_static call (same meaning as
+ * bvhgb_lbvh_read_errors; cfg: the configuration that call was given, which fixes where the sort
+ * keeps its error word in the shared array). Synchronous on 'stream'; 0 = the tree is valid. */
+BVHGB_API int bvhgb_lbvh_static_read_errors(const bvhgb_lbvh_config *cfg, uint32_t *flags, bvhgb_stream stream);
 /* Device error bits of the last build (4 = an inconsistent exchange slot was met and the build
  * stopped; 1 = the sort's look-back gave up); synchronous on 'stream'. 0 = the build is valid. */
 BVHGB_API int bvhgb_lbvh_read_errors(bvhgb_lbvh_workspace *ws, uint32_t *flags, bvhgb_stream stream);
@@ -209,6 +219,8 @@ typedef struct bvhgb_bn13_config {
   uint32_t heapCapacity; /* branch-and-bound queue entries per item (reference: 4096) */
   uint32_t profileKernels; /* 1: bracket every reinsertion-search launch with CUDA events */
   uint32_t searchMode;     /* BVHGB_SEARCH_BATCHED (0, default) or BVHGB_SEARCH_HEAP (1) */
+  uint32_t chunkSize;      /* items per chunk; 0: (batchPercent / 100 * numNodes) / numChunks
+                            * (Bittner13GPU.cpp:79-80); the reference's allocateMemory passes it */
 } bvhgb_bn13_config;
 
 /* Reinsertion search. HEAP: findNode1 (Bittner13CUDA.cu:141-191) one node at a time in the order of
@@ -240,6 +252,9 @@ BVHGB_API int bvhgb_bn13_run(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32
 /* bn13_selectNodes (:659-726) and bn13_rmAndReinsChunk (:729-766). */
 BVHGB_API int bvhgb_bn13_select_nodes(bvhgb_bn13_workspace *ws, const bvhgb_node *nodes, bvhgb_stream stream);
 BVHGB_API int bvhgb_bn13_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t chunk, bvhgb_stream stream);
+/* fixTree1 (Bittner13CUDA.cu:372-404, 641-648): recomputes every inner node's box and surface area
+ * bottom up from the leaves' boxes (all inner nodes, not only the paths a chunk dirtied). */
+BVHGB_API int bvhgb_bn13_refit(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, bvhgb_stream stream);
 /* calcNumSkipped (:806-821) and friends; synchronous on 'stream'. */
 BVHGB_API int bvhgb_bn13_get_stats(bvhgb_bn13_workspace *ws, bvhgb_bn13_stats *stats, bvhgb_stream stream);
 /* Number of items per iteration (numChunks * chunkSize, Bittner13GPU.cpp:90-92). */
@@ -464,6 +479,18 @@ BVHGB_API int bvhgb_tracer_trace_bounce(const bvhgb_tracer *tr, const float *ver
                                         float offset, const bvhgb_hit *primary, bvhgb_hit *bounce, float *rayOrg,
                                         float *rayDir, bvhgb_stream stream);
 
+/* generateRays (CUDAKernels.cu:43-59, 386-397): one primary ray per pixel written as the
+ * reference's 48-byte Ray record (lib/base/Ray.hpp:38-80: origin, direction, 1 / direction, signs,
+ * pixel x, y) into rays[y * width + x]; rays must be 16-byte aligned. */
+BVHGB_API int bvhgb_generate_rays(void *rays, const bvhgb_camera *cam, bvhgb_stream stream);
+/* tracerImage (CUDAKernels.cu:399-417): closest hit of each of the n Ray records, the pixel
+ * {hit, diffuse, intCount} into img[i] and (optional) (primId, t) into hits[i]. bundle selects the
+ * reference's block-cooperative schedule (rayBundles); the pixels do not depend on it. */
+BVHGB_API int bvhgb_trace_ray_image(const bvhgb_node *nodes, uint32_t numNodes, uint32_t root, const float *vert,
+                                    const uint32_t *faces, const void *rays, uint32_t n,
+                                    const bvhgb_trace_config *cfg, int bundle, bvhgb_pixel *img, bvhgb_hit *hits,
+                                    bvhgb_stream stream);
+
 /* Device-side traversal error bits seen since the last reset (2 = stack overflow, 4 = bad child
  * index); synchronous. */
 BVHGB_API int bvhgb_trace_read_errors(uint32_t *flags, int reset);
@@ -488,6 +515,11 @@ BVHGB_API int bvhgb_free_bvh(bvhgb_bvh_pointer *ptr);
 BVHGB_API int bvhgb_free_mesh(bvhgb_mesh_raw *mesh);
 /* BVH::fixLevels (BVH.cpp:39-70) on a host copy; returns the max level in *maxLevel. */
 BVHGB_API int bvhgb_fix_levels_host(bvhgb_node *nodes, uint32_t numNodes, uint32_t root, uint16_t *maxLevel);
+/* resetCUDA (cudaFN.cu:184-187): cudaDeviceReset of the current device. Every workspace, tracer
+ * and device array made on it before is gone; what the library caches per context (shared-memory
+ * opt-ins, the allocation-free build's array address) is looked up again in the new context, also
+ * after a cudaDeviceReset the caller makes itself. */
+BVHGB_API int bvhgb_reset_device(void);
 /* cudaDeviceSynchronize (LBVH_doCUDASyc, doCudaDevSync, tracerDoCudaSync). */
 BVHGB_API int bvhgb_device_sync(void);
 

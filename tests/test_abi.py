@@ -93,3 +93,25 @@ def test_every_entry_rejects_null_handles_without_crashing():
             assert r == 0, name
         else:
             assert r == 8, (name, r)  # BVHGB_INVALID_ARGUMENT
+
+
+def test_allocation_free_build_argument_checks_without_gpu():
+    """bvhgb_lbvh_build_static and its error read-back reject bad arguments on the host, before any
+    device call: nothing to build (numFaces = 0) is OK, missing buffers and bad configurations are
+    invalid arguments, sizes above the array's maximum are too large."""
+    from bvhtest_gb300 import native
+    lib = native.load()
+    build = lib.bvhgb_lbvh_build_static
+    build.restype = C.c_int
+    build.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(native.LbvhConfig), C.c_void_p, C.c_void_p]
+    read = lib.bvhgb_lbvh_static_read_errors
+    read.restype = C.c_int
+    read.argtypes = [C.POINTER(native.LbvhConfig), C.POINTER(C.c_uint32), C.c_void_p]
+    assert build(None, None, 0, None, None, None) == 0
+    assert build(None, None, 10, None, None, None) == 8
+    bad = native.LbvhConfig(31, 0)
+    assert build(None, None, 10, C.byref(bad), None, None) == 8
+    assert build(None, None, 262144 + 1, None, None, None) == 11
+    flags = C.c_uint32()
+    assert read(None, None, None) == 8
+    assert read(C.byref(bad), C.byref(flags), None) == 8

@@ -29,6 +29,16 @@ def _entry():
     return fn, native
 
 
+def _errors(native, cfg, stream):
+    """Device error bits the last static build left in the shared array (0 = valid tree)."""
+    fn = native.load().bvhgb_lbvh_static_read_errors
+    fn.restype = C.c_int
+    fn.argtypes = [C.POINTER(native.LbvhConfig), C.POINTER(C.c_uint32), C.c_void_p]
+    flags = C.c_uint32(0xFFFFFFFF)
+    assert fn(C.byref(cfg), C.byref(flags), stream) == 0
+    return flags.value
+
+
 def _mesh(n, seed):
     import torch
     vert, faces = scenes.uniform_soup(n, seed=seed)
@@ -49,6 +59,7 @@ def test_static_build_matches_allocating_build_on_consecutive_calls():
         st = build_static(C.c_void_p(v.data_ptr()), C.c_void_p(f.data_ptr()), n, C.byref(cfg),
                           C.c_void_p(out.data_ptr()), stream)
         assert st == 0, native.load().bvhgb_last_error()
+        assert _errors(native, cfg, stream) == 0, (n, bits, topo)
         torch.cuda.synchronize()
         assert torch.equal(out, expected), (n, bits, topo)
 
