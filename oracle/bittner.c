@@ -12,6 +12,7 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -676,8 +677,20 @@ static void run_iteration(orc_node *t, uint32_t root, const uint32_t *order, uin
   }
 }
 
+static double now_ms(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec * 1e3 + (double)ts.tv_nsec * 1e-6;
+}
+
 int orc_bittner_chunked(orc_node *t, uint32_t n_nodes, uint32_t root, uint32_t iters,
                         const orc_bn13_cfg *cfg, double *sah_trace, orc_bn13_stats *stats) {
+  return orc_bittner_chunked_until(t, n_nodes, root, iters, cfg, 0.0, sah_trace, NULL, stats, NULL);
+}
+
+int orc_bittner_chunked_until(orc_node *t, uint32_t n_nodes, uint32_t root, uint32_t iters,
+                              const orc_bn13_cfg *cfg, double stop_sah, double *sah_trace, double *iter_ms,
+                              orc_bn13_stats *stats, uint32_t *done) {
   uint32_t numc;
   const uint32_t csize = chunk_size(n_nodes, cfg, &numc);
   const uint32_t cap = cfg->heap_cap ? cfg->heap_cap : 4096;
@@ -696,7 +709,9 @@ int orc_bittner_chunked(orc_node *t, uint32_t n_nodes, uint32_t root, uint32_t i
   chunk_work_init(&w, n_nodes, csize, cap);
 
   if (sah_trace) sah_trace[0] = orc_sah(t, n_nodes, root);
-  for (uint32_t it = 0; it < iters; ++it) {
+  uint32_t it = 0;
+  for (; it < iters; ++it) {
+    const double t0 = now_ms();
     uint32_t n_order = n_inner;
     if (cfg->std_select) {
       /* Bittner13Par.cpp:421-437: nth_element + sort of the chunk-rounded batch over all nodes. */
@@ -712,8 +727,17 @@ int orc_bittner_chunked(orc_node *t, uint32_t n_nodes, uint32_t root, uint32_t i
       for (uint32_t j = 0; j < n_inner; ++j) order[j] = todo[j].idx;
       run_iteration(t, root, order, n_order, numc, csize, cap, cfg, &w, &st);
     }
-    if (sah_trace) sah_trace[it + 1] = orc_sah(t, n_nodes, root);
+    if (iter_ms) iter_ms[it] = now_ms() - t0;
+    if (sah_trace || stop_sah > 0.0) {
+      const double sah = orc_sah(t, n_nodes, root);
+      if (sah_trace) sah_trace[it + 1] = sah;
+      if (stop_sah > 0.0 && sah <= stop_sah) {
+        ++it;
+        break;
+      }
+    }
   }
+  if (done) *done = it;
   chunk_work_free(&w, &st);
   if (stats) *stats = st;
   free(inner); free(todo); free(order); free(order_all);

@@ -21,6 +21,14 @@ int orc_num_threads(void) {
 #endif
 }
 
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
 /* AABB::surfaceArea (lib/base/BVH.hpp:62-65): 2 * (dx*dy + dx*dz + dy*dz), each product and
  * sum rounded separately (the file is compiled with -ffp-contract=off). */
 float orc_surface_area(const orc_aabb *b) {

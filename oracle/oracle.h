@@ -146,6 +146,13 @@ typedef struct orc_bn13_stats {
 int orc_bittner_chunked(orc_node *nodes, uint32_t n_nodes, uint32_t root, uint32_t iters,
                         const orc_bn13_cfg *cfg, double *sah_trace, orc_bn13_stats *stats);
 
+/* The same, stopping after the first iteration whose SAH is <= stop_sah (when stop_sah > 0);
+ * iter_ms (optional, iters entries) gets each iteration's wall time without the SAH evaluation,
+ * *done the iterations run. */
+int orc_bittner_chunked_until(orc_node *nodes, uint32_t n_nodes, uint32_t root, uint32_t iters,
+                              const orc_bn13_cfg *cfg, double stop_sah, double *sah_trace, double *iter_ms,
+                              orc_bn13_stats *stats, uint32_t *done);
+
 /* One iteration of the chunked algorithm with a given batch order: order[pos] is the node at batch
  * position pos (the role of the sorted todo list). Used to check a GPU iteration whose selection
  * came from the learned scorer. */
@@ -217,6 +224,7 @@ uint8_t orc_shade(const float org[3], const float dir[3], float t, const float *
 /* ---- Misc ----------------------------------------------------------------------------------- */
 uint32_t orc_adler32(const uint8_t *data, size_t len);
 int orc_num_threads(void);
+void orc_set_threads(int n); /* OpenMP threads of later calls (n > 0) */
 
 #ifdef __cplusplus
 }

