@@ -67,6 +67,22 @@ uint64_t context_id() {
   return (uint64_t)id;
 }
 
+// Allocation-failure injection for tests of the error paths: after g_alloc_budget more successful
+// allocations the next one fails as if the device were out of memory (-1: off).
+std::atomic<int64_t> g_alloc_budget{-1};
+
+cudaError_t dev_malloc(void **p, size_t bytes) {
+  int64_t b = g_alloc_budget.load(std::memory_order_relaxed);
+  while (b >= 0) {
+    if (b == 0) {
+      *p = nullptr;
+      return cudaErrorMemoryAllocation;
+    }
+    if (g_alloc_budget.compare_exchange_weak(b, b - 1, std::memory_order_relaxed)) break;
+  }
+  return cudaMalloc(p, bytes);
+}
+
 int sm_count() {
   int dev = 0, n = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 148;
@@ -129,6 +145,12 @@ extern "C" BVHGB_API const char *bvhgb_status_string(int s) {
 extern "C" BVHGB_API const char *bvhgb_last_error(void) { return g_last_error; }
 extern "C" BVHGB_API uint64_t bvhgb_launch_count(void) { return g_launches.load(); }
 
+extern "C" BVHGB_API int bvhgb_debug_fail_allocations(int64_t after, int64_t *previous) {
+  const int64_t old = g_alloc_budget.exchange(after < 0 ? -1 : after, std::memory_order_relaxed);
+  if (previous) *previous = old;
+  return BVHGB_OK;
+}
+
 extern "C" BVHGB_API int bvhgb_reset_device(void) {
   // Cached per-context state (shared-memory opt-ins, symbol addresses) is keyed by context_id(),
   // so the context made after this reset looks it all up again.
@@ -170,9 +192,9 @@ extern "C" BVHGB_API int bvhgb_copy_mesh_to_gpu(const float *vert, uint32_t numV
   bvhgb_mesh_raw m{};
   cudaError_t e = cudaSuccess;
   size_t vb = 12ull * numVert, nb = 12ull * numNorm, fb = 12ull * numFaces;
-  if (e == cudaSuccess) e = cudaMalloc(&m.vert, vb ? vb : 16);
-  if (e == cudaSuccess) e = cudaMalloc(&m.norm, nb ? nb : 16);
-  if (e == cudaSuccess) e = cudaMalloc(&m.faces, fb ? fb : 16);
+  if (e == cudaSuccess) e = dev_malloc(&m.vert, vb ? vb : 16);
+  if (e == cudaSuccess) e = dev_malloc(&m.norm, nb ? nb : 16);
+  if (e == cudaSuccess) e = dev_malloc(&m.faces, fb ? fb : 16);
   if (e == cudaSuccess && vb) e = cudaMemcpy(m.vert, vert, vb, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && nb) e = cudaMemcpy(m.norm, norm, nb, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && fb) e = cudaMemcpy(m.faces, faces, fb, cudaMemcpyHostToDevice);
@@ -220,7 +242,7 @@ static int make_device_bvh(bvhgb_bvh_pointer *out, uint32_t numNodes, uint32_t r
   img.vCapacity = numNodes;
   img.vRootIndex = root;
   img.vMaxLevel = maxLevel;
-  BVHGB_CUDA_TRY(cudaMalloc(&out->bvh, sizeof(bvhgb_device_bvh)));
+  BVHGB_CUDA_TRY(dev_malloc(&out->bvh, sizeof(bvhgb_device_bvh)));
   BVHGB_CUDA_TRY(cudaMemcpy(out->bvh, &img, sizeof(img), cudaMemcpyHostToDevice));
   return BVHGB_OK;
 }
@@ -239,7 +261,7 @@ extern "C" BVHGB_API int bvhgb_copy_bvh_to_gpu(const bvhgb_node *nodes, uint32_t
   *out = bvhgb_bvh_pointer{};
   if (numNodes == 0) return BVHGB_OK;
   if (!nodes || root >= numNodes) return BVHGB_INVALID_ARGUMENT;
-  cudaError_t e = cudaMalloc(&out->nodes, sizeof(bvhgb_node) * (size_t)numNodes);
+  cudaError_t e = dev_malloc(&out->nodes, sizeof(bvhgb_node) * (size_t)numNodes);
   if (e == cudaSuccess) e = cudaMemcpy(out->nodes, nodes, sizeof(bvhgb_node) * (size_t)numNodes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     set_last_error("bvhgb_copy_bvh_to_gpu", e);
@@ -257,7 +279,7 @@ extern "C" BVHGB_API int bvhgb_allocate_bvh(bvhgb_bvh_pointer *out, uint32_t num
   if (out->bvh || out->nodes) return BVHGB_BVH_ERROR;  // LBVH_CUDA.cu:400
   if (numFaces >= (1u << 30)) return BVHGB_TOO_LARGE;
   uint32_t numNodes = 2 * numFaces - 1;
-  cudaError_t e = cudaMalloc(&out->nodes, sizeof(bvhgb_node) * (size_t)numNodes);
+  cudaError_t e = dev_malloc(&out->nodes, sizeof(bvhgb_node) * (size_t)numNodes);
   if (e != cudaSuccess) {
     set_last_error("bvhgb_allocate_bvh", e);
     out->nodes = nullptr;

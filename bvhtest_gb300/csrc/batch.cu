@@ -460,7 +460,7 @@ extern "C" BVHGB_API int bvhgb_batch_create(uint32_t numMeshes, const uint32_t *
   const size_t sortBytes = sort_temp_bytes((uint32_t)sortN, 8, 0, 32 + ws->meshBits);
   cudaError_t e = cudaSuccess;
   auto alloc = [&](auto **p, size_t bytes) {
-    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void **>(p), std::max<size_t>(bytes, 16));
+    if (e == cudaSuccess) e = dev_malloc(reinterpret_cast<void **>(p), std::max<size_t>(bytes, 16));
   };
   alloc(&ws->faceOff, 4 * (numMeshes + 1));
   alloc(&ws->nodeOff, 4 * (numMeshes + 1));

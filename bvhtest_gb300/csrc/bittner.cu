@@ -476,7 +476,7 @@ extern "C" BVHGB_API int bvhgb_bn13_create(const bvhgb_node *nodes, uint32_t num
   // initData (Bittner13CUDA.cu:939-987): inner nodes in ascending index order.
   std::vector<uint32_t> hflags(numNodes);
   uint32_t *dflag = nullptr;
-  cudaError_t e = cudaMalloc(&dflag, 4ull * numNodes);
+  cudaError_t e = dev_malloc(&dflag, 4ull * numNodes);
   if (e == cudaSuccess) {
     init_inner_kernel<<<min(ceil_div(numNodes, 256), 4096u), 256, 0, s>>>(nodes, numNodes, dflag);
     count_launch();
@@ -493,19 +493,19 @@ extern "C" BVHGB_API int bvhgb_bn13_create(const bvhgb_node *nodes, uint32_t num
   const size_t ni = inner.size() ? inner.size() : 1;
   const size_t cs = ws->chunkSize ? ws->chunkSize : 1;
   const size_t sortBytes = select_temp_bytes(ws->numInner, selection_count(ws));
-  if (e == cudaSuccess) e = cudaMalloc(&ws->inner, 4 * ni);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->keys, 4 * ni);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->vals, 4 * ni);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->todo, 4 * ni);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->sortTemp, sortBytes ? sortBytes : 256);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->patches, sizeof(PatchOut) * cs);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->valid, 4 * cs);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->toFix, 12 * cs);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->owner, 4ull * numNodes);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->counter, 4ull * numNodes);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->err, 4);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->heaps, sizeof(HeapItem) * cs * ws->cfg.heapCapacity);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->stats, sizeof(unsigned long long) * S_COUNT);
+  if (e == cudaSuccess) e = dev_malloc(&ws->inner, 4 * ni);
+  if (e == cudaSuccess) e = dev_malloc(&ws->keys, 4 * ni);
+  if (e == cudaSuccess) e = dev_malloc(&ws->vals, 4 * ni);
+  if (e == cudaSuccess) e = dev_malloc(&ws->todo, 4 * ni);
+  if (e == cudaSuccess) e = dev_malloc(&ws->sortTemp, sortBytes ? sortBytes : 256);
+  if (e == cudaSuccess) e = dev_malloc(&ws->patches, sizeof(PatchOut) * cs);
+  if (e == cudaSuccess) e = dev_malloc(&ws->valid, 4 * cs);
+  if (e == cudaSuccess) e = dev_malloc(&ws->toFix, 12 * cs);
+  if (e == cudaSuccess) e = dev_malloc(&ws->owner, 4ull * numNodes);
+  if (e == cudaSuccess) e = dev_malloc(&ws->counter, 4ull * numNodes);
+  if (e == cudaSuccess) e = dev_malloc(&ws->err, 4);
+  if (e == cudaSuccess) e = dev_malloc(&ws->heaps, sizeof(HeapItem) * cs * ws->cfg.heapCapacity);
+  if (e == cudaSuccess) e = dev_malloc(&ws->stats, sizeof(unsigned long long) * S_COUNT);
   if (e == cudaSuccess && inner.size())
     e = cudaMemcpyAsync(ws->inner, inner.data(), 4 * inner.size(), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ws->counter, 0, 4ull * numNodes, s);

@@ -141,6 +141,12 @@ inline cudaStream_t as_stream(bvhgb_stream s) { return reinterpret_cast<cudaStre
 inline uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 int sm_count();
 uint64_t context_id();
+// cudaMalloc through the library's allocation-failure injection (bvhgb_debug_fail_allocations).
+cudaError_t dev_malloc(void **p, size_t bytes);
+template <typename T>
+inline cudaError_t dev_malloc(T **p, size_t bytes) {
+  return dev_malloc(reinterpret_cast<void **>(p), bytes);
+}
 }  // namespace bvhgb
 
 #define BVHGB_CUDA_TRY(call)                          \

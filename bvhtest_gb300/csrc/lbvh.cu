@@ -178,14 +178,14 @@ extern "C" BVHGB_API int bvhgb_lbvh_create(uint32_t maxFaces, const bvhgb_lbvh_c
   const size_t m = maxFaces ? maxFaces : 1;
   ws->sortTempBytes = sort_temp_bytes(maxFaces, ws->keyBytes, 0, c.mortonBits);
   cudaError_t e = cudaSuccess;
-  if (e == cudaSuccess) e = cudaMalloc(&ws->scene, 256);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->keys, ws->keyBytes * m);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->keysSorted, ws->keyBytes * m);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->vals, 4 * m);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->valsSorted, 4 * m);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->slots, 4 * m);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->triBoxes, 32 * m);
-  if (e == cudaSuccess) e = cudaMalloc(&ws->sortTemp, ws->sortTempBytes ? ws->sortTempBytes : 256);
+  if (e == cudaSuccess) e = dev_malloc(&ws->scene, 256);
+  if (e == cudaSuccess) e = dev_malloc(&ws->keys, ws->keyBytes * m);
+  if (e == cudaSuccess) e = dev_malloc(&ws->keysSorted, ws->keyBytes * m);
+  if (e == cudaSuccess) e = dev_malloc(&ws->vals, 4 * m);
+  if (e == cudaSuccess) e = dev_malloc(&ws->valsSorted, 4 * m);
+  if (e == cudaSuccess) e = dev_malloc(&ws->slots, 4 * m);
+  if (e == cudaSuccess) e = dev_malloc(&ws->triBoxes, 32 * m);
+  if (e == cudaSuccess) e = dev_malloc(&ws->sortTemp, ws->sortTempBytes ? ws->sortTempBytes : 256);
   if (e != cudaSuccess) {
     set_last_error("bvhgb_lbvh_create", e);
     bvhgb_lbvh_destroy(ws);

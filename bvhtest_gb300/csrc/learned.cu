@@ -775,16 +775,16 @@ int lr_scratch_alloc(LrScratch &s, uint32_t numNodes) {
   lr_scratch_free(s);
   const size_t n = std::max(numNodes, 1u), ni = n / 2 + 1;
   cudaError_t e = cudaSuccess;
-  e = cudaMalloc(&s.ad, 8 * n);
-  if (e == cudaSuccess) e = cudaMalloc(&s.leafCount, 4 * n);
-  if (e == cudaSuccess) e = cudaMalloc(&s.sa, 4 * n);
-  if (e == cudaSuccess) e = cudaMalloc(&s.par, 4 * n);
-  if (e == cudaSuccess) e = cudaMalloc(&s.acc, 8 * n);
-  if (e == cudaSuccess) e = cudaMalloc(&s.err, 4);
-  if (e == cudaSuccess) e = cudaMalloc(&s.hist, 4 * kHistWords);
-  if (e == cudaSuccess) e = cudaMalloc(&s.pend, 16 * ni);
-  if (e == cudaSuccess) e = cudaMalloc(&s.x, 2ull * kIn * ni);
-  if (e == cudaSuccess) e = cudaMalloc(&s.y, 4 * ni);
+  e = dev_malloc(&s.ad, 8 * n);
+  if (e == cudaSuccess) e = dev_malloc(&s.leafCount, 4 * n);
+  if (e == cudaSuccess) e = dev_malloc(&s.sa, 4 * n);
+  if (e == cudaSuccess) e = dev_malloc(&s.par, 4 * n);
+  if (e == cudaSuccess) e = dev_malloc(&s.acc, 8 * n);
+  if (e == cudaSuccess) e = dev_malloc(&s.err, 4);
+  if (e == cudaSuccess) e = dev_malloc(&s.hist, 4 * kHistWords);
+  if (e == cudaSuccess) e = dev_malloc(&s.pend, 16 * ni);
+  if (e == cudaSuccess) e = dev_malloc(&s.x, 2ull * kIn * ni);
+  if (e == cudaSuccess) e = dev_malloc(&s.y, 4 * ni);
   if (e == cudaSuccess) e = cudaMemset(s.err, 0, 4);
   if (e != cudaSuccess) {
     set_last_error("lr_scratch_alloc", e);
@@ -891,7 +891,7 @@ int ensure_part(bvhgb_mlp *m, uint32_t tiles) {
   cudaFree(m->part);
   m->part = nullptr;
   m->partCap = 0;
-  BVHGB_CUDA_TRY(cudaMalloc(&m->part, 4ull * kMlpParams * std::max(tiles, 1u)));
+  BVHGB_CUDA_TRY(dev_malloc(&m->part, 4ull * kMlpParams * std::max(tiles, 1u)));
   m->partCap = std::max(tiles, 1u);
   return BVHGB_OK;
 }
@@ -901,7 +901,7 @@ int ensure_loss(bvhgb_mlp *m, uint32_t n) {
   cudaFree(m->loss);
   m->loss = nullptr;
   m->lossCap = 0;
-  BVHGB_CUDA_TRY(cudaMalloc(&m->loss, 4ull * std::max(n, 1u)));
+  BVHGB_CUDA_TRY(dev_malloc(&m->loss, 4ull * std::max(n, 1u)));
   m->lossCap = std::max(n, 1u);
   return BVHGB_OK;
 }
@@ -914,13 +914,13 @@ extern "C" BVHGB_API int bvhgb_mlp_create(uint64_t seed, bvhgb_mlp **out) {
   if (!out) return BVHGB_INVALID_ARGUMENT;
   *out = nullptr;
   auto *m = new bvhgb_mlp();
-  cudaError_t e = cudaMalloc(&m->p, 4 * kMlpParams);
-  if (e == cudaSuccess) e = cudaMalloc(&m->g, 4 * kMlpParams);
-  if (e == cudaSuccess) e = cudaMalloc(&m->m, 4 * kMlpParams);
-  if (e == cudaSuccess) e = cudaMalloc(&m->v, 4 * kMlpParams);
-  if (e == cudaSuccess) e = cudaMalloc(&m->pb, 2 * kMlpParams);
-  if (e == cudaSuccess) e = cudaMalloc(&m->stepDev, 4);
-  if (e == cudaSuccess) e = cudaMalloc(&m->err, 4);
+  cudaError_t e = dev_malloc(&m->p, 4 * kMlpParams);
+  if (e == cudaSuccess) e = dev_malloc(&m->g, 4 * kMlpParams);
+  if (e == cudaSuccess) e = dev_malloc(&m->m, 4 * kMlpParams);
+  if (e == cudaSuccess) e = dev_malloc(&m->v, 4 * kMlpParams);
+  if (e == cudaSuccess) e = dev_malloc(&m->pb, 2 * kMlpParams);
+  if (e == cudaSuccess) e = dev_malloc(&m->stepDev, 4);
+  if (e == cudaSuccess) e = dev_malloc(&m->err, 4);
   if (e == cudaSuccess) e = cudaMemset(m->err, 0, 4);
   if (e != cudaSuccess) {
     set_last_error("bvhgb_mlp_create", e);
@@ -1029,7 +1029,7 @@ extern "C" BVHGB_API int bvhgb_mlp_train(bvhgb_mlp *m, const uint16_t *x, const 
     cudaFree(m->idx);
     m->idx = nullptr;
     m->idxCap = 0;
-    BVHGB_CUDA_TRY(cudaMalloc(&m->idx, 4ull * batch));
+    BVHGB_CUDA_TRY(dev_malloc(&m->idx, 4ull * batch));
     m->idxCap = batch;
   }
   uint32_t step0 = 0;

@@ -39,6 +39,10 @@ constexpr uint32_t kValMask = (1u << 30) - 1u;
 // Predecessors read per look-back round trip. The tiles of a wave start together, so a tile k
 // places behind the last finished one needs about k / kLook round trips.
 constexpr int kLook = 16;
+// Polls of an unpublished predecessor before a tile gives up and raises kErrTimeout (the tile then
+// scatters with the partial prefix it has: positions below the true ones, so every write stays in
+// bounds). Adjustable for tests of that path (bvhgb_sort_set_spin_limit).
+__constant__ uint32_t g_lookback_spin_limit = kSpinLimit;
 
 // The last digit may be narrower than 8 bits when (endBit - beginBit) is not a multiple of 8.
 __host__ __device__ __forceinline__ uint32_t digit_mask(uint32_t shift, uint32_t endBit) {
@@ -219,7 +223,7 @@ __global__ void __launch_bounds__(THREADS, THREADS <= 256 ? 2 : 1) onesweep_kern
           const uint32_t *ps = status + (size_t)(pred - q) * kRadix + d;
           uint32_t spins = 0;
           while ((v[q] & kFlagMask) == 0u) {
-            if (++spins > kSpinLimit) {
+            if (++spins > g_lookback_spin_limit) {
               atomicOr(err, kErrTimeout);
               break;
             }
@@ -260,8 +264,13 @@ __global__ void __launch_bounds__(THREADS, THREADS <= 256 ? 2 : 1) onesweep_kern
     K k = sm.keys[i];
     uint32_t d = (uint32_t)(k >> shift) & mask;
     uint32_t dst = sm.globalBase[d] + (i - sm.tileStart[d]);
-    keysOut[dst] = k;
-    valsOut[dst] = sm.vals[i];
+    // Always true for a consistent sort; after a look-back timeout (err set) a later pass reads a
+    // permuted, partly stale key array whose digits no longer match the histogram, and this keeps
+    // its writes inside the arrays.
+    if (dst < n) {
+      keysOut[dst] = k;
+      valsOut[dst] = sm.vals[i];
+    }
   }
 }
 
@@ -356,6 +365,15 @@ int sort_prepare() {
   BVHGB_CUDA_TRY((set_smem_attr<uint64_t, 256, 16>()));
   BVHGB_CUDA_TRY((set_smem_attr<uint64_t, 512, 16>()));
   if (ctx != 0) done.push_back(ctx);
+  return BVHGB_OK;
+}
+
+int sort_set_spin_limit(uint32_t limit, uint32_t *previous) {
+  uint32_t old = 0;
+  BVHGB_CUDA_TRY(cudaMemcpyFromSymbol(&old, g_lookback_spin_limit, sizeof(old)));
+  const uint32_t v = limit == 0xFFFFFFFFu ? kSpinLimit : limit;
+  BVHGB_CUDA_TRY(cudaMemcpyToSymbol(g_lookback_spin_limit, &v, sizeof(v)));
+  if (previous) *previous = old;
   return BVHGB_OK;
 }
 
@@ -698,4 +716,8 @@ extern "C" BVHGB_API int bvhgb_sort_set_default_tile(uint32_t tileKeys, uint32_t
   const uint32_t old = tileKeys ? bvhgb::g_default_tile.exchange(tileKeys) : bvhgb::g_default_tile.load();
   if (previous) *previous = old;
   return BVHGB_OK;
+}
+
+extern "C" BVHGB_API int bvhgb_sort_set_spin_limit(uint32_t limit, uint32_t *previous) {
+  return bvhgb::sort_set_spin_limit(limit, previous);
 }

@@ -17,6 +17,8 @@ uint32_t *sort_error_word(void *temp, uint32_t n, uint32_t keyBytes, uint32_t be
 // default (kSortTileDefault unless bvhgb_sort_set_default_tile changed it).
 constexpr uint32_t kSortTileDefault = 8192;
 bool sort_tile_valid(uint32_t tileKeys);
+// Polls of an unpublished predecessor before a look-back gives up (0xFFFFFFFF: the default).
+int sort_set_spin_limit(uint32_t limit, uint32_t *previous);
 int sort_pairs(void *temp, const void *keysIn, void *keysOut, const uint32_t *valsIn, uint32_t *valsOut, uint32_t n,
                uint32_t keyBytes, uint32_t beginBit, uint32_t endBit, cudaStream_t s, uint32_t tileKeys = 0);
 // The values of the first k pairs of a stable ascending sort of (keys, vals), 32-bit keys, in that

@@ -459,7 +459,7 @@ extern "C" BVHGB_API int bvhgb_tracer_create(uint32_t maxNodes, bvhgb_tracer **o
   *out = nullptr;
   auto *tr = new bvhgb_tracer();
   tr->maxNodes = maxNodes;
-  const cudaError_t e = cudaMalloc(&tr->trav, sizeof(TravNode) * (size_t)maxNodes);
+  const cudaError_t e = dev_malloc(&tr->trav, sizeof(TravNode) * (size_t)maxNodes);
   if (e != cudaSuccess) {
     set_last_error("bvhgb_tracer_create", e);
     delete tr;

@@ -100,6 +100,8 @@ PROTOS = {
     "bvhgb_radix_sort_pairs": (I32, [VP, C.POINTER(SZ), VP, VP, VP, VP, U32, U32, U32, U32, VP]),
     "bvhgb_select_smallest_pairs": (I32, [VP, C.POINTER(SZ), VP, VP, VP, U32, U32, VP]),
     "bvhgb_sort_set_default_tile": (I32, [U32, C.POINTER(U32)]),
+    "bvhgb_sort_set_spin_limit": (I32, [U32, C.POINTER(U32)]),
+    "bvhgb_debug_fail_allocations": (I32, [C.c_int64, C.POINTER(C.c_int64)]),
     "bvhgb_calc_sah": (I32, [VP, U32, U32, C.POINTER(C.c_double), VP]),
     "bvhgb_bn13_create": (I32, [VP, U32, U32, C.POINTER(Bn13Config), C.POINTER(VP), VP]),
     "bvhgb_bn13_destroy": (I32, [VP]),

@@ -201,6 +201,16 @@ BVHGB_API int bvhgb_select_smallest_pairs(void *temp, size_t *tempBytes, const u
  * call. tileKeys = 0 only reads the setting. *previous (may be NULL) receives the old value. The
  * results do not depend on it. No counterpart in the reference (cub picks its own tiles). */
 BVHGB_API int bvhgb_sort_set_default_tile(uint32_t tileKeys, uint32_t *previous);
+/* Diagnostics of the failure paths (no counterpart in the reference). bvhgb_sort_set_spin_limit:
+ * how many times a sort tile polls a predecessor that has not published its digit counts before it
+ * gives up, sets the timeout bit (1) of the sort's error word (bvhgb_lbvh_read_errors) and scatters
+ * with the partial prefix it has (every write stays in bounds; the order is then not valid).
+ * 0xFFFFFFFF restores the default (2^24 polls with a short sleep); synchronous, not during stream
+ * capture. bvhgb_debug_fail_allocations: after 'after' more successful device allocations inside
+ * the library, the next one fails as out of memory (-1: off; *previous, may be NULL, gets the
+ * old budget). */
+BVHGB_API int bvhgb_sort_set_spin_limit(uint32_t limit, uint32_t *previous);
+BVHGB_API int bvhgb_debug_fail_allocations(int64_t after, int64_t *previous);
 
 /* ---- SAH (Bittner13CUDA.cu:776-803, BVH.cpp:23-37) ------------------------------------------- */
 
