@@ -321,6 +321,22 @@ def run_ours(args, w, rank, world, local):
         e.record(stream)
         return e
 
+    # The primary rays' traversal schedule, chosen by timing both on this tree (the reference's
+    # rayBundles option): one ray per thread, or a warp of neighbouring rays as one bundle.
+    tracer.update(nodes, num_nodes=n_nodes)
+    sched = {}
+    for bundles in (False, True):
+        for _ in range(2):
+            tracer.trace_image(vert, faces, cam, ray_bundles=bundles)
+        e0 = ev()
+        for _ in range(5):
+            tracer.trace_image(vert, faces, cam, ray_bundles=bundles)
+        e1 = ev()
+        torch.cuda.synchronize()
+        sched["bundle_ms" if bundles else "per_ray_ms"] = round(e0.elapsed_time(e1) / 5, 4)
+    use_bundles = sched["bundle_ms"] < sched["per_ray_ms"]
+    sched["chosen"] = "bundle" if use_bundles else "per_ray"
+
     def step():
         marks = [ev()]
         lbvh.init_tri_data(vert, faces)
@@ -334,7 +350,7 @@ def run_ours(args, w, rank, world, local):
         opt.run(w["iters"])
         marks.append(ev())
         tracer.update(nodes, num_nodes=n_nodes)  # traversal records of this tree, timed with the trace
-        img, hits = tracer.trace_image(vert, faces, cam)
+        img, hits = tracer.trace_image(vert, faces, cam, ray_bundles=use_bundles)
         bounce, _, _ = tracer.trace_bounce(vert, faces, cam, hits, seed=17)
         marks.append(ev())
         return marks, hits, bounce
@@ -442,6 +458,7 @@ def run_ours(args, w, rank, world, local):
         "build_ms": round(build_ms, 3), "optimize_ms": round(mean["optimize"], 3),
         "optimize_ms_per_iteration": round(mean["optimize"] / w["iters"], 4),
         "trace_ms": round(mean["trace"], 3), "mrays_per_s": round(mrays, 1), "rays_per_step": rays,
+        "primary_schedule": sched,
         "build_phase_ms": {k: round(mean[k], 4) for k in alg},
         "build_hbm_gbs": round(build_gbs, 1),
         "build_roofline": {"bound": "hbm", "achieved": round(build_gbs, 1), "peak": peak, "unit": "GB/s",

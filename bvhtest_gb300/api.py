@@ -380,15 +380,17 @@ def make_camera(pos, lookAt, up, fov, width, height) -> Camera:
                   int(height))
 
 
-def make_trace_config(light=(2.0, 2.0, 2.0), face_culling=False, tmin=0.0, tmax=float("inf")) -> TraceConfig:
-    return TraceConfig((C.c_float * 3)(*light), int(face_culling), float(tmin), float(tmax))
+def make_trace_config(light=(2.0, 2.0, 2.0), face_culling=False, tmin=0.0, tmax=float("inf"),
+                      ray_bundles=False) -> TraceConfig:
+    return TraceConfig((C.c_float * 3)(*light), int(face_culling), float(tmin), float(tmax), int(ray_bundles))
 
 
 def trace_image(nodes, vert, faces, camera: dict, root=0, light=(2.0, 2.0, 2.0), face_culling=False, with_hits=True,
-                num_nodes=None, stream=None):
-    """generateRays + tracerImage (CUDAKernels.cu:386-417): returns (pixels int32 [h*w], hits int64 [h*w] | None)."""
+                num_nodes=None, ray_bundles=False, stream=None):
+    """generateRays + tracerImage (CUDAKernels.cu:386-417): returns (pixels int32 [h*w], hits int64 [h*w] | None).
+    ray_bundles: warps traverse as bundles (the reference's rayBundles); same hits."""
     cam = make_camera(**camera)
-    cfg = make_trace_config(light, face_culling)
+    cfg = make_trace_config(light, face_culling, ray_bundles=ray_bundles)
     npx = cam.width * cam.height
     img = torch.empty(npx, dtype=torch.int32, device="cuda")
     hits = torch.empty(npx, dtype=torch.int64, device="cuda") if with_hits else None
@@ -456,9 +458,9 @@ class Tracer:
         return self
 
     def trace_image(self, vert, faces, camera: dict, light=(2.0, 2.0, 2.0), face_culling=False, with_hits=True,
-                    stream=None):
+                    ray_bundles=False, stream=None):
         cam = make_camera(**camera)
-        cfg = make_trace_config(light, face_culling)
+        cfg = make_trace_config(light, face_culling, ray_bundles=ray_bundles)
         npx = cam.width * cam.height
         img = torch.empty(npx, dtype=torch.int32, device="cuda")
         hits = torch.empty(npx, dtype=torch.int64, device="cuda") if with_hits else None

@@ -38,6 +38,8 @@ __global__ void cost_kernel(const bvhgb_node *__restrict__ t, const uint32_t *__
   }
 }
 
+// One thread per batch item: the reference's per-thread searches, findNode1 (HEAP) or findNode2 (ALT).
+template <int MODE>
 __global__ void patch_kernel(const bvhgb_node *__restrict__ t, uint32_t root, const uint32_t *__restrict__ todo,
                              uint32_t numTodo, uint32_t chunk, uint32_t numChunks, uint32_t chunkSize,
                              uint32_t offsetAccess, PatchOut *__restrict__ out, uint32_t *__restrict__ valid,
@@ -62,8 +64,8 @@ __global__ void patch_kernel(const bvhgb_node *__restrict__ t, uint32_t root, co
   const uint32_t node = ok ? __ldg(todo + pos) : kNone;
   const Heap pq{heapTop + (threadIdx.x & (kSearchThreads - 1)), heaps + (size_t)k * cap};
   ok = ok && remove_node(p, node, ins, un, g);
-  ok = ok && reinsert<false>(p, ins[0], un[0], true, pq, cap, ctr);
-  ok = ok && reinsert<false>(p, ins[1], un[1], false, pq, cap, ctr);
+  ok = ok && reinsert<MODE>(p, ins[0], un[0], true, pq, cap, ctr);
+  ok = ok && reinsert<MODE>(p, ins[1], un[1], false, pq, cap, ctr);
   if (p.bad) {
     atomicOr(err, kErrBadIndex);
     ok = false;
@@ -273,8 +275,8 @@ __global__ void __launch_bounds__(kWarpItemsPerBlock * 32) gain_warp_kernel(
   const Heap unused{nullptr, nullptr};
   bool ok = x < numNodes;
   ok = ok && remove_node(p, x, ins, un, g);
-  ok = ok && reinsert<true>(p, ins[0], un[0], true, unused, 0, ctr);
-  ok = ok && reinsert<true>(p, ins[1], un[1], false, unused, 0, ctr);
+  ok = ok && reinsert<BVHGB_SEARCH_BATCHED>(p, ins[0], un[0], true, unused, 0, ctr);
+  ok = ok && reinsert<BVHGB_SEARCH_BATCHED>(p, ins[1], un[1], false, unused, 0, ctr);
   if (p.bad) ok = false;
   float v = 0.0f;
   if (ok) v = isolated_gain(p, g, un[0], un[1], ok);
@@ -382,9 +384,14 @@ int run_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t c, cudaStrea
   } else {
     // One warp per block: these searches are latency-bound, so spreading them over more SMs beats
     // packing them (CUDABlockSize only sizes the other kernels; results do not depend on it).
-    patch_kernel<<<ceil_div(cs, kSearchThreads), kSearchThreads, 0, s>>>(
-        nodes, ws->root, ws->todo, ws->numInner, c, ws->numChunks, cs, ws->cfg.offsetAccess, ws->patches, ws->valid,
-        ws->toFix, ws->owner, ws->heaps, ws->cfg.heapCapacity, ws->stats, ws->numNodes, ws->err);
+    if (ws->cfg.searchMode == BVHGB_SEARCH_ALT)
+      patch_kernel<BVHGB_SEARCH_ALT><<<ceil_div(cs, kSearchThreads), kSearchThreads, 0, s>>>(
+          nodes, ws->root, ws->todo, ws->numInner, c, ws->numChunks, cs, ws->cfg.offsetAccess, ws->patches,
+          ws->valid, ws->toFix, ws->owner, ws->heaps, ws->cfg.heapCapacity, ws->stats, ws->numNodes, ws->err);
+    else
+      patch_kernel<BVHGB_SEARCH_HEAP><<<ceil_div(cs, kSearchThreads), kSearchThreads, 0, s>>>(
+          nodes, ws->root, ws->todo, ws->numInner, c, ws->numChunks, cs, ws->cfg.offsetAccess, ws->patches,
+          ws->valid, ws->toFix, ws->owner, ws->heaps, ws->cfg.heapCapacity, ws->stats, ws->numNodes, ws->err);
   }
   BVHGB_LAUNCH_CHECK("bn13 patch");
   if (prof) BVHGB_CUDA_TRY(record_event(ws->evStop[c], s));
@@ -450,7 +457,7 @@ extern "C" BVHGB_API int bvhgb_bn13_create(const bvhgb_node *nodes, uint32_t num
   *out = nullptr;
   auto *ws = new bvhgb_bn13_workspace();
   ws->cfg = cfg ? *cfg : bvhgb_bn13_config{32u, 128u, 1.0f, 0u, 4096u, 0u, BVHGB_SEARCH_BATCHED};
-  if (ws->cfg.searchMode > BVHGB_SEARCH_HEAP) {
+  if (ws->cfg.searchMode > BVHGB_SEARCH_ALT) {
     delete ws;
     return BVHGB_INVALID_ARGUMENT;
   }
@@ -504,7 +511,9 @@ extern "C" BVHGB_API int bvhgb_bn13_create(const bvhgb_node *nodes, uint32_t num
   if (e == cudaSuccess) e = dev_malloc(&ws->owner, 4ull * numNodes);
   if (e == cudaSuccess) e = dev_malloc(&ws->counter, 4ull * numNodes);
   if (e == cudaSuccess) e = dev_malloc(&ws->err, 4);
-  if (e == cudaSuccess) e = dev_malloc(&ws->heaps, sizeof(HeapItem) * cs * ws->cfg.heapCapacity);
+  // Only the heap search keeps a queue in global memory (entries beyond the shared-memory top).
+  const size_t heapItems = ws->cfg.searchMode == BVHGB_SEARCH_HEAP ? cs * ws->cfg.heapCapacity : 1;
+  if (e == cudaSuccess) e = dev_malloc(&ws->heaps, sizeof(HeapItem) * heapItems);
   if (e == cudaSuccess) e = dev_malloc(&ws->stats, sizeof(unsigned long long) * S_COUNT);
   if (e == cudaSuccess && inner.size())
     e = cudaMemcpyAsync(ws->inner, inner.data(), 4 * inner.size(), cudaMemcpyHostToDevice, s);

@@ -279,6 +279,88 @@ __device__ uint32_t find_node(const Patch &p, uint32_t n, const Heap &pq, uint32
   return best;
 }
 
+// findNode2 (Bittner13CUDA.cu:194-264), the approximate search of altFindNode: kAltQueue (cost,
+// node) slots, empty = +inf. Each step pops the first slot of smallest cost; an expanded node's
+// left child takes the popped slot and its right child the slot the previous scan found to hold
+// the largest cost (the first empty one while there is one, else the worst entry, which is lost);
+// a scan in which no cost exceeds 0 keeps the previous max slot. One thread per item; the slots
+// live in registers (the scans are unrolled, the two writes select by index).
+constexpr uint32_t kAltQueue = 16;  // CUDA_ALT_QUEUE_SIZE (Bittner13CUDA.hpp:30)
+
+__device__ uint32_t find_node2(const Patch &p, uint32_t n, SearchCounters &ctr) {
+  const float kInf = __int_as_float(0x7f800000);
+  float best_cost = kInf;
+  uint32_t best = 0;
+  const Box nbox = tree_box(p.t, p.chk(n));
+  const float sarea = tree_sa(p.t, p.chk(n));
+  float co[kAltQueue];
+  uint32_t nl[kAltQueue];
+#pragma unroll
+  for (uint32_t i = 0; i < kAltQueue; ++i) {
+    co[i] = kInf;
+    nl[i] = 0;
+  }
+  uint32_t mnI = 0, mxI = 1;
+  float mn = 0.0f;
+  nl[0] = p.root;
+  co[0] = 0.0f;
+  for (uint32_t it = 0; mn < kInf; ++it) {
+    if (it > p.numNodes) {  // only a corrupted tree gets here
+      p.bad = true;
+      break;
+    }
+    uint32_t cur = 0;
+    float cc = 0.0f;
+#pragma unroll
+    for (uint32_t i = 0; i < kAltQueue; ++i)
+      if (i == mnI) {
+        cur = nl[i];
+        cc = co[i];
+        co[i] = kInf;
+      }
+    if (fadd(cc, sarea) >= best_cost) break;
+    ctr.visits++;
+    const NodeP cn = p.get_subset(cur);
+    Box b = p.get_aabb(cur);
+    float induced = fmul(-1.0f, surface_area(b));
+    merge_into(b, nbox);
+    const float direct = surface_area(b);
+    const float total = fadd(cc, direct);
+    if (total < best_cost) {
+      best_cost = total;
+      best = cur;
+    }
+    induced = fadd(induced, total);
+    if (fadd(induced, sarea) < best_cost && !cn.isLeafFlag) {
+#pragma unroll
+      for (uint32_t i = 0; i < kAltQueue; ++i) {
+        if (i == mnI) {
+          nl[i] = cn.left;
+          co[i] = induced;
+        }
+        if (i == mxI) {  // after the left child: the same slot takes the right one
+          nl[i] = cn.right;
+          co[i] = induced;
+        }
+      }
+    }
+    mn = kInf;
+    float mx = 0.0f;
+#pragma unroll
+    for (uint32_t i = 0; i < kAltQueue; ++i) {
+      if (co[i] < mn) {
+        mn = co[i];
+        mnI = i;
+      }
+      if (co[i] > mx) {
+        mx = co[i];
+        mxI = i;
+      }
+    }
+  }
+  return best;
+}
+
 // removeNode (Bittner13CUDA.cu:267-305).
 __device__ bool remove_node(Patch &p, uint32_t x, uint32_t ins[2], uint32_t un[2], uint32_t &g_out) {
   if (tree_leaf(p.t, p.chk(x)) || x == p.root) return false;
@@ -589,10 +671,14 @@ __device__ uint32_t find_node_batched(const Patch &p, uint32_t n, SearchCounters
 }
 
 // reinsert (Bittner13CUDA.cu:308-358).
-template <bool BATCHED>
+// MODE: BVHGB_SEARCH_BATCHED (warp-cooperative), BVHGB_SEARCH_HEAP (findNode1) or
+// BVHGB_SEARCH_ALT (findNode2).
+template <int MODE>
 __device__ bool reinsert(Patch &p, uint32_t x, uint32_t unused, bool update, const Heap &pq, uint32_t cap,
                          SearchCounters &ctr) {
-  const uint32_t best = BATCHED ? find_node_batched(p, x, ctr) : find_node(p, x, pq, cap, ctr);
+  const uint32_t best = MODE == BVHGB_SEARCH_BATCHED ? find_node_batched(p, x, ctr)
+                        : MODE == BVHGB_SEARCH_ALT   ? find_node2(p, x, ctr)
+                                                     : find_node(p, x, pq, cap, ctr);
   if (best == p.root) return false;
   const uint32_t bpi = p.index(best);
   uint32_t sb;
@@ -654,8 +740,8 @@ __device__ __forceinline__ void warp_patch_item(const bvhgb_node *__restrict__ t
   uint32_t ins[2], un[2], g = kNone;
   const Heap unused{nullptr, nullptr};
   ok = ok && remove_node(p, node, ins, un, g);
-  ok = ok && reinsert<true>(p, ins[0], un[0], true, unused, 0, ctr);
-  ok = ok && reinsert<true>(p, ins[1], un[1], false, unused, 0, ctr);
+  ok = ok && reinsert<BVHGB_SEARCH_BATCHED>(p, ins[0], un[0], true, unused, 0, ctr);
+  ok = ok && reinsert<BVHGB_SEARCH_BATCHED>(p, ins[1], un[1], false, unused, 0, ctr);
   if (p.bad) ok = false;
   __syncwarp();
   if (lane != 0) return;

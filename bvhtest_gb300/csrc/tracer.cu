@@ -165,7 +165,9 @@ __global__ void __launch_bounds__(128) trace_bounce_kernel(const bvhgb_node *__r
   out[pix] = o;
 }
 
-template <bool REC>
+// BUNDLE: the warp traverses as one bundle of rays (traverse_bundle, the reference's rayBundles);
+// otherwise each ray on its own. Same hits either way.
+template <bool REC, bool BUNDLE>
 __global__ void __launch_bounds__(128) trace_image_kernel(const bvhgb_node *__restrict__ nodes,
                                                           const TravNode *__restrict__ trav, uint32_t numNodes,
                                                           uint32_t root, const float *__restrict__ vert,
@@ -174,13 +176,18 @@ __global__ void __launch_bounds__(128) trace_image_kernel(const bvhgb_node *__re
                                                           bvhgb_hit *__restrict__ hits) {
   const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= cam.w || y >= cam.h) return;
+  const bool active = x < cam.w && y < cam.h;
+  if (!BUNDLE && !active) return;  // a bundle keeps its whole warp in the traversal
   RayPre r;
-  camera_ray(cam, x, y, r);
+  camera_ray(cam, active ? x : 0u, active ? y : 0u, r);
   Hit h;
   const uint32_t visits =
-      REC ? traverse_records(r, nodes, trav, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors)
-          : traverse(r, nodes, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
+      BUNDLE ? traverse_bundle<REC>(r, active, nodes, trav, numNodes, root, vert, faces, tp.tmin, tp.tmax,
+                                    tp.cull != 0, h, &g_trace_errors)
+      : REC  ? traverse_records(r, nodes, trav, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h,
+                                &g_trace_errors)
+             : traverse(r, nodes, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
+  if (!active) return;
   bvhgb_pixel px_out;
   px_out.hit = 0;
   px_out.diffuse = 0;
@@ -259,7 +266,7 @@ __global__ void gen_rays_kernel(RefRay *__restrict__ rays, CamParams cam) {
 
 // kTraceRay (CUDAKernels.cu:114-223) on caller-supplied Ray records: closest hit, the pixel
 // {hit, diffuse, intCount} and (optionally) (primId, t), one ray per pixel in record order.
-template <bool REC>
+template <bool REC, bool BUNDLE>
 __global__ void __launch_bounds__(128) trace_ray_image_kernel(const bvhgb_node *__restrict__ nodes,
                                                               const TravNode *__restrict__ trav, uint32_t numNodes,
                                                               uint32_t root, const float *__restrict__ vert,
@@ -268,8 +275,9 @@ __global__ void __launch_bounds__(128) trace_ray_image_kernel(const bvhgb_node *
                                                               TraceParams tp, bvhgb_pixel *__restrict__ img,
                                                               bvhgb_hit *__restrict__ hits) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float4 *rp = reinterpret_cast<const float4 *>(rays + i);
+  const bool active = i < n;
+  if (!BUNDLE && !active) return;  // a bundle keeps its whole warp in the traversal
+  const float4 *rp = reinterpret_cast<const float4 *>(rays + (active ? i : 0u));
   const float4 a = __ldg(rp), b = __ldg(rp + 1);
   RayPre r;
   r.o[0] = a.x; r.o[1] = a.y; r.o[2] = a.z;
@@ -277,8 +285,12 @@ __global__ void __launch_bounds__(128) trace_ray_image_kernel(const bvhgb_node *
   setup_ray(r);
   Hit h;
   const uint32_t visits =
-      REC ? traverse_records(r, nodes, trav, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors)
-          : traverse(r, nodes, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
+      BUNDLE ? traverse_bundle<REC>(r, active, nodes, trav, numNodes, root, vert, faces, tp.tmin, tp.tmax,
+                                    tp.cull != 0, h, &g_trace_errors)
+      : REC  ? traverse_records(r, nodes, trav, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h,
+                                &g_trace_errors)
+             : traverse(r, nodes, numNodes, root, vert, faces, tp.tmin, tp.tmax, tp.cull != 0, h, &g_trace_errors);
+  if (!active) return;
   bvhgb_pixel px_out;
   px_out.hit = 0;
   px_out.diffuse = 0;
@@ -372,12 +384,16 @@ int launch_image(const bvhgb_node *nodes, const TravNode *trav, uint32_t numNode
   const CamParams cp = make_cam_params(cam);
   dim3 block(16, 8);
   dim3 grid(ceil_div(cam->width, 16), ceil_div(cam->height, 8));
-  if (trav)
-    trace_image_kernel<true><<<grid, block, 0, s>>>(nodes, trav, numNodes, root, vert, faces, cp, make_trace_params(cfg),
-                                                    img, hits);
+  const TraceParams tp = make_trace_params(cfg);
+  const bool bundle = cfg && cfg->rayBundles;
+  if (trav && bundle)
+    trace_image_kernel<true, true><<<grid, block, 0, s>>>(nodes, trav, numNodes, root, vert, faces, cp, tp, img, hits);
+  else if (trav)
+    trace_image_kernel<true, false><<<grid, block, 0, s>>>(nodes, trav, numNodes, root, vert, faces, cp, tp, img, hits);
+  else if (bundle)
+    trace_image_kernel<false, true><<<grid, block, 0, s>>>(nodes, trav, numNodes, root, vert, faces, cp, tp, img, hits);
   else
-    trace_image_kernel<false><<<grid, block, 0, s>>>(nodes, trav, numNodes, root, vert, faces, cp,
-                                                     make_trace_params(cfg), img, hits);
+    trace_image_kernel<false, false><<<grid, block, 0, s>>>(nodes, trav, numNodes, root, vert, faces, cp, tp, img, hits);
   BVHGB_LAUNCH_CHECK("trace image");
   return BVHGB_OK;
 }
@@ -532,10 +548,13 @@ extern "C" BVHGB_API int bvhgb_trace_ray_image(const bvhgb_node *nodes, uint32_t
   if (!nodes || !vert || !faces || !rays || !img || numNodes == 0 || root >= numNodes) return BVHGB_INVALID_ARGUMENT;
   if (reinterpret_cast<uintptr_t>(rays) % 16) return BVHGB_INVALID_ARGUMENT;
   if (n == 0) return BVHGB_OK;
-  (void)bundle;  // both schedules give the same pixels; one kernel serves both
-  trace_ray_image_kernel<false><<<ceil_div(n, 128), 128, 0, as_stream(stream)>>>(
-      nodes, nullptr, numNodes, root, vert, faces, static_cast<const RefRay *>(rays), n, make_trace_params(cfg), img,
-      hits);
+  const TraceParams tp = make_trace_params(cfg);
+  if (bundle || (cfg && cfg->rayBundles))
+    trace_ray_image_kernel<false, true><<<ceil_div(n, 128), 128, 0, as_stream(stream)>>>(
+        nodes, nullptr, numNodes, root, vert, faces, static_cast<const RefRay *>(rays), n, tp, img, hits);
+  else
+    trace_ray_image_kernel<false, false><<<ceil_div(n, 128), 128, 0, as_stream(stream)>>>(
+        nodes, nullptr, numNodes, root, vert, faces, static_cast<const RefRay *>(rays), n, tp, img, hits);
   BVHGB_LAUNCH_CHECK("trace ray image");
   return BVHGB_OK;
 }

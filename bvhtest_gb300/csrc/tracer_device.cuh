@@ -318,5 +318,131 @@ __device__ __forceinline__ uint32_t traverse_records(const RayPre &r, const bvhg
   return visits;
 }
 
+// ---- ray bundles ---------------------------------------------------------------------------------
+// kTraceRayBundle (CUDAKernels.cu:240-383) traverses the tree once for a block of 64 rays: a node
+// is visited when any ray of the block hits it, the nearer child first by a vote of the rays. Here
+// the bundle is a warp (32 neighbouring primary rays): each lane tests its own ray against both
+// children of the warp's node (the node record is one broadcast load), __any_sync decides whether
+// the warp goes down a side, a majority ballot picks the near side, and the stack is warp-uniform
+// (each lane keeps its own entry distance of a pushed node, +inf where its ray missed it, so a pop
+// is skipped when no lane can still improve). A lane tests a leaf's triangles only where its own
+// ray hits the leaf's box. Every lane thus tests a superset of what its own traversal would test,
+// and the closest-hit rule (smallest t, then smallest primitive) picks the same hit; the visit
+// count (intCount) is the warp's. All lanes of the warp must call it; inactive lanes pass active =
+// false and get no hit. REC: traversal records (true) or the node array (false).
+template <bool REC>
+__device__ __forceinline__ uint32_t traverse_bundle(const RayPre &r, bool active, const bvhgb_node *__restrict__ nodes,
+                                                    const TravNode *__restrict__ trav, uint32_t numNodes,
+                                                    uint32_t root, const float *__restrict__ vert,
+                                                    const uint32_t *__restrict__ faces, float tmin, float tmax,
+                                                    bool cull, Hit &h, uint32_t *err) {
+  const float kInf = __int_as_float(0x7f800000);
+  uint32_t stN[kStack];
+  float stT[kStack];
+  int sp = 0;
+  uint32_t visits = 0;
+  h.prim = kNone;
+  h.t = tmax;
+  float4 a, b, c;
+  load_node(nodes, root, a, b, c);
+  float tn;
+  const bool hitRoot = active && box_hit(r, a, b, tmin, tmax, tn);
+  if (!__any_sync(0xFFFFFFFFu, hitRoot)) return 0;
+  if (__float_as_uint(c.y) & 0xFFFFu) {
+    if (hitRoot) test_leaf(r, vert, faces, __float_as_uint(b.w), __float_as_uint(c.x), tmin, tmax, cull, h);
+    return 0;
+  }
+  uint32_t cur = root;
+  for (uint32_t it = 0;; ++it) {
+    if (it > numNodes) {  // each node is visited at most once per warp: a cyclic (corrupted) input
+      if (active) atomicOr(err, kErrBadIndex);
+      break;
+    }
+    ++visits;
+    float4 l0, l1, r0, r1;
+    uint32_t lref, rref, lcnt, rcnt;
+    bool ok = true;
+    if (REC) {
+      const float4 *q = reinterpret_cast<const float4 *>(trav + cur);
+      const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2);
+      const uint4 q3 = __ldg(reinterpret_cast<const uint4 *>(q + 3));
+      l0 = q0;
+      l1 = make_float4(q1.x, q1.y, 0.0f, 0.0f);
+      r0 = make_float4(q1.z, q1.w, q2.x, q2.y);
+      r1 = make_float4(q2.z, q2.w, 0.0f, 0.0f);
+      lref = q3.x;
+      rref = q3.y;
+      lcnt = q3.z;
+      rcnt = q3.w;
+    } else {
+      float4 ca, cb, cc;
+      load_node(nodes, cur, ca, cb, cc);
+      const uint32_t li = __float_as_uint(cb.w), ri = __float_as_uint(cc.x);
+      ok = li < numNodes && ri < numNodes;
+      float4 lc, rc;
+      if (ok) {
+        load_node(nodes, li, l0, l1, lc);
+        load_node(nodes, ri, r0, r1, rc);
+        const bool ll = (__float_as_uint(lc.y) & 0xFFFFu) != 0, rl = (__float_as_uint(rc.y) & 0xFFFFu) != 0;
+        lref = ll ? __float_as_uint(l1.w) : li;
+        rref = rl ? __float_as_uint(r1.w) : ri;
+        lcnt = ll ? __float_as_uint(lc.x) : 0u;
+        rcnt = rl ? __float_as_uint(rc.x) : 0u;
+      }
+    }
+    if (!ok) {
+      if (active) atomicOr(err, kErrBadIndex);
+    } else {
+      float lim = h.prim == kNone ? tmax : fmul(h.t, kBestSlack);
+      float tl = kInf, tr = kInf;
+      bool hl = active && box_hit(r, l0, l1, tmin, lim, tl);
+      bool hr = active && box_hit(r, r0, r1, tmin, lim, tr);
+      if (hl && lcnt) {
+        test_leaf(r, vert, faces, lref, lcnt, tmin, tmax, cull, h);
+        hl = false;
+      }
+      if (hr && rcnt) {
+        test_leaf(r, vert, faces, rref, rcnt, tmin, tmax, cull, h);
+        hr = false;
+      }
+      lim = h.prim == kNone ? tmax : fmul(h.t, kBestSlack);
+      hl = hl && tl <= lim;
+      hr = hr && tr <= lim;
+      const bool anyL = __any_sync(0xFFFFFFFFu, hl), anyR = __any_sync(0xFFFFFFFFu, hr);
+      if (anyL && anyR) {
+        const int wantL = __popc(__ballot_sync(0xFFFFFFFFu, hl && (!hr || tl <= tr)));
+        const int wantR = __popc(__ballot_sync(0xFFFFFFFFu, hr && (!hl || tr < tl)));
+        const bool lfirst = wantL >= wantR;
+        if (sp < kStack) {
+          stN[sp] = lfirst ? rref : lref;
+          stT[sp] = lfirst ? (hr ? tr : kInf) : (hl ? tl : kInf);
+          ++sp;
+        } else if (active) {
+          atomicOr(err, kErrStackOverflow);
+        }
+        cur = lfirst ? lref : rref;
+        continue;
+      }
+      if (anyL || anyR) {
+        cur = anyL ? lref : rref;
+        continue;
+      }
+    }
+    // Pop the next subtree that some lane can still improve on.
+    bool found = false;
+    while (sp > 0) {
+      --sp;
+      const float lim = h.prim == kNone ? tmax : fmul(h.t, kBestSlack);
+      if (__any_sync(0xFFFFFFFFu, active && stT[sp] <= lim)) {
+        cur = stN[sp];
+        found = true;
+        break;
+      }
+    }
+    if (!found) break;
+  }
+  return active ? visits : 0u;
+}
+
 }  // namespace
 }  // namespace bvhgb

@@ -634,9 +634,12 @@ class Bittner13GPU : public Command {
       error("sort = false is not supported (the reference reports the same: Bittner13CUDA.cu:719)");
       return ErrorCode::GENERIC_ERROR;
     }
-    if (vAltFindNode) warn("altFindNode: the reference's approximate 16-slot queue is not built; using the searchMode search");
-    bvhgb_bn13_config cfg{vNumChunks, vBlockSize, vBatchPercent, vOffsetAccess ? 1u : 0u, 4096u, 0u,
-                          vSearch == "heap" ? (uint32_t)BVHGB_SEARCH_HEAP : (uint32_t)BVHGB_SEARCH_BATCHED};
+    // altFindNode selects the reference's approximate 16-slot search (findNode2); otherwise
+    // searchMode picks the batched (default) or the heap (findNode1) search.
+    const uint32_t mode = vAltFindNode || vSearch == "alt" ? (uint32_t)BVHGB_SEARCH_ALT
+                          : vSearch == "heap"              ? (uint32_t)BVHGB_SEARCH_HEAP
+                                                           : (uint32_t)BVHGB_SEARCH_BATCHED;
+    bvhgb_bn13_config cfg{vNumChunks, vBlockSize, vBatchPercent, vOffsetAccess ? 1u : 0u, 4096u, 0u, mode};
     ErrorCode e = from_status(bvhgb_bn13_create(s.cudaBVH.nodes, s.cudaBVH.numNodes, s.root, &cfg, &vWs, nullptr));
     if (e != ErrorCode::OK || vScorer.empty()) return e;
     // learned selection: weights relative to the base path unless absolute
@@ -712,7 +715,6 @@ class CUDATracer : public Command {
  protected:
   ErrorCode setup(State &s) override {
     if (s.cameras.empty()) return ErrorCode::WARNING;  // CUDATracer.cpp:76-77
-    if (vRayBundles) warn("rayBundles: the block-cooperative traversal is not built; tracing per ray");
     return ErrorCode::OK;
   }
   ErrorCode runImpl(State &s) override;
@@ -865,7 +867,8 @@ ErrorCode CUDATracer::runImpl(State &s) {
     cam.fov = c.fov;
     cam.width = c.width;
     cam.height = c.height;
-    bvhgb_trace_config tc{{vLight[0], vLight[1], vLight[2]}, vFaceCulling ? 1u : 0u, 0.0f, INFINITY};
+    bvhgb_trace_config tc{{vLight[0], vLight[1], vLight[2]}, vFaceCulling ? 1u : 0u, 0.0f, INFINITY,
+                          vRayBundles ? 1u : 0u};
     const size_t npx = (size_t)c.width * c.height;
     bvhgb_pixel *img = nullptr;
     bvhgb_hit *hits = nullptr;

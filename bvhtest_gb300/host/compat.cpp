@@ -87,7 +87,7 @@ bool bn13_ready(GPUWorkingMemory *data, CUDAMemoryBVHPointer *bvh, const AlgoCFG
   c.batchPercent = 1.0f;
   c.offsetAccess = cfg.offsetAccess ? 1u : 0u;
   c.heapCapacity = 4096;  // CUDA_QUEUE_SIZE (Bittner13CUDA.hpp:29)
-  c.searchMode = BVHGB_SEARCH_BATCHED;
+  c.searchMode = cfg.altFindNode ? BVHGB_SEARCH_ALT : BVHGB_SEARCH_BATCHED;  // findNode2 or the batched search
   c.chunkSize = cfg.chunkSize ? cfg.chunkSize : h->chunkSize;
   if (!ok(bvhgb_bn13_create(reinterpret_cast<bvhgb_node *>(bvh->nodes), bvh->numNodes, root_of(bvh), &c, &h->ws,
                             nullptr),
@@ -363,11 +363,12 @@ void tracerImage(Ray *_rays, CUDAPixel *_img, BVHNode *_nodes, uint32_t _rootNod
                  uint32_t _w, uint32_t _h, bool _bundle) {
   if (!_rays || !_img || !_nodes || _mesh.numFaces == 0) return;
   const char *two = std::getenv("BVHGB_COMPAT_TWO_SIDED");
-  bvhgb_trace_config cfg{{_light.x, _light.y, _light.z}, (two && two[0] == '1') ? 0u : 1u, 0.0f, INFINITY};
+  bvhgb_trace_config cfg{{_light.x, _light.y, _light.z}, (two && two[0] == '1') ? 0u : 1u, 0.0f, INFINITY,
+                         _bundle ? 1u : 0u};
   const uint32_t numNodes = 2 * _mesh.numFaces - 1;  // the most nodes a tree over numFaces faces has
   ok(bvhgb_trace_ray_image(reinterpret_cast<bvhgb_node *>(_nodes), numNodes, _rootNode,
                            reinterpret_cast<const float *>(_mesh.vert), reinterpret_cast<const uint32_t *>(_mesh.faces),
-                           _rays, _w * _h, &cfg, _bundle ? 1 : 0, reinterpret_cast<bvhgb_pixel *>(_img), nullptr,
+                           _rays, _w * _h, &cfg, 0, reinterpret_cast<bvhgb_pixel *>(_img), nullptr,
                            nullptr),
      "tracerImage");
 }

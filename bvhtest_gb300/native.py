@@ -56,7 +56,8 @@ class Camera(C.Structure):
 
 
 class TraceConfig(C.Structure):
-    _fields_ = [("light", C.c_float * 3), ("faceCulling", C.c_uint32), ("tmin", C.c_float), ("tmax", C.c_float)]
+    _fields_ = [("light", C.c_float * 3), ("faceCulling", C.c_uint32), ("tmin", C.c_float), ("tmax", C.c_float),
+                ("rayBundles", C.c_uint32)]
 
 
 class BatchConfig(C.Structure):

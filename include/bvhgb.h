@@ -228,7 +228,7 @@ typedef struct bvhgb_bn13_config {
   uint32_t offsetAccess; /* offsetAccess = false */
   uint32_t heapCapacity; /* branch-and-bound queue entries per item (reference: 4096) */
   uint32_t profileKernels; /* 1: bracket every reinsertion-search launch with CUDA events */
-  uint32_t searchMode;     /* BVHGB_SEARCH_BATCHED (0, default) or BVHGB_SEARCH_HEAP (1) */
+  uint32_t searchMode;     /* BVHGB_SEARCH_BATCHED (0, default), BVHGB_SEARCH_HEAP (1) or BVHGB_SEARCH_ALT (2) */
   uint32_t chunkSize;      /* items per chunk; 0: (batchPercent / 100 * numNodes) / numChunks
                             * (Bittner13GPU.cpp:79-80); the reference's allocateMemory passes it */
 } bvhgb_bn13_config;
@@ -238,7 +238,10 @@ typedef struct bvhgb_bn13_config {
  * pruning evaluated 32 lowest-bound frontier nodes per round by a warp per item (frontier of 128
  * kept ordered by (cost, node)); it finds the same positions in practice at a fraction of the
  * latency. Both are deterministic and restated by the oracle. */
-enum { BVHGB_SEARCH_BATCHED = 0, BVHGB_SEARCH_HEAP = 1 };
+enum { BVHGB_SEARCH_BATCHED = 0, BVHGB_SEARCH_HEAP = 1, BVHGB_SEARCH_ALT = 2 };
+/* ALT: findNode2 (Bittner13CUDA.cu:194-264), the reference's altFindNode: an approximate search
+ * in a fixed queue of 16 slots whose worst entry is overwritten when it is full, one thread per
+ * item; cheaper per item, worse positions (the SAH it reaches is reported beside findNode1's). */
 
 typedef struct bvhgb_bn13_stats {
   uint64_t items;            /* batch items processed */
@@ -447,6 +450,10 @@ typedef struct bvhgb_trace_config {
   uint32_t faceCulling; /* CUDA_FACE_CULLING: front faces only */
   float tmin;           /* hits need t > tmin (0) */
   float tmax;           /* ... and t <= tmax (+inf) */
+  uint32_t rayBundles;  /* rayBundles (CUDATracer.cpp:31-40): image traces run a warp of 32
+                         * neighbouring rays as one bundle through the tree (the reference's
+                         * kTraceRayBundle, CUDAKernels.cu:240-383); same hits, intCount counts the
+                         * bundle's visits. Secondary and arbitrary rays always trace one by one. */
 } bvhgb_trace_config;
 
 /* generateRays + tracerImage (CUDAKernels.cu:386-417) fused: one primary ray per pixel,

@@ -462,9 +462,65 @@ static uint32_t gpu_find_node_batched(const bpatch *p, uint32_t n, uint64_t *ove
 }
 
 /* reinsert (Bittner13CUDA.cu:308-358). mode 0: batched search, 1: findNode1 heap order. */
+/* findNode2 (Bittner13CUDA.cu:194-264, the same as Bittner13Par.cpp:131-187 with its queue of
+ * altFindNodeQueueSize entries): the approximate search of altFindNode. A fixed array of qsize
+ * (cost, node) slots, empty = +inf; each step pops the first slot of smallest cost; an expanded
+ * node's left child takes the popped slot and its right child the slot that the previous scan
+ * found to hold the largest cost (the first empty one while there is one, else the worst entry,
+ * which is dropped); the scan keeps its previous max slot when no cost exceeds 0. */
+#define ALT_QUEUE_MAX 64
+static uint32_t gpu_find_node_alt(const bpatch *p, uint32_t n, uint32_t qsize, uint64_t *visits) {
+  float best_cost = INFINITY;
+  uint32_t best = 0;
+  const orc_node *nd = &p->t[n];
+  orc_aabb nbox = nd->bbox;
+  float sarea = nd->surfaceArea;
+  float co[ALT_QUEUE_MAX];
+  uint32_t nl[ALT_QUEUE_MAX];
+  if (qsize > ALT_QUEUE_MAX) qsize = ALT_QUEUE_MAX;
+  for (uint32_t i = 0; i < qsize; ++i) { co[i] = INFINITY; nl[i] = 0; }
+  uint32_t mn_i = 0, mx_i = 1;
+  float mn = 0.0f;
+  nl[0] = p->root;
+  co[0] = 0.0f;
+  while (mn < INFINITY) {
+    const uint32_t cur = nl[mn_i];
+    const float cc = co[mn_i];
+    co[mn_i] = INFINITY;
+    if (cc + sarea >= best_cost) break;
+    if (visits) (*visits)++;
+    npatch cn = bp_get_subset(p, cur);
+    orc_aabb b = bp_get_aabb(p, cur);
+    float induced = -1.0f * orc_surface_area(&b);
+    merge_into(&b, &nbox);
+    float direct = orc_surface_area(&b);
+    float total = cc + direct;
+    if (total < best_cost) {
+      best_cost = total;
+      best = cur;
+    }
+    induced = induced + total;
+    if (induced + sarea < best_cost && !cn.isLeafFlag) {
+      nl[mn_i] = cn.left;
+      nl[mx_i] = cn.right;
+      co[mn_i] = induced;
+      co[mx_i] = induced;
+    }
+    mn = INFINITY;
+    float mx = 0.0f;
+    for (uint32_t i = 0; i < qsize; ++i) {
+      if (co[i] < mn) { mn = co[i]; mn_i = i; }
+      if (co[i] > mx) { mx = co[i]; mx_i = i; }
+    }
+  }
+  return best;
+}
+
 static int gpu_reinsert(bpatch *p, uint32_t x, uint32_t unused, int update, hitem *pq, uint32_t cap,
                         uint64_t *overflow, int mode, uint64_t *visits) {
-  uint32_t best = mode == 0 ? gpu_find_node_batched(p, x, overflow, visits) : gpu_find_node(p, x, pq, cap, overflow);
+  uint32_t best = mode == 0   ? gpu_find_node_batched(p, x, overflow, visits)
+                  : mode == 2 ? gpu_find_node_alt(p, x, cap, visits)
+                              : gpu_find_node(p, x, pq, cap, overflow);
   if (best == p->root) return 0;
   uint32_t bpi = bp_index(p, best);
   npatch *b;

@@ -115,7 +115,9 @@ typedef struct orc_bn13_cfg {
   float batch_percent;   /* batchPercent (1.0) */
   uint32_t offset_access;/* offsetAccess */
   uint32_t heap_cap;     /* B&B heap capacity (the reference uses 4096) */
-  uint32_t search_mode;  /* 0: batched best-first (32 per round, frontier 128); 1: findNode1 heap */
+  uint32_t search_mode;  /* 0: batched best-first (32 per round, frontier 128); 1: findNode1 heap;
+                          * 2: findNode2, the approximate queue of altFindNode (heap_cap = its
+                          *    number of slots: 16 on the GPU, Bittner13CUDA.hpp:30) */
   uint32_t conflict_rule;/* 0: an item is applied iff it holds the lowest batch rank on every node it
                           *    patches, failed items' claims included (the GPU kernels);
                           * 1: items are taken in batch order and an item is applied iff none of its

@@ -9,7 +9,8 @@ Contents (all trees start from the oracle's LBVH, which equals the GPU's bit for
   c1_*  uniform 65,536 triangles (seed 1), 30-bit refCompat LBVH:
         Bittner13 (sequential) and Bittner13Par (32 chunks, 1 thread) for 100 iterations at 1%:
         the reference's own float SAH after every iteration, the SHA-256 of the final node array
-        (levels fixed by the reference's teardown), Bittner13Par's skip count;
+        (levels fixed by the reference's teardown), Bittner13Par's skip count; Bittner13Par with
+        altFindNode (16 queue slots) for 20 iterations: tree hash and skip count;
         the camera's 512 x 512 primary rays (SHA-256 of directions) and the CPUTracer image
         (SHA-256 of the grey values, the inner-node visit counts and the hit mask).
   c2_*  large scene (4,194,304 triangles, seed 2), 63-bit karras LBVH: Bittner13 and Bittner13Par
@@ -38,6 +39,7 @@ from oracle import refpy  # noqa: E402
 
 OUT = Path(__file__).with_name("ref_pin.npz")
 C1_ITERS = 100
+C1_ALT_ITERS = 20  # Bittner13Par with altFindNode (the 16-slot queue of findNode2)
 C2_ITERS = 200
 C5_ITERS = 20
 THREADS = os.cpu_count() or 1
@@ -70,6 +72,10 @@ def part_c1(out):
     out["c1_par_sha"] = sha(b)
     out["c1_par_skipped"] = np.uint32(sk)
     out["c1_par_total"] = np.uint32(tot)
+    c, _, sk, _, st = refpy.bittner13par(nodes, C1_ALT_ITERS, alt_find_node=True, alt_queue=16, threads=1)
+    assert st == 0
+    out["c1_par_alt_sha"] = sha(c)
+    out["c1_par_alt_skipped"] = np.uint32(sk)
     cam = scenes.camera_default()
     c = (cam["pos"], cam["lookAt"], cam["up"], cam["fov"], cam["width"], cam["height"])
     _, dirs = refpy.camera_rays(*c)

@@ -51,10 +51,10 @@ def _cam():
     return c["pos"], c["lookAt"], c["up"], c["fov"], c["width"], c["height"]
 
 
-def _par(orc, nodes, iters, **kw):
+def _par(orc, nodes, iters, search_mode=1, heap_cap=16384, **kw):
     """The oracle's chunked algorithm with the reference CPU twin's rules (heap search, first-come
     conflicts, standard-library selection order), levels fixed as Bittner13Par's teardown does."""
-    out, trace, st = orc.bittner_chunked(nodes, iters, search_mode=1, heap_cap=16384, conflict_rule=1,
+    out, trace, st = orc.bittner_chunked(nodes, iters, search_mode=search_mode, heap_cap=heap_cap, conflict_rule=1,
                                          std_select=1, **kw)
     orc.fix_levels(out)
     return out, trace, st
@@ -81,6 +81,13 @@ def test_chunked_optimizer_equals_reference_fixture(orc, pin, c1):
     assert st["skipped_conflict"] + st["skipped_invalid"] == int(pin["c1_par_skipped"])
     assert st["items"] == int(pin["c1_par_total"])
     assert np.allclose(trace, pin["c1_par_sah"], rtol=5e-5, atol=0)
+
+
+def test_alt_find_node_equals_reference_fixture(orc, pin, c1):
+    # findNode2 (the approximate 16-slot queue of altFindNode) with Bittner13Par's rules
+    out, _, st = _par(orc, c1[2], 20, search_mode=2, heap_cap=16)
+    assert np.array_equal(_sha(out), pin["c1_par_alt_sha"])
+    assert st["skipped_conflict"] + st["skipped_invalid"] == int(pin["c1_par_alt_skipped"])
 
 
 def test_camera_and_tracer_equal_reference_fixture(orc, pin, c1):
@@ -122,6 +129,16 @@ def test_live_chunked_optimizer(orc, ref, c1, threads):
     assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
     assert sk == stats["skipped_conflict"] + stats["skipped_invalid"]
     assert tot == stats["items"]
+
+
+@pytest.mark.parametrize("slots", [16, 4, 32])
+def test_live_alt_find_node(orc, ref, c1, slots):
+    """altFindNode: findNode2's fixed queue (Bittner13Par.cpp:131-187) restated by the oracle."""
+    a, _, sk, _, st = ref.bittner13par(c1[2], 10, alt_find_node=True, alt_queue=slots, threads=1)
+    assert st == 0
+    b, _, stats = _par(orc, c1[2], 10, search_mode=2, heap_cap=slots)
+    assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
+    assert sk == stats["skipped_conflict"] + stats["skipped_invalid"]
 
 
 def test_live_offset_access(orc, ref, c1):

@@ -165,3 +165,34 @@ def test_prepared_tracer_gives_the_same_hits(gpu):
             tr.update(nodes, num_nodes=n_nodes)
     assert gpu.trace_errors() == 0
     tr.close()
+
+
+@pytest.mark.parametrize("cull", [False, True])
+def test_ray_bundles_give_the_per_ray_hits(gpu, orc, cull):
+    """rayBundles (the reference's kTraceRayBundle, CUDAKernels.cu:240-383): a warp of neighbouring
+    primary rays traverses as one bundle; every ray still gets the closest hit of its own
+    traversal (and of the brute force), on the node array and on the traversal records, for a
+    camera whose image edges leave partial warps."""
+    import torch
+    vert, faces, v, f, nodes = _scene(gpu, 30000, seed=9)
+    n_nodes = 2 * 30000 - 1
+    cam = dict(scenes.camera_default(), width=203, height=117)
+    tr = gpu.Tracer(n_nodes).update(nodes, num_nodes=n_nodes)
+    img_a, hits_a = gpu.trace_image(nodes, v, f, cam, num_nodes=n_nodes, face_culling=cull)
+    img_b, hits_b = gpu.trace_image(nodes, v, f, cam, num_nodes=n_nodes, face_culling=cull, ray_bundles=True)
+    img_c, hits_c = tr.trace_image(v, f, cam, face_culling=cull, ray_bundles=True)
+    torch.cuda.synchronize()
+    assert gpu.trace_errors() == 0
+    assert torch.equal(hits_a, hits_b) and torch.equal(hits_a, hits_c)
+    pa, pb, pc = (gpu.pixels_to_numpy(x) for x in (img_a, img_b, img_c))
+    for p in (pb, pc):
+        assert np.array_equal(pa["hit"], p["hit"]) and np.array_equal(pa["diffuse"], p["diffuse"])
+    h = gpu.hits_to_numpy(hits_b)
+    org, dirs = orc.camera_rays(cam["pos"], cam["lookAt"], cam["up"], cam["fov"], cam["width"], cam["height"])
+    sel = np.arange(0, org.shape[0], 37)
+    bf = orc.trace_brute(org[sel], dirs[sel], vert, faces, cull=cull)
+    assert np.array_equal(h["prim"][sel], bf["prim"])
+    assert (h["prim"] != MISS).mean() > 0.02  # about 4% of this view hits the 30,000 small triangles
+    # a bundle visits at least the nodes of each of its rays' own traversals
+    assert (pb["intCount"].astype(np.int64) >= pa["intCount"]).all()
+    tr.close()
