@@ -8,11 +8,13 @@
 // 5825 values plus its BF16 copy, AdamW moments beside them.
 //
 // GELU is the tanh approximation of Hendrycks and Gimpel, 0.5 z (1 + tanh(sqrt(2/pi)(z + 0.044715 z^3))).
-// Backward passes the BF16 rounding of weights and activations through as identity.
+// Backward passes the BF16 rounding of weights and activations through as identity; the gradients
+// of the pre-activations are rounded to BF16 where they enter the tensor-core products.
 #include <cuda_bf16.h>
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -330,11 +332,64 @@ __global__ void __launch_bounds__(128, 4) mlp_forward_tc_kernel(const __nv_bfloa
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols) : "memory");
 }
 
-// Forward + backward of one tile of kTile samples per block (one thread per sample). Gradients of
-// loss = sum (y - t)^2 / scaleN are added to grad (FP32); the tile's loss to loss[slot].
-constexpr int kTile = 128;
-constexpr int kStride = kTile + 1;  // [unit][sample] arrays padded against bank conflicts
-constexpr size_t kTrainSmem = sizeof(float) * (kWPad + kIn * kStride + 3 * kH * kStride + kTile);
+// Forward + backward of one tile of kTile samples per block, every contraction on the tensor cores
+// (mma.sync m16n8k16, BF16 operands, FP32 accumulation). Gradients of loss = sum (y - t)^2 / scaleN
+// are stored as the tile's row of part (FP32); the tile's loss is added to loss[slot].
+//   forward   Z1[q][j] = b1 + X[q][:] . W1[j][:]    (q = sample, K = 24 features padded to 32)
+//             Z2[q][j] = b2 + A1[q][:] . W2[j][:]   (A1 = bf16(gelu(Z1)), K = 64)
+//             y[q]     = b3 + sum_j W3[j] bf16(gelu(Z2[q][j]))
+//   backward  dZ2[q][j] = bf16(dY[q] W3[j] gelu'(Z2[q][j])),  dZ1[q][i] = bf16(sum_j dZ2[q][j] W2[j][i] gelu'(Z1[q][i]))
+//             dW2[j][i] = sum_q dZ2[q][j] A1[q][i],  dW1[j][f] = sum_q dZ1[q][j] X[q][f]  (K = the 128 samples)
+// The two gradient rounding points (dZ2, dZ1 to BF16) are the tensor cores' operand type; the FP64
+// oracle (oracle/mlp.py) rounds at the same places. Sums over the tile run in a fixed order, so a
+// training step repeats bit for bit.
+constexpr int kTile = 128;                 // samples per block, 4 warps
+constexpr int kK1 = 32;                    // layer-1 K: 24 features + 8 zeros
+constexpr int kSX = 40;                    // bf16 row strides chosen so fragment loads hit distinct banks
+constexpr int kSH = 72;
+constexpr int kSZ = 68;                    // fp32 row stride of the pre-activations
+constexpr size_t kTrainSmem = sizeof(float) * (kWPad + 2 * kTile * kSZ + kTile) +
+                              sizeof(uint16_t) * (kH * kSX + 2 * kH * kSH + kTile * kSX + 3 * kTile * kSH);
+
+__device__ __forceinline__ void mma16816(float c[4], const uint32_t a[4], const uint32_t b[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+__device__ __forceinline__ uint32_t ld32(const uint16_t *p) { return *reinterpret_cast<const uint32_t *>(p); }
+__device__ __forceinline__ uint32_t pack2(uint16_t lo, uint16_t hi) { return (uint32_t)lo | ((uint32_t)hi << 16); }
+__device__ __forceinline__ uint16_t bf16_u16(float x) { return __bfloat16_as_ushort(__float2bfloat16_rn(x)); }
+__device__ __forceinline__ float bf16_val(uint16_t b) { return __uint_as_float((uint32_t)b << 16); }
+
+// A fragment of a 16 x 16 tile at (r0, k0) of a row-major [row][k] array (g = lane / 4, t = lane % 4).
+__device__ __forceinline__ void frag_a(const uint16_t *m, int stride, int r0, int k0, int g, int t, uint32_t a[4]) {
+  const uint16_t *p = m + (r0 + g) * stride + k0 + 2 * t;
+  a[0] = ld32(p);
+  a[1] = ld32(p + 8 * stride);
+  a[2] = ld32(p + 8);
+  a[3] = ld32(p + 8 * stride + 8);
+}
+// A fragment of the transpose: element (r, k) of the tile is m[k][r].
+__device__ __forceinline__ void frag_a_t(const uint16_t *m, int stride, int r0, int k0, int g, int t, uint32_t a[4]) {
+  const uint16_t *p = m + (k0 + 2 * t) * stride + r0 + g;
+  a[0] = pack2(p[0], p[stride]);
+  a[1] = pack2(p[8], p[stride + 8]);
+  a[2] = pack2(p[8 * stride], p[9 * stride]);
+  a[3] = pack2(p[8 * stride + 8], p[9 * stride + 8]);
+}
+// B fragment (16 x 8 at (k0, n0)) of an array stored [n][k] (so element (k, n) = m[n][k]).
+__device__ __forceinline__ void frag_b(const uint16_t *m, int stride, int k0, int n0, int g, int t, uint32_t b[2]) {
+  const uint16_t *p = m + (n0 + g) * stride + k0 + 2 * t;
+  b[0] = ld32(p);
+  b[1] = ld32(p + 8);
+}
+// B fragment of an array stored [k][n].
+__device__ __forceinline__ void frag_b_t(const uint16_t *m, int stride, int k0, int n0, int g, int t, uint32_t b[2]) {
+  const uint16_t *p = m + (k0 + 2 * t) * stride + n0 + g;
+  b[0] = pack2(p[0], p[stride]);
+  b[1] = pack2(p[8 * stride], p[9 * stride]);
+}
 
 __global__ void __launch_bounds__(kTile) mlp_train_kernel(const __nv_bfloat16 *__restrict__ w,
                                                           const uint16_t *__restrict__ x, const float *__restrict__ tgt,
@@ -343,99 +398,262 @@ __global__ void __launch_bounds__(kTile) mlp_train_kernel(const __nv_bfloat16 *_
                                                           const uint32_t *__restrict__ stepDev, uint32_t step0,
                                                           uint32_t lossCap) {
   extern __shared__ __align__(16) float sm[];
-  // This tile's gradient: every parameter's sum over the tile is stored once, in the tile's own row
-  // (grad_reduce_kernel adds the rows in a fixed order, so training repeats bit for bit).
   float *grad = part + (size_t)blockIdx.x * kMlpParams;
-  float *W = sm;
-  float *X = W + kWPad;
-  float *Z1 = X + kIn * kStride;  // pre-activations of layer 1, later their gradients
-  float *A1 = Z1 + kH * kStride;
-  float *Z2 = A1 + kH * kStride;  // pre-activations of layer 2, later their gradients
-  float *dY = Z2 + kH * kStride;
+  float *W = sm;                       // fp32 copy of the (BF16) parameters: biases and W3
+  float *Z1 = W + kWPad;               // [q][j] pre-activations
+  float *Z2 = Z1 + kTile * kSZ;
+  float *dY = Z2 + kTile * kSZ;
+  uint16_t *sW1 = reinterpret_cast<uint16_t *>(dY + kTile);  // [j][f], f padded to 32
+  uint16_t *sW2 = sW1 + kH * kSX;                             // [j][i]
+  uint16_t *sW2T = sW2 + kH * kSH;                            // [i][j]
+  uint16_t *sX = sW2T + kH * kSH;                             // [q][f]
+  uint16_t *sA1 = sX + kTile * kSX;                           // [q][i] = bf16(gelu(Z1))
+  uint16_t *sD2 = sA1 + kTile * kSH;                          // [q][j] = dZ2
+  uint16_t *sD1 = sD2 + kTile * kSH;                          // [q][i] = dZ1; first the layer-2 activations
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  const uint32_t s = blockIdx.x * kTile + tid;
-  const bool live = s < n;
-  const uint32_t row = live ? (index ? __ldg(index + s) : s) : 0u;
-  load_weights(w, W);
+  const int g = (int)(lane >> 2), t = (int)(lane & 3u);
+  const uint16_t *wb = reinterpret_cast<const uint16_t *>(w);
+  for (int i = tid; i < kMlpParams; i += kTile) W[i] = bf16_val(__ldg(wb + i));
+  for (int i = tid; i < kH * kK1; i += kTile) {
+    const int j = i / kK1, f = i % kK1;
+    sW1[j * kSX + f] = f < kIn ? __ldg(wb + oW1 + j * kIn + f) : (uint16_t)0;
+  }
+  for (int i = tid; i < kH * kH; i += kTile) {
+    const int j = i / kH, k = i % kH;
+    const uint16_t v = __ldg(wb + oW2 + i);
+    sW2[j * kSH + k] = v;
+    sW2T[k * kSH + j] = v;
+  }
   {
-    float in[kIn];
-    if (live) load_row(x, row, in);
+    const uint32_t s = blockIdx.x * kTile + tid;
+    const bool live = s < n;
+    const uint32_t row = live ? (index ? __ldg(index + s) : s) : 0u;
+    const uint4 *p = reinterpret_cast<const uint4 *>(x + (size_t)row * kIn);
+    uint32_t *dst = reinterpret_cast<uint32_t *>(sX + tid * kSX);
 #pragma unroll
-    for (int k = 0; k < kIn; ++k) X[k * kStride + tid] = live ? in[k] : 0.0f;
+    for (int c = 0; c < 3; ++c) {
+      const uint4 v = live ? __ldg(p + c) : make_uint4(0u, 0u, 0u, 0u);
+      dst[4 * c + 0] = v.x;
+      dst[4 * c + 1] = v.y;
+      dst[4 * c + 2] = v.z;
+      dst[4 * c + 3] = v.w;
+    }
+#pragma unroll
+    for (int c = 12; c < kK1 / 2; ++c) dst[c] = 0u;
   }
   __syncthreads();
-  // forward, one column per thread
-  for (int j = 0; j < kH; ++j) {
-    float z = W[oB1 + j];
+
+  // ---- forward: warp w owns samples [32w, 32w + 32), two 16-row tiles ----
+  const int q0 = 32 * (int)warp;
+  float yPart[2][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};  // [tile][row g / g + 8]
+  for (int mt = 0; mt < 2; ++mt) {
+    const int r0 = q0 + 16 * mt;
+    float acc[8][4];
 #pragma unroll
-    for (int k = 0; k < kIn; ++k) z += W[oW1 + j * kIn + k] * X[k * kStride + tid];
-    Z1[j * kStride + tid] = z;
-    A1[j * kStride + tid] = bf16r(gelu(z));
-  }
-  float yv = W[oB3];
-  for (int j = 0; j < kH; ++j) {
-    float z = W[oB2 + j];
-#pragma unroll 16
-    for (int i = 0; i < kH; ++i) z += W[oW2 + j * kH + i] * A1[i * kStride + tid];
-    Z2[j * kStride + tid] = z;
-    yv += W[oW3 + j] * bf16r(gelu(z));
-  }
-  const float diff = live ? yv - __ldg(tgt + row) : 0.0f;
-  const float dy = 2.0f * diff / scaleN;
-  dY[tid] = dy;
-  float l = diff * diff / scaleN;
+    for (int nt = 0; nt < 8; ++nt) {
+      const float b0 = W[oB1 + 8 * nt + 2 * t], b1v = W[oB1 + 8 * nt + 2 * t + 1];
+      acc[nt][0] = b0;
+      acc[nt][1] = b1v;
+      acc[nt][2] = b0;
+      acc[nt][3] = b1v;
+    }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xFFFFFFFFu, l, o);
+    for (int k0 = 0; k0 < kK1; k0 += 16) {
+      uint32_t a[4];
+      frag_a(sX, kSX, r0, k0, g, t, a);
+#pragma unroll
+      for (int nt = 0; nt < 8; ++nt) {
+        uint32_t b[2];
+        frag_b(sW1, kSX, k0, 8 * nt, g, t, b);
+        mma16816(acc[nt], a, b);
+      }
+    }
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int q = r0 + g + 8 * h, j = 8 * nt + 2 * t;
+        Z1[q * kSZ + j] = acc[nt][2 * h];
+        Z1[q * kSZ + j + 1] = acc[nt][2 * h + 1];
+        sA1[q * kSH + j] = bf16_u16(gelu(acc[nt][2 * h]));
+        sA1[q * kSH + j + 1] = bf16_u16(gelu(acc[nt][2 * h + 1]));
+      }
+    }
+  }
+  __syncwarp();
+  for (int mt = 0; mt < 2; ++mt) {
+    const int r0 = q0 + 16 * mt;
+    float acc[8][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+      const float b0 = W[oB2 + 8 * nt + 2 * t], b1v = W[oB2 + 8 * nt + 2 * t + 1];
+      acc[nt][0] = b0;
+      acc[nt][1] = b1v;
+      acc[nt][2] = b0;
+      acc[nt][3] = b1v;
+    }
+#pragma unroll
+    for (int k0 = 0; k0 < kH; k0 += 16) {
+      uint32_t a[4];
+      frag_a(sA1, kSH, r0, k0, g, t, a);
+#pragma unroll
+      for (int nt = 0; nt < 8; ++nt) {
+        uint32_t b[2];
+        frag_b(sW2, kSH, k0, 8 * nt, g, t, b);
+        mma16816(acc[nt], a, b);
+      }
+    }
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int q = r0 + g + 8 * h, j = 8 * nt + 2 * t;
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          const float z = acc[nt][2 * h + e];
+          Z2[q * kSZ + j + e] = z;
+          const uint16_t a2 = bf16_u16(gelu(z));
+          sD1[q * kSH + j + e] = a2;  // the layer-2 activations, until dZ1 takes the buffer
+          yPart[mt][h] += W[oW3 + j + e] * bf16_val(a2);
+        }
+      }
+    }
+  }
+  // y of each row: the four lanes of a quad hold its 64 columns
+  float lsum = 0.0f;
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      float v = yPart[mt][h];
+      v += __shfl_xor_sync(0xFFFFFFFFu, v, 1);
+      v += __shfl_xor_sync(0xFFFFFFFFu, v, 2);
+      const int q = q0 + 16 * mt + g + 8 * h;
+      const uint32_t s = blockIdx.x * kTile + q;
+      const bool live = s < n;
+      const uint32_t row = live ? (index ? __ldg(index + s) : s) : 0u;
+      const float yv = W[oB3] + v;
+      const float diff = live ? yv - __ldg(tgt + row) : 0.0f;
+      if (t == 0) {
+        dY[q] = 2.0f * diff / scaleN;
+        lsum += diff * diff / scaleN;
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xFFFFFFFFu, lsum, o);
   if (lane == 0) {
     uint32_t slot = 0;
     if (stepDev) slot = *stepDev - step0;
-    if (slot < lossCap) atomicAdd(lossBase + slot, l);
+    if (slot < lossCap) atomicAdd(lossBase + slot, lsum);
+  }
+  __syncwarp();
+  // dZ2 of the warp's rows
+  for (int i = lane; i < 32 * kH; i += 32) {
+    const int q = q0 + i / kH, j = i % kH;
+    sD2[q * kSH + j] = bf16_u16(dY[q] * W[oW3 + j] * gelu_grad(Z2[q * kSZ + j]));
   }
   __syncthreads();
-  // dW3[j] = sum_q dY[q] A2[j][q], db3 = sum_q dY[q] (warp per output unit, lanes over samples)
+  // dW3[j] = sum_q dY[q] A2[q][j], db3 = sum_q dY[q]: a warp per unit, lanes over samples
   for (int j = warp; j < kH; j += kTile / 32) {
-    float g = 0.0f;
-    for (int q = lane; q < kTile; q += 32) g += dY[q] * bf16r(gelu(Z2[j * kStride + q]));
+    float gsum = 0.0f;
+    for (int q = lane; q < kTile; q += 32) gsum += dY[q] * bf16_val(sD1[q * kSH + j]);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xFFFFFFFFu, g, o);
-    if (lane == 0) grad[oW3 + j] = g;
+    for (int o = 16; o > 0; o >>= 1) gsum += __shfl_xor_sync(0xFFFFFFFFu, gsum, o);
+    if (lane == 0) grad[oW3 + j] = gsum;
   }
   if (warp == 0) {
-    float g = 0.0f;
-    for (int q = lane; q < kTile; q += 32) g += dY[q];
+    float gsum = 0.0f;
+    for (int q = lane; q < kTile; q += 32) gsum += dY[q];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xFFFFFFFFu, g, o);
-    if (lane == 0) grad[oB3] = g;
+    for (int o = 16; o > 0; o >>= 1) gsum += __shfl_xor_sync(0xFFFFFFFFu, gsum, o);
+    if (lane == 0) grad[oB3] = gsum;
   }
-  __syncthreads();
-  // dZ2 = dY W3 gelu'(Z2); dZ1 = (W2^T dZ2) gelu'(Z1), one column per thread
-  for (int j = 0; j < kH; ++j) Z2[j * kStride + tid] = dy * W[oW3 + j] * gelu_grad(Z2[j * kStride + tid]);
-  for (int i = 0; i < kH; ++i) {
-    float da = 0.0f;
-#pragma unroll 16
-    for (int j = 0; j < kH; ++j) da += W[oW2 + j * kH + i] * Z2[j * kStride + tid];
-    Z1[i * kStride + tid] = da * gelu_grad(Z1[i * kStride + tid]);
-  }
-  __syncthreads();
-  // weight gradients reduced over the tile: warp per output unit j, lanes over the inputs
-  for (int j = warp; j < kH; j += kTile / 32) {
-    const float *dz2 = Z2 + j * kStride, *dz1 = Z1 + j * kStride;
-    float g2a = 0.0f, g2b = 0.0f, g1 = 0.0f;
-    const float *a1a = A1 + lane * kStride, *a1b = A1 + (lane + 32) * kStride;
-    const float *xk = X + (lane < (uint32_t)kIn ? lane : 0u) * kStride;
-    for (int q = 0; q < kTile; ++q) {
-      const float d2 = dz2[q], d1 = dz1[q];
-      g2a += d2 * a1a[q];
-      g2b += d2 * a1b[q];
-      g1 += d1 * xk[q];
+  // dA1 = dZ2 . W2 for the warp's rows (registers), then dZ1 once every warp has read the
+  // activations out of sD1
+  float dacc[2][8][4];
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt) {
+    const int r0 = q0 + 16 * mt;
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) dacc[mt][nt][0] = dacc[mt][nt][1] = dacc[mt][nt][2] = dacc[mt][nt][3] = 0.0f;
+#pragma unroll
+    for (int k0 = 0; k0 < kH; k0 += 16) {
+      uint32_t a[4];
+      frag_a(sD2, kSH, r0, k0, g, t, a);
+#pragma unroll
+      for (int nt = 0; nt < 8; ++nt) {
+        uint32_t b[2];
+        frag_b(sW2T, kSH, k0, 8 * nt, g, t, b);
+        mma16816(dacc[mt][nt], a, b);
+      }
     }
-    grad[oW2 + j * kH + lane] = g2a;
-    grad[oW2 + j * kH + lane + 32] = g2b;
-    if (lane < (uint32_t)kIn) grad[oW1 + j * kIn + lane] = g1;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt) {
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int q = q0 + 16 * mt + g + 8 * h, i = 8 * nt + 2 * t;
+#pragma unroll
+        for (int e = 0; e < 2; ++e)
+          sD1[q * kSH + i + e] = bf16_u16(dacc[mt][nt][2 * h + e] * gelu_grad(Z1[q * kSZ + i + e]));
+      }
+    }
+  }
+  __syncthreads();
+  // ---- weight gradients: warp w owns units [16w, 16w + 16), K = the tile's samples ----
+  {
+    const int j0 = 16 * (int)warp;
+    float g2[8][4], g1[4][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) g2[nt][0] = g2[nt][1] = g2[nt][2] = g2[nt][3] = 0.0f;
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) g1[nt][0] = g1[nt][1] = g1[nt][2] = g1[nt][3] = 0.0f;
+#pragma unroll 2
+    for (int k0 = 0; k0 < kTile; k0 += 16) {
+      uint32_t a2[4], a1[4];
+      frag_a_t(sD2, kSH, j0, k0, g, t, a2);
+      frag_a_t(sD1, kSH, j0, k0, g, t, a1);
+#pragma unroll
+      for (int nt = 0; nt < 8; ++nt) {
+        uint32_t b[2];
+        frag_b_t(sA1, kSH, k0, 8 * nt, g, t, b);
+        mma16816(g2[nt], a2, b);
+      }
+#pragma unroll
+      for (int nt = 0; nt < 4; ++nt) {
+        uint32_t b[2];
+        frag_b_t(sX, kSX, k0, 8 * nt, g, t, b);
+        mma16816(g1[nt], a1, b);
+      }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int j = j0 + g + 8 * h;
+#pragma unroll
+      for (int nt = 0; nt < 8; ++nt) {
+        grad[oW2 + j * kH + 8 * nt + 2 * t] = g2[nt][2 * h];
+        grad[oW2 + j * kH + 8 * nt + 2 * t + 1] = g2[nt][2 * h + 1];
+      }
+#pragma unroll
+      for (int nt = 0; nt < 4; ++nt) {
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          const int f = 8 * nt + 2 * t + e;
+          if (f < kIn) grad[oW1 + j * kIn + f] = g1[nt][2 * h + e];
+        }
+      }
+    }
+  }
+  // bias gradients: a warp per unit, lanes over samples
+  for (int j = warp; j < kH; j += kTile / 32) {
     float b2 = 0.0f, b1 = 0.0f;
     for (int q = lane; q < kTile; q += 32) {
-      b2 += dz2[q];
-      b1 += dz1[q];
+      b2 += bf16_val(sD2[q * kSH + j]);
+      b1 += bf16_val(sD1[q * kSH + j]);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -877,12 +1095,16 @@ int lr_score_keys(const bvhgb_mlp *m, LrScratch &s, const bvhgb_node *nodes, uin
 }
 
 namespace {
+// The shared-memory opt-in belongs to the context: set once per context (another device, or the
+// context after a device reset, sets it again). Thread-safe.
 int ensure_train_attr() {
-  static bool done = false;
-  if (!done) {
-    BVHGB_CUDA_TRY(cudaFuncSetAttribute(mlp_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem));
-    done = true;
-  }
+  static std::mutex mu;
+  static std::vector<uint64_t> done;
+  const uint64_t ctx = context_id();
+  std::lock_guard<std::mutex> lock(mu);
+  if (ctx != 0 && std::find(done.begin(), done.end(), ctx) != done.end()) return BVHGB_OK;
+  BVHGB_CUDA_TRY(cudaFuncSetAttribute(mlp_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem));
+  if (ctx != 0) done.push_back(ctx);
   return BVHGB_OK;
 }
 

@@ -3,7 +3,8 @@
 The network is 24 -> 64 -> 64 -> 1 with GELU (tanh form of Hendrycks and Gimpel). As in the CUDA
 kernels, inputs, weights and both hidden activations are BF16 values (round to nearest even from
 FP32); everything else is computed here in float64. The backward treats each BF16 rounding as the
-identity (straight-through), which is what the CUDA backward computes.
+identity (straight-through), which is what the CUDA backward computes, and rounds the gradients of
+both pre-activations to BF16, where the CUDA backward hands them to the tensor cores.
 
 Parameter layout (5825 values): W1[64][24] b1[64] W2[64][64] b2[64] W3[64] b3[1].
 """
@@ -82,10 +83,11 @@ def loss_and_grad(params, x, t, rounding=True):
     loss = float(np.sum(d * d) / n)
     dy = 2.0 * d / n
     g = {"W3": a2.T @ dy, "b3": np.array([dy.sum()])}
-    dz2 = np.outer(dy, P["W3"]) * gelu_grad(z2)
+    # the CUDA backward feeds dz2 and dz1 to the tensor cores as BF16: they are rounded there
+    dz2 = _round(np.outer(dy, P["W3"]) * gelu_grad(z2), rounding)
     g["W2"] = dz2.T @ a1
     g["b2"] = dz2.sum(0)
-    dz1 = (dz2 @ P["W2"]) * gelu_grad(z1)
+    dz1 = _round((dz2 @ P["W2"]) * gelu_grad(z1), rounding)
     g["W1"] = dz1.T @ x
     g["b1"] = dz1.sum(0)
     return loss, pack(g)
