@@ -101,30 +101,27 @@ __global__ void __launch_bounds__(kWarpItemsPerBlock * 32, 5) patch_warp_kernel(
   warp_patch_item(t, root, numNodes, node, ok, k, out + k, valid + k, toFix + 3 * k, owner, stats, err);
 }
 
-__global__ void apply_kernel(bvhgb_node *t, const PatchOut *__restrict__ in, uint32_t *__restrict__ valid,
-                             uint32_t *__restrict__ toFix, const uint32_t *__restrict__ owner, uint32_t chunkSize,
-                             unsigned long long *__restrict__ stats) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= chunkSize) return;
-  apply_item(t, in[k], valid + k, toFix + 3 * k, owner, k, stats);
-}
-
-// One thread per dirty path (3 per item).
-__global__ void count_kernel(const bvhgb_node *__restrict__ t, uint32_t root, const PatchOut *__restrict__ in,
-                             const uint32_t *__restrict__ toFix, uint32_t *__restrict__ owner,
-                             uint32_t *__restrict__ counter, uint32_t chunkSize, uint32_t numNodes,
-                             uint32_t *__restrict__ err) {
+// Apply + count (apply_count_path): three threads per item.
+__global__ void apply_count_kernel(bvhgb_node *t, uint32_t root, const PatchOut *__restrict__ in,
+                                   const uint32_t *__restrict__ valid, uint32_t *__restrict__ toFix,
+                                   const uint32_t *__restrict__ owner, uint32_t *__restrict__ counter,
+                                   uint32_t chunkSize, uint32_t numNodes, unsigned long long *__restrict__ stats,
+                                   uint32_t *__restrict__ err) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 3 * chunkSize) return;
   const uint32_t k = i / 3;
-  count_path(t, root, numNodes, in[k], i - 3 * k, toFix[i], owner, counter, err);
+  apply_count_path(t, root, numNodes, in, k, i - 3 * k, valid, toFix, owner, counter, stats, err);
 }
 
-__global__ void refit_kernel(bvhgb_node *t, uint32_t root, const uint32_t *__restrict__ toFix,
-                             uint32_t *__restrict__ counter, uint32_t chunkSize, uint32_t numNodes,
-                             uint32_t *__restrict__ err) {
+// Release the claims of the chunk, then refit the dirty paths (refit_path).
+__global__ void release_refit_kernel(bvhgb_node *t, uint32_t root, const PatchOut *__restrict__ in,
+                                     const uint32_t *__restrict__ toFix, uint32_t *__restrict__ owner,
+                                     uint32_t *__restrict__ counter, uint32_t chunkSize, uint32_t numNodes,
+                                     uint32_t *__restrict__ err) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 3 * chunkSize) return;
+  const uint32_t k = i / 3;
+  release_claims(in[k], i - 3 * k, owner);
   refit_path(t, root, numNodes, toFix[i], counter, err);
 }
 
@@ -374,7 +371,6 @@ int run_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t c, cudaStrea
   const uint32_t cs = ws->chunkSize;
   if (cs == 0) return BVHGB_OK;
   const uint32_t bs = ws->cfg.blockSize ? ws->cfg.blockSize : 128;
-  const uint32_t grid = ceil_div(cs, bs);
   const bool prof = !ws->evStart.empty();
   if (prof) BVHGB_CUDA_TRY(record_event(ws->evStart[c], s));
   if (ws->cfg.searchMode == BVHGB_SEARCH_BATCHED) {
@@ -395,13 +391,14 @@ int run_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t c, cudaStrea
   }
   BVHGB_LAUNCH_CHECK("bn13 patch");
   if (prof) BVHGB_CUDA_TRY(record_event(ws->evStop[c], s));
-  apply_kernel<<<grid, bs, 0, s>>>(nodes, ws->patches, ws->valid, ws->toFix, ws->owner, cs, ws->stats);
-  BVHGB_LAUNCH_CHECK("bn13 apply");
-  count_kernel<<<ceil_div(3ull * cs, bs), bs, 0, s>>>(nodes, ws->root, ws->patches, ws->toFix, ws->owner, ws->counter,
-                                                      cs, ws->numNodes,
-                                   ws->err);
-  BVHGB_LAUNCH_CHECK("bn13 count");
-  refit_kernel<<<ceil_div(3ull * cs, bs), bs, 0, s>>>(nodes, ws->root, ws->toFix, ws->counter, cs, ws->numNodes, ws->err);
+  // apply + count in one launch (the count reads the winners' new parents from their patches),
+  // then the release of the claims and the refit
+  apply_count_kernel<<<ceil_div(3ull * cs, bs), bs, 0, s>>>(nodes, ws->root, ws->patches, ws->valid, ws->toFix,
+                                                            ws->owner, ws->counter, cs, ws->numNodes, ws->stats,
+                                                            ws->err);
+  BVHGB_LAUNCH_CHECK("bn13 apply+count");
+  release_refit_kernel<<<ceil_div(3ull * cs, bs), bs, 0, s>>>(nodes, ws->root, ws->patches, ws->toFix, ws->owner,
+                                                              ws->counter, cs, ws->numNodes, ws->err);
   BVHGB_LAUNCH_CHECK("bn13 refit");
   return BVHGB_OK;
 }

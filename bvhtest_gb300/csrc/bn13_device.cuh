@@ -792,6 +792,92 @@ __device__ __forceinline__ void apply_item(bvhgb_node *t, const PatchOut &in, ui
   atomicAdd(&stats[S_APPLIED], 1ull);
 }
 
+// Apply and count in one launch, three threads per item. The count climbs the new tree while the
+// winners' patches are still being written: a node that a winning item patched takes its new parent
+// from that item's patch record, every other node keeps its parent (its record is not written in
+// this launch). A node y is patched by a winner iff its owner o (the lowest rank that claimed it;
+// the claims are final before this launch) wins, i.e. owns every node of its own patch: a higher
+// rank that also claimed y does not own y, so it cannot win. The claims are released later, by
+// the refit launch.
+__device__ __forceinline__ bool item_wins(const PatchOut &in, const uint32_t *__restrict__ owner, uint32_t rank) {
+  bool win = true;
+#pragma unroll
+  for (int s = 0; s < NSLOT; ++s) {
+    const uint32_t x = in.idx[s];
+    if (x != kNone && owner[x] != rank) win = false;
+  }
+  return win;
+}
+
+// The parent of y in the tree being patched, given y's owner o and its parent p before the patch.
+__device__ __forceinline__ uint32_t new_parent(const PatchOut *__restrict__ in, const uint32_t *__restrict__ owner,
+                                               uint32_t y, uint32_t o, uint32_t p) {
+  if (o == kNone) return p;
+  const PatchOut &po = in[o];
+  if (!item_wins(po, owner, o)) return p;
+#pragma unroll
+  for (int s = 0; s < NSLOT; ++s)
+    if (po.idx[s] == y) return po.nd[s].parent;
+  return p;
+}
+
+// Thread j of item k: all three decide the item's outcome (the owner array is final; valid[k], the
+// patch kernel's verdict, is only read here, so the three threads see the same value); thread 0
+// writes the patch and the statistics, thread j counts the arrivals along the item's j-th dirty
+// path (kFixTree3_1) in the new tree. The start node gets bit 31 as in count_path.
+__device__ __forceinline__ void apply_count_path(bvhgb_node *t, uint32_t root, uint32_t numNodes,
+                                                 const PatchOut *__restrict__ in, uint32_t k, uint32_t j,
+                                                 const uint32_t *__restrict__ valid, uint32_t *__restrict__ toFix,
+                                                 const uint32_t *__restrict__ owner, uint32_t *__restrict__ counter,
+                                                 unsigned long long *__restrict__ stats, uint32_t *__restrict__ err) {
+  if (!valid[k]) return;  // refused by removeNode or the search: it claimed nothing
+  uint32_t x = toFix[3 * k + j];
+  const PatchOut &me = in[k];
+  const bool win = item_wins(me, owner, k);
+  if (!win) {
+    toFix[3 * k + j] = kNone;  // the refit skips a lost item's paths
+    if (j == 0) atomicAdd(&stats[S_CONFLICT], 1ull);
+    return;
+  }
+  if (j == 0) {
+#pragma unroll
+    for (int s = 0; s < NSLOT; ++s) {
+      const uint32_t y = me.idx[s];
+      if (y == kNone) continue;
+      const NodeP n = me.nd[s];
+      t[y].parent = n.parent;
+      t[y].left = n.left;
+      t[y].right = n.right;
+      t[y].isLeft = n.isLeft;
+    }
+    atomicAdd(&stats[S_APPLIED], 1ull);
+  }
+  if (x == kNone) return;
+  uint32_t add = 0x80000001u;
+  for (uint32_t steps = 0;; ++steps) {
+    if (x >= numNodes || steps > numNodes) {
+      atomicOr(err, kErrBadIndex);
+      break;
+    }
+    // owner, old parent and the counter update go out together: one round trip per level where
+    // no patch touched the node
+    const uint32_t o = owner[x];
+    const uint32_t p = __ldcg(&t[x].parent);  // discarded if a winner rewrites it in this launch
+    if (atomicAdd(&counter[x], add) != 0u) break;
+    if (x == root) break;
+    add = 1u;
+    x = new_parent(in, owner, x, o, p);
+  }
+}
+
+// Release a third of an item's claims (after the launch that counted with them).
+__device__ __forceinline__ void release_claims(const PatchOut &in, uint32_t j, uint32_t *__restrict__ owner) {
+  for (uint32_t s = j; s < (uint32_t)NSLOT; s += 3) {
+    const uint32_t y = in.idx[s];
+    if (y != kNone) owner[y] = kNone;
+  }
+}
+
 // Release a third of an item's claims and count the arrivals along one dirty path (kFixTree3_1);
 // the parent link is loaded together with the counter update, so a level costs one round trip.
 // The path's own start node gets bit 31 as well (the refit below must know its start nodes).
@@ -817,39 +903,70 @@ __device__ __forceinline__ void count_path(const bvhgb_node *__restrict__ t, uin
   }
 }
 
-// The last path to arrive at a node recomputes its box (kFixTree3_2). A node's links do not change
-// in this launch, so they are read before its counter. A counter holds the arrivals still expected
-// (low 16 bits, from the count pass) and, above, how many arrivals brought a changed box: a path
-// whose node's box came out bitwise unchanged wrote nothing, so its arrival needs no release and
-// adds nothing; if no arrival at a node changed (and it is not a start node, whose children were
-// relinked), the node's box is already the union of its children's and only the climb goes on.
-// Near the root, where all paths meet, boxes rarely change, so most of a long climb costs one
-// relaxed round trip per level. Every node whose children were relinked by a patch is a start
-// node (grand parent, reused nodes; bit 31 of its counter, set by the count pass) or the parent of
-// a reused node, so a start node always reports a change. The last arrival resets the counter.
+// The last path to arrive at a node recomputes its box (kFixTree3_2). A counter holds the arrivals
+// still expected (low 16 bits, from the count pass), above them how many arrivals brought a changed
+// box, and bit 31 marks a start node (grand parent or reused node: its children were relinked, so
+// it always reports a change). A path whose node's box came out bitwise unchanged wrote nothing,
+// so its arrival needs no release and adds nothing; if no arrival at a node changed and it is not a
+// start node, its box is already the union of its children's and only the climb goes on. The last
+// arrival resets the counter.
+//
+// Links do not change in this launch and a node's box is written only by its last arrival, so the
+// climb reads one level ahead: while it handles node x it already loads the parent's record and
+// counter and, speculatively, the box of x's other child. That box is stale only if another arrival
+// at x changed it, and such an arrival raised x's changed count before it left (acq_rel), so the
+// last arrival reads it again exactly when that count is not zero. A node whose counter already
+// shows this path as the only arrival left, with no changed arrival before it, needs no atomic at
+// all: nobody else reads or writes it or its children in this launch (a later reader of the boxes
+// written below it meets this path at a shared node, whose acq_rel arrival orders them). Most of a
+// climb below the nodes where paths meet thus costs one round trip per level.
 __device__ __forceinline__ void refit_path(bvhgb_node *t, uint32_t root, uint32_t numNodes, uint32_t x,
                                           uint32_t *__restrict__ counter, uint32_t *__restrict__ err) {
   if (x == kNone) return;
+  if (x >= numNodes) {
+    atomicOr(err, kErrBadIndex);
+    return;
+  }
+  const float4 *q = reinterpret_cast<const float4 *>(t + x);
+  float4 w0 = __ldcg(q), w1 = __ldcg(q + 1), w2 = __ldcg(q + 2);  // [mn.xyz mx.x] [mx.yz parent left] [right flags . sa]
+  uint32_t cnt = __ldcg(&counter[x]);
   uint32_t from = kNone;  // child the path came from, whose box is 'cur'
   Box cur;
   bool changed = true;    // the start node's children were relinked
   for (uint32_t steps = 0;; ++steps) {
-    if (x >= numNodes || steps > numNodes) {
-      atomicOr(err, kErrBadIndex);
-      return;
-    }
-    const float4 w0 = __ldcg(reinterpret_cast<const float4 *>(t + x));      // mn.xyz mx.x
-    const float4 w1 = __ldcg(reinterpret_cast<const float4 *>(t + x) + 1);  // mx.y mx.z parent left
-    const float4 w2 = __ldcg(reinterpret_cast<const float4 *>(t + x) + 2);  // right flags level sa
-    const uint32_t add = changed ? 0xFFFFu : 0xFFFFFFFFu;  // one arrival less (low 16 bits), one changed more
-    const uint32_t old = changed ? atom_add_acq_rel(&counter[x], add) : atom_add_acquire(&counter[x], add);
-    if ((old & 0xFFFFu) != 1u) return;  // not the last arrival
-    counter[x] = 0u;
     const uint32_t parent = __float_as_uint(w1.z), l = __float_as_uint(w1.w), r = __float_as_uint(w2.x);
-    if ((__float_as_uint(w2.y) & 0xFFFFu) || l >= numNodes || r >= numNodes) {
+    if ((__float_as_uint(w2.y) & 0xFFFFu) || l >= numNodes || r >= numNodes || steps > numNodes) {
       if (!(__float_as_uint(w2.y) & 0xFFFFu)) atomicOr(err, kErrBadIndex);
       return;
     }
+    const bool top = x == root;
+    if (!top && parent >= numNodes) {
+      atomicOr(err, kErrBadIndex);
+      return;
+    }
+    // this level's child boxes (speculative) and the next level's record and counter
+    Box lb = from == l ? cur : load_box_cg(t + l);
+    Box rb = from == r ? cur : load_box_cg(t + r);
+    float4 n0 = w0, n1 = w1, n2 = w2;
+    uint32_t ncnt = 0u;
+    if (!top) {
+      const float4 *pq = reinterpret_cast<const float4 *>(t + parent);
+      n0 = __ldcg(pq);
+      n1 = __ldcg(pq + 1);
+      n2 = __ldcg(pq + 2);
+      ncnt = __ldcg(&counter[parent]);
+    }
+    uint32_t old = cnt;
+    if ((cnt & 0x7FFFFFFFu) != 1u) {  // other arrivals are (or were) expected here
+      const uint32_t add = changed ? 0xFFFFu : 0xFFFFFFFFu;  // one arrival less (low 16 bits), one changed more
+      old = changed ? atom_add_acq_rel(&counter[x], add) : atom_add_acquire(&counter[x], add);
+      if ((old & 0xFFFFu) != 1u) return;  // not the last arrival
+      if ((old >> 16) & 0x7FFFu) {        // a child's box was rewritten in this launch
+        if (from != l) lb = load_box_cg(t + l);
+        if (from != r) rb = load_box_cg(t + r);
+      }
+    }
+    counter[x] = 0u;
     const bool start = (old >> 31) != 0u;  // x started a path (this one or an earlier arrival)
     const bool anyChanged = changed || start || ((old >> 16) & 0x7FFFu) != 0u;
     Box b;
@@ -857,28 +974,30 @@ __device__ __forceinline__ void refit_path(bvhgb_node *t, uint32_t root, uint32_
     b.mx[0] = w0.w; b.mx[1] = w1.x; b.mx[2] = w1.y;
     bool upChanged = false;
     if (anyChanged) {
-      Box nb = from == l ? cur : load_box_cg(t + l);
-      const Box rb = from == r ? cur : load_box_cg(t + r);
-      merge_into(nb, rb);
+      merge_into(lb, rb);
 #pragma unroll
       for (int k = 0; k < 3; ++k)
-        upChanged |= __float_as_uint(nb.mn[k]) != __float_as_uint(b.mn[k]) ||
-                     __float_as_uint(nb.mx[k]) != __float_as_uint(b.mx[k]);
+        upChanged |= __float_as_uint(lb.mn[k]) != __float_as_uint(b.mn[k]) ||
+                     __float_as_uint(lb.mx[k]) != __float_as_uint(b.mx[k]);
       if (upChanged) {
         float4 *p = reinterpret_cast<float4 *>(t + x);
-        p[0] = make_float4(nb.mn[0], nb.mn[1], nb.mn[2], nb.mx[0]);
-        p[1] = make_float4(nb.mx[1], nb.mx[2], w1.z, w1.w);
-        t[x].surfaceArea = surface_area(nb);
-        b = nb;
+        p[0] = make_float4(lb.mn[0], lb.mn[1], lb.mn[2], lb.mx[0]);
+        p[1] = make_float4(lb.mx[1], lb.mx[2], w1.z, w1.w);
+        t[x].surfaceArea = surface_area(lb);
+        b = lb;
       }
     }
-    if (x == root) return;
+    if (top) return;
     // A start node may have moved (a reused node now hangs under a new parent), so its parent
     // cannot compare against the old box: it always counts as changed.
     changed = upChanged || start;
     from = x;
     cur = b;
     x = parent;
+    w0 = n0;
+    w1 = n1;
+    w2 = n2;
+    cnt = ncnt;
   }
 }
 
