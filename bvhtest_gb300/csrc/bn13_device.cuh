@@ -406,7 +406,8 @@ constexpr uint32_t kFrontierCap = 32u * kFrontier;
 
 // The k-th smallest (1 <= k <= number of flagged entries) of the 32-bit keys of the slots flagged
 // in 'in' (bit s: this lane's slot s), S slots per lane: a most-significant-bit-first radix
-// selection by warp ballots, starting below the bits that all flagged keys share.
+// selection, one warp sum per bit (of each lane's flagged keys with the bit clear), starting below
+// the bits that all flagged keys share.
 template <int S>
 __device__ __forceinline__ uint32_t warp_select_kth(const uint32_t (&key)[S], uint32_t in, uint32_t k) {
   uint32_t lo = 0xFFFFFFFFu, hi = 0u;
@@ -426,9 +427,7 @@ __device__ __forceinline__ uint32_t warp_select_kth(const uint32_t (&key)[S], ui
     uint32_t ones = 0;  // this lane's slots whose key has the bit set
 #pragma unroll
     for (int s = 0; s < S; ++s) ones |= ((key[s] >> bit) & 1u) << s;
-    uint32_t zeros = 0;
-#pragma unroll
-    for (int s = 0; s < S; ++s) zeros += __popc(__ballot_sync(kFull, ((alive & ~ones) >> s) & 1u));
+    const uint32_t zeros = __reduce_add_sync(kFull, (uint32_t)__popc(alive & ~ones));  // one collective per bit
     if (k > zeros) {
       k -= zeros;
       res |= 1u << bit;
