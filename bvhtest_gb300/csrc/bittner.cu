@@ -101,24 +101,34 @@ __global__ void __launch_bounds__(kWarpItemsPerBlock * 32, 5) patch_warp_kernel(
   warp_patch_item(t, root, numNodes, node, ok, k, out + k, valid + k, toFix + 3 * k, owner, stats, err);
 }
 
-// Apply + count (apply_count_path): three threads per item.
-__global__ void apply_count_kernel(bvhgb_node *t, uint32_t root, const PatchOut *__restrict__ in,
-                                   const uint32_t *__restrict__ valid, uint32_t *__restrict__ toFix,
-                                   const uint32_t *__restrict__ owner, uint32_t *__restrict__ counter,
-                                   uint32_t chunkSize, uint32_t numNodes, unsigned long long *__restrict__ stats,
-                                   uint32_t *__restrict__ err) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+// The climbs of the chunk tail run one per warp (lane 0; the other lanes leave at once). The paths
+// of one item, or of neighbouring items, have nothing in common: in a shared warp every level of
+// every path would wait for the slowest lane's level (an acq_rel arrival costs about four times a
+// plain L2 round trip), so a warp of its own keeps each climb at its own latency. The SMs have the
+// room: a chunk has at most a few thousand paths.
+constexpr uint32_t kTailWarpsPerBlock = 4;
+
+__device__ __forceinline__ uint32_t tail_path_index() {
+  return (threadIdx.x & 31u) ? 0xFFFFFFFFu : (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+}
+
+// Apply + count (apply_count_path): three climbs per item.
+__global__ void __launch_bounds__(kTailWarpsPerBlock * 32) apply_count_kernel(
+    bvhgb_node *t, uint32_t root, const PatchOut *__restrict__ in, const uint32_t *__restrict__ valid,
+    uint32_t *__restrict__ toFix, const uint32_t *__restrict__ owner, uint32_t *__restrict__ counter,
+    uint32_t chunkSize, uint32_t numNodes, unsigned long long *__restrict__ stats, uint32_t *__restrict__ err) {
+  const uint32_t i = tail_path_index();
   if (i >= 3 * chunkSize) return;
   const uint32_t k = i / 3;
   apply_count_path(t, root, numNodes, in, k, i - 3 * k, valid, toFix, owner, counter, stats, err);
 }
 
 // Release the claims of the chunk, then refit the dirty paths (refit_path).
-__global__ void release_refit_kernel(bvhgb_node *t, uint32_t root, const PatchOut *__restrict__ in,
-                                     const uint32_t *__restrict__ toFix, uint32_t *__restrict__ owner,
-                                     uint32_t *__restrict__ counter, uint32_t chunkSize, uint32_t numNodes,
-                                     uint32_t *__restrict__ err) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kTailWarpsPerBlock * 32) release_refit_kernel(
+    bvhgb_node *t, uint32_t root, const PatchOut *__restrict__ in, const uint32_t *__restrict__ toFix,
+    uint32_t *__restrict__ owner, uint32_t *__restrict__ counter, uint32_t chunkSize, uint32_t numNodes,
+    uint32_t *__restrict__ err) {
+  const uint32_t i = tail_path_index();
   if (i >= 3 * chunkSize) return;
   const uint32_t k = i / 3;
   release_claims(in[k], i - 3 * k, owner);
@@ -370,7 +380,6 @@ cudaError_t record_event(cudaEvent_t ev, cudaStream_t s) {
 int run_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t c, cudaStream_t s) {
   const uint32_t cs = ws->chunkSize;
   if (cs == 0) return BVHGB_OK;
-  const uint32_t bs = ws->cfg.blockSize ? ws->cfg.blockSize : 128;
   const bool prof = !ws->evStart.empty();
   if (prof) BVHGB_CUDA_TRY(record_event(ws->evStart[c], s));
   if (ws->cfg.searchMode == BVHGB_SEARCH_BATCHED) {
@@ -379,7 +388,8 @@ int run_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t c, cudaStrea
         ws->toFix, ws->owner, ws->stats, ws->numNodes, ws->err);
   } else {
     // One warp per block: these searches are latency-bound, so spreading them over more SMs beats
-    // packing them (CUDABlockSize only sizes the other kernels; results do not depend on it).
+    // packing them. Every chunk kernel sizes its own blocks: CUDABlockSize is accepted and kept in
+    // the configuration, and results never depend on it.
     if (ws->cfg.searchMode == BVHGB_SEARCH_ALT)
       patch_kernel<BVHGB_SEARCH_ALT><<<ceil_div(cs, kSearchThreads), kSearchThreads, 0, s>>>(
           nodes, ws->root, ws->todo, ws->numInner, c, ws->numChunks, cs, ws->cfg.offsetAccess, ws->patches,
@@ -393,12 +403,14 @@ int run_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t c, cudaStrea
   if (prof) BVHGB_CUDA_TRY(record_event(ws->evStop[c], s));
   // apply + count in one launch (the count reads the winners' new parents from their patches),
   // then the release of the claims and the refit
-  apply_count_kernel<<<ceil_div(3ull * cs, bs), bs, 0, s>>>(nodes, ws->root, ws->patches, ws->valid, ws->toFix,
-                                                            ws->owner, ws->counter, cs, ws->numNodes, ws->stats,
-                                                            ws->err);
+  const uint32_t tailBlocks = ceil_div(3ull * cs, kTailWarpsPerBlock);
+  apply_count_kernel<<<tailBlocks, kTailWarpsPerBlock * 32, 0, s>>>(nodes, ws->root, ws->patches, ws->valid,
+                                                                    ws->toFix, ws->owner, ws->counter, cs,
+                                                                    ws->numNodes, ws->stats, ws->err);
   BVHGB_LAUNCH_CHECK("bn13 apply+count");
-  release_refit_kernel<<<ceil_div(3ull * cs, bs), bs, 0, s>>>(nodes, ws->root, ws->patches, ws->toFix, ws->owner,
-                                                              ws->counter, cs, ws->numNodes, ws->err);
+  release_refit_kernel<<<tailBlocks, kTailWarpsPerBlock * 32, 0, s>>>(nodes, ws->root, ws->patches, ws->toFix,
+                                                                      ws->owner, ws->counter, cs, ws->numNodes,
+                                                                      ws->err);
   BVHGB_LAUNCH_CHECK("bn13 refit");
   return BVHGB_OK;
 }
