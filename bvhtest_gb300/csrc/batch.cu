@@ -37,6 +37,7 @@ struct bvhgb_batch_workspace {
   void *sortTemp = nullptr;
   // optimizer
   uint32_t *todo = nullptr, *valid = nullptr, *toFix = nullptr, *owner = nullptr, *counter = nullptr;
+  unsigned long long *mail = nullptr;  // refit mail slots, three words per node, empty between launches
   bvhgb::PatchOut *patches = nullptr;
   unsigned long long *stats = nullptr;
   // captured whole pipeline
@@ -251,14 +252,15 @@ __global__ void batch_count_kernel(const bvhgb_node *__restrict__ nodes, const P
 }
 
 __global__ void batch_refit_kernel(bvhgb_node *nodes, const uint32_t *__restrict__ toFix,
-                                   uint32_t *__restrict__ counter, const uint32_t *__restrict__ itemMesh,
+                                   uint32_t *__restrict__ counter, unsigned long long *__restrict__ mail,
+                                   const uint32_t *__restrict__ itemMesh,
                                    const uint32_t *__restrict__ itemOff, const uint32_t *__restrict__ faceOff,
                                    const uint32_t *__restrict__ nodeOff, uint32_t items, uint32_t *__restrict__ err) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 3 * items) return;
   const MeshItem it = item_of(itemMesh, itemOff, i / 3);
   const uint32_t n = __ldg(faceOff + it.m + 1) - __ldg(faceOff + it.m), nb = __ldg(nodeOff + it.m);
-  refit_path(nodes + nb, 0u, 2 * n - 1, toFix[i], counter + nb, err);
+  refit_path(nodes + nb, 0u, 2 * n - 1, toFix[i], counter + nb, mail + 3ull * nb, err);
 }
 
 // SplitMix64 of (seed, index, lane) -> uniform in [0, 1) with 24 bits.
@@ -366,8 +368,8 @@ int batch_iteration(bvhgb_batch_workspace *ws, bvhgb_node *nodes, cudaStream_t s
                                                              ws->itemMesh, ws->itemOff, ws->faceOff, ws->nodeOff, T,
                                                              ws->err);
     BVHGB_LAUNCH_CHECK("batch count");
-    batch_refit_kernel<<<ceil_div(3ull * T, bs), bs, 0, s>>>(nodes, ws->toFix, ws->counter, ws->itemMesh, ws->itemOff,
-                                                             ws->faceOff, ws->nodeOff, T, ws->err);
+    batch_refit_kernel<<<ceil_div(3ull * T, bs), bs, 0, s>>>(nodes, ws->toFix, ws->counter, ws->mail, ws->itemMesh,
+                                                             ws->itemOff, ws->faceOff, ws->nodeOff, T, ws->err);
     BVHGB_LAUNCH_CHECK("batch refit");
   }
   return BVHGB_OK;
@@ -483,6 +485,7 @@ extern "C" BVHGB_API int bvhgb_batch_create(uint32_t numMeshes, const uint32_t *
   alloc(&ws->patches, sizeof(PatchOut) * T);
   alloc(&ws->owner, 4 * N);
   alloc(&ws->counter, 4 * N);
+  alloc(&ws->mail, 24 * N);
   alloc(&ws->stats, sizeof(unsigned long long) * S_COUNT);
   if (e == cudaSuccess) e = cudaMemcpy(ws->faceOff, ws->hFaceOff.data(), 4 * (numMeshes + 1), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(ws->nodeOff, ws->hNodeOff.data(), 4 * (numMeshes + 1), cudaMemcpyHostToDevice);
@@ -492,6 +495,7 @@ extern "C" BVHGB_API int bvhgb_batch_create(uint32_t numMeshes, const uint32_t *
   if (e == cudaSuccess) e = cudaMemcpy(ws->itemMesh, itemMesh.data(), 4 * itemMesh.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(ws->owner, 0xFF, 4 * N);
   if (e == cudaSuccess) e = cudaMemset(ws->counter, 0, 4 * N);
+  if (e == cudaSuccess) e = cudaMemset(ws->mail, 0xFF, 24 * N);
   if (e == cudaSuccess) e = cudaMemset(ws->stats, 0, sizeof(unsigned long long) * S_COUNT);
   if (e == cudaSuccess) e = cudaMemset(ws->err, 0, 4);
   if (e != cudaSuccess) {
@@ -510,7 +514,7 @@ extern "C" BVHGB_API int bvhgb_batch_destroy(bvhgb_batch_workspace *ws) {
                   (void *)ws->itemMesh, (void *)ws->scene, (void *)ws->err, (void *)ws->keys, (void *)ws->keysSorted,
                   (void *)ws->vals, (void *)ws->valsSorted, (void *)ws->slots, (void *)ws->triBoxes, ws->sortTemp,
                   (void *)ws->todo, (void *)ws->valid, (void *)ws->toFix, (void *)ws->patches, (void *)ws->owner,
-                  (void *)ws->counter, (void *)ws->stats})
+                  (void *)ws->counter, (void *)ws->mail, (void *)ws->stats})
     cudaFree(p);
   delete ws;
   return BVHGB_OK;

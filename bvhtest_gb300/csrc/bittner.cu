@@ -12,8 +12,9 @@
 //            scheduling (the reference locks first-come and is not deterministic);
 //   count  : owners are released and each dirty path (grand parent, both reused nodes) counts its
 //            arrivals on the way to the root (kFixTree3_1);
-//   refit  : the last arrival at a node recomputes its box from its children (kFixTree3_2) with
-//            acq_rel counters, so no box is read before it is final.
+//   refit  : the last arrival at a node recomputes its box from its children (kFixTree3_2); the
+//            counters are relaxed and a rewritten child box reaches the last arrival through a
+//            self-validating mail slot, so no box is read before it is final.
 // bvhgb_bn13_run captures one iteration into a CUDA graph and replays it. With a learned scorer
 // set, iteration i selects by the scorer unless plainEvery > 0 and i % plainEvery == plainEvery - 1,
 // in which case it selects by the inefficiency (one graph per kind of iteration).
@@ -126,13 +127,13 @@ __global__ void __launch_bounds__(kTailWarpsPerBlock * 32) apply_count_kernel(
 // Release the claims of the chunk, then refit the dirty paths (refit_path).
 __global__ void __launch_bounds__(kTailWarpsPerBlock * 32) release_refit_kernel(
     bvhgb_node *t, uint32_t root, const PatchOut *__restrict__ in, const uint32_t *__restrict__ toFix,
-    uint32_t *__restrict__ owner, uint32_t *__restrict__ counter, uint32_t chunkSize, uint32_t numNodes,
-    uint32_t *__restrict__ err) {
+    uint32_t *__restrict__ owner, uint32_t *__restrict__ counter, unsigned long long *__restrict__ mail,
+    uint32_t chunkSize, uint32_t numNodes, uint32_t *__restrict__ err) {
   const uint32_t i = tail_path_index();
   if (i >= 3 * chunkSize) return;
   const uint32_t k = i / 3;
   release_claims(in[k], i - 3 * k, owner);
-  refit_path(t, root, numNodes, toFix[i], counter, err);
+  refit_path(t, root, numNodes, toFix[i], counter, mail, err);
 }
 
 // Full bottom-up refit (kFixTree1, Bittner13CUDA.cu:372-404): every leaf starts a climb; at each
@@ -312,6 +313,7 @@ struct bvhgb_bn13_workspace {
   void *sortTemp = nullptr;
   PatchOut *patches = nullptr;
   uint32_t *valid = nullptr, *toFix = nullptr, *owner = nullptr, *counter = nullptr, *err = nullptr;
+  unsigned long long *mail = nullptr;  // three words per node, empty between launches
   HeapItem *heaps = nullptr;
   unsigned long long *stats = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [0] plain iteration, [1] learned iteration
@@ -409,8 +411,8 @@ int run_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t c, cudaStrea
                                                                     ws->numNodes, ws->stats, ws->err);
   BVHGB_LAUNCH_CHECK("bn13 apply+count");
   release_refit_kernel<<<tailBlocks, kTailWarpsPerBlock * 32, 0, s>>>(nodes, ws->root, ws->patches, ws->toFix,
-                                                                      ws->owner, ws->counter, cs, ws->numNodes,
-                                                                      ws->err);
+                                                                      ws->owner, ws->counter, ws->mail, cs,
+                                                                      ws->numNodes, ws->err);
   BVHGB_LAUNCH_CHECK("bn13 refit");
   return BVHGB_OK;
 }
@@ -519,6 +521,7 @@ extern "C" BVHGB_API int bvhgb_bn13_create(const bvhgb_node *nodes, uint32_t num
   if (e == cudaSuccess) e = dev_malloc(&ws->toFix, 12 * cs);
   if (e == cudaSuccess) e = dev_malloc(&ws->owner, 4ull * numNodes);
   if (e == cudaSuccess) e = dev_malloc(&ws->counter, 4ull * numNodes);
+  if (e == cudaSuccess) e = dev_malloc(&ws->mail, 24ull * numNodes);
   if (e == cudaSuccess) e = dev_malloc(&ws->err, 4);
   // Only the heap search keeps a queue in global memory (entries beyond the shared-memory top).
   const size_t heapItems = ws->cfg.searchMode == BVHGB_SEARCH_HEAP ? cs * ws->cfg.heapCapacity : 1;
@@ -527,6 +530,7 @@ extern "C" BVHGB_API int bvhgb_bn13_create(const bvhgb_node *nodes, uint32_t num
   if (e == cudaSuccess && inner.size())
     e = cudaMemcpyAsync(ws->inner, inner.data(), 4 * inner.size(), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ws->counter, 0, 4ull * numNodes, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ws->mail, 0xFF, 24ull * numNodes, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ws->owner, 0xFF, 4ull * numNodes, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ws->err, 0, 4, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ws->stats, 0, sizeof(unsigned long long) * S_COUNT, s);
@@ -565,6 +569,7 @@ extern "C" BVHGB_API int bvhgb_bn13_destroy(bvhgb_bn13_workspace *ws) {
   cudaFree(ws->toFix);
   cudaFree(ws->owner);
   cudaFree(ws->counter);
+  cudaFree(ws->mail);
   cudaFree(ws->err);
   cudaFree(ws->heaps);
   cudaFree(ws->stats);

@@ -902,25 +902,74 @@ __device__ __forceinline__ void count_path(const bvhgb_node *__restrict__ t, uin
   }
 }
 
-// The last path to arrive at a node recomputes its box (kFixTree3_2). A counter holds the arrivals
-// still expected (low 16 bits, from the count pass), above them how many arrivals brought a changed
-// box, and bit 31 marks a start node (grand parent or reused node: its children were relinked, so
-// it always reports a change). A path whose node's box came out bitwise unchanged wrote nothing,
-// so its arrival needs no release and adds nothing; if no arrival at a node changed and it is not a
-// start node, its box is already the union of its children's and only the climb goes on. The last
-// arrival resets the counter.
+// ---- dirty-path refit (kFixTree3_2) ------------------------------------------------------------
+// The last path to arrive at a node recomputes its box. A node's counter (set by the count pass)
+// holds the arrivals still expected in its low 16 bits and bit 31 for a start node (grand parent or
+// reused node: its children were relinked, so it is always recomputed). Each arrival subtracts one
+// and, for the child it comes from (side 0 left, 1 right), sets bit 16 + side if it rewrote that
+// child's box in this launch and bit 18 + side if the child changed (rewritten, or a start node,
+// which may have moved under a new parent). A side arrives at most once, so the bits never carry.
+//
+// Every counter update is relaxed: a rewritten box does not travel through the node record, whose
+// visibility would need a release by the writer and an acquire by the reader (fences that cost
+// several L2 round trips each), but through a mail slot of three 64-bit words per child that
+// carries its own validity. A path that may not be the last at a node posts its child's new box
+// there before its update; the last arrival finds the posting side in the counter bits and reads
+// the slot until all three words differ from the empty pattern (each 64-bit word is written and
+// read whole), then empties it again; a path that posted and turned out last empties its own. A
+// child whose box was not rewritten in this launch is read from its record, loaded speculatively
+// together with the counter update. (Two coordinates of a box that both hold the bit pattern
+// 0xFFFFFFFF would read as empty: the wait then ends at its limit with kErrTimeout.)
 //
 // Links do not change in this launch and a node's box is written only by its last arrival, so the
-// climb reads one level ahead: while it handles node x it already loads the parent's record and
-// counter and, speculatively, the box of x's other child. That box is stale only if another arrival
-// at x changed it, and such an arrival raised x's changed count before it left (acq_rel), so the
-// last arrival reads it again exactly when that count is not zero. A node whose counter already
-// shows this path as the only arrival left, with no changed arrival before it, needs no atomic at
-// all: nobody else reads or writes it or its children in this launch (a later reader of the boxes
-// written below it meets this path at a shared node, whose acq_rel arrival orders them). Most of a
-// climb below the nodes where paths meet thus costs one round trip per level.
+// climb reads one level ahead: while it handles node x it loads the parent's record and counter. A
+// node whose counter already shows this path as the only arrival left needs no update at all.
+constexpr unsigned long long kMailEmpty = 0xFFFFFFFFFFFFFFFFull;
+
+__device__ __forceinline__ unsigned long long pack2(float a, float b) {
+  return (unsigned long long)__float_as_uint(a) | ((unsigned long long)__float_as_uint(b) << 32);
+}
+
+__device__ __forceinline__ void mail_post(unsigned long long *mail, uint32_t child, const Box &b) {
+  unsigned long long *m = mail + 3ull * child;
+  __stcg(m, pack2(b.mn[0], b.mn[1]));
+  __stcg(m + 1, pack2(b.mn[2], b.mx[0]));
+  __stcg(m + 2, pack2(b.mx[1], b.mx[2]));
+}
+
+__device__ __forceinline__ void mail_clear(unsigned long long *mail, uint32_t child) {
+  unsigned long long *m = mail + 3ull * child;
+  __stcg(m, kMailEmpty);
+  __stcg(m + 1, kMailEmpty);
+  __stcg(m + 2, kMailEmpty);
+}
+
+// Takes the box posted for 'child' (bounded wait per word) and empties the slot.
+__device__ __forceinline__ Box mail_take(unsigned long long *mail, uint32_t child, uint32_t *__restrict__ err) {
+  unsigned long long *m = mail + 3ull * child;
+  unsigned long long w[3] = {__ldcg(m), __ldcg(m + 1), __ldcg(m + 2)};
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    for (uint32_t spins = 0; w[q] == kMailEmpty; ++spins) {
+      if (spins > kSpinLimit) {
+        atomicOr(err, kErrTimeout);
+        break;
+      }
+      __nanosleep(32);
+      w[q] = __ldcg(m + q);
+    }
+  }
+  mail_clear(mail, child);
+  Box b;
+  b.mn[0] = __uint_as_float((uint32_t)w[0]); b.mn[1] = __uint_as_float((uint32_t)(w[0] >> 32));
+  b.mn[2] = __uint_as_float((uint32_t)w[1]); b.mx[0] = __uint_as_float((uint32_t)(w[1] >> 32));
+  b.mx[1] = __uint_as_float((uint32_t)w[2]); b.mx[2] = __uint_as_float((uint32_t)(w[2] >> 32));
+  return b;
+}
+
 __device__ __forceinline__ void refit_path(bvhgb_node *t, uint32_t root, uint32_t numNodes, uint32_t x,
-                                          uint32_t *__restrict__ counter, uint32_t *__restrict__ err) {
+                                          uint32_t *__restrict__ counter, unsigned long long *__restrict__ mail,
+                                          uint32_t *__restrict__ err) {
   if (x == kNone) return;
   if (x >= numNodes) {
     atomicOr(err, kErrBadIndex);
@@ -931,10 +980,12 @@ __device__ __forceinline__ void refit_path(bvhgb_node *t, uint32_t root, uint32_
   uint32_t cnt = __ldcg(&counter[x]);
   uint32_t from = kNone;  // child the path came from, whose box is 'cur'
   Box cur;
+  bool written = false;   // cur was rewritten in this launch
   bool changed = true;    // the start node's children were relinked
   for (uint32_t steps = 0;; ++steps) {
     const uint32_t parent = __float_as_uint(w1.z), l = __float_as_uint(w1.w), r = __float_as_uint(w2.x);
-    if ((__float_as_uint(w2.y) & 0xFFFFu) || l >= numNodes || r >= numNodes || steps > numNodes) {
+    if ((__float_as_uint(w2.y) & 0xFFFFu) || l >= numNodes || r >= numNodes || steps > numNodes ||
+        (from != kNone && from != l && from != r)) {
       if (!(__float_as_uint(w2.y) & 0xFFFFu)) atomicOr(err, kErrBadIndex);
       return;
     }
@@ -943,7 +994,9 @@ __device__ __forceinline__ void refit_path(bvhgb_node *t, uint32_t root, uint32_
       atomicOr(err, kErrBadIndex);
       return;
     }
-    // this level's child boxes (speculative) and the next level's record and counter
+    const uint32_t side = from == r ? 1u : 0u;  // meaningful only when from != kNone
+    // this level's child boxes from their records (valid unless rewritten in this launch) and the
+    // next level's record and counter
     Box lb = from == l ? cur : load_box_cg(t + l);
     Box rb = from == r ? cur : load_box_cg(t + r);
     float4 n0 = w0, n1 = w1, n2 = w2;
@@ -957,17 +1010,19 @@ __device__ __forceinline__ void refit_path(bvhgb_node *t, uint32_t root, uint32_
     }
     uint32_t old = cnt;
     if ((cnt & 0x7FFFFFFFu) != 1u) {  // other arrivals are (or were) expected here
-      const uint32_t add = changed ? 0xFFFFu : 0xFFFFFFFFu;  // one arrival less (low 16 bits), one changed more
-      old = changed ? atom_add_acq_rel(&counter[x], add) : atom_add_acquire(&counter[x], add);
+      const bool post = from != kNone && written;
+      if (post) mail_post(mail, from, cur);
+      uint32_t add = 0xFFFFFFFFu;  // one arrival less
+      if (from != kNone) add += (written ? (1u << (16 + side)) : 0u) + (changed ? (1u << (18 + side)) : 0u);
+      old = atomicAdd(&counter[x], add);
       if ((old & 0xFFFFu) != 1u) return;  // not the last arrival
-      if ((old >> 16) & 0x7FFFu) {        // a child's box was rewritten in this launch
-        if (from != l) lb = load_box_cg(t + l);
-        if (from != r) rb = load_box_cg(t + r);
-      }
+      if (post) mail_clear(mail, from);   // posted for nobody
+      if (from != l && ((old >> 16) & 1u)) lb = mail_take(mail, l, err);
+      if (from != r && ((old >> 17) & 1u)) rb = mail_take(mail, r, err);
     }
     counter[x] = 0u;
     const bool start = (old >> 31) != 0u;  // x started a path (this one or an earlier arrival)
-    const bool anyChanged = changed || start || ((old >> 16) & 0x7FFFu) != 0u;
+    const bool anyChanged = changed || start || ((old >> 18) & 3u) != 0u;
     Box b;
     b.mn[0] = w0.x; b.mn[1] = w0.y; b.mn[2] = w0.z;
     b.mx[0] = w0.w; b.mx[1] = w1.x; b.mx[2] = w1.y;
@@ -989,6 +1044,7 @@ __device__ __forceinline__ void refit_path(bvhgb_node *t, uint32_t root, uint32_
     if (top) return;
     // A start node may have moved (a reused node now hangs under a new parent), so its parent
     // cannot compare against the old box: it always counts as changed.
+    written = upChanged;
     changed = upChanged || start;
     from = x;
     cur = b;
