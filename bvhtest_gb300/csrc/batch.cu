@@ -237,13 +237,19 @@ __global__ void batch_apply_kernel(bvhgb_node *nodes, const PatchOut *__restrict
   apply_item(nodes + nb, in[q], valid + q, toFix + 3 * (size_t)q, owner + nb, it.k, stats);
 }
 
+// The count and refit climbs run one per warp (lane 0): climbs sharing a warp would each wait, level
+// by level, for the slowest lane's level.
+__device__ __forceinline__ uint32_t batch_path_index() {
+  return (threadIdx.x & 31u) ? 0xFFFFFFFFu : (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+}
+
 __global__ void batch_count_kernel(const bvhgb_node *__restrict__ nodes, const PatchOut *__restrict__ in,
                                    const uint32_t *__restrict__ toFix, uint32_t *__restrict__ owner,
                                    uint32_t *__restrict__ counter, const uint32_t *__restrict__ itemMesh,
                                    const uint32_t *__restrict__ itemOff, const uint32_t *__restrict__ faceOff,
                                    const uint32_t *__restrict__ nodeOff, uint32_t items,
                                    uint32_t *__restrict__ err) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = batch_path_index();
   if (i >= 3 * items) return;
   const uint32_t q = i / 3;
   const MeshItem it = item_of(itemMesh, itemOff, q);
@@ -256,7 +262,7 @@ __global__ void batch_refit_kernel(bvhgb_node *nodes, const uint32_t *__restrict
                                    const uint32_t *__restrict__ itemMesh,
                                    const uint32_t *__restrict__ itemOff, const uint32_t *__restrict__ faceOff,
                                    const uint32_t *__restrict__ nodeOff, uint32_t items, uint32_t *__restrict__ err) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = batch_path_index();
   if (i >= 3 * items) return;
   const MeshItem it = item_of(itemMesh, itemOff, i / 3);
   const uint32_t n = __ldg(faceOff + it.m + 1) - __ldg(faceOff + it.m), nb = __ldg(nodeOff + it.m);
@@ -364,11 +370,11 @@ int batch_iteration(bvhgb_batch_workspace *ws, bvhgb_node *nodes, cudaStream_t s
     batch_apply_kernel<<<ceil_div(T, bs), bs, 0, s>>>(nodes, ws->patches, ws->valid, ws->toFix, ws->owner,
                                                       ws->itemMesh, ws->itemOff, ws->nodeOff, T, ws->stats);
     BVHGB_LAUNCH_CHECK("batch apply");
-    batch_count_kernel<<<ceil_div(3ull * T, bs), bs, 0, s>>>(nodes, ws->patches, ws->toFix, ws->owner, ws->counter,
+    batch_count_kernel<<<ceil_div(3ull * T, bs / 32), bs, 0, s>>>(nodes, ws->patches, ws->toFix, ws->owner, ws->counter,
                                                              ws->itemMesh, ws->itemOff, ws->faceOff, ws->nodeOff, T,
                                                              ws->err);
     BVHGB_LAUNCH_CHECK("batch count");
-    batch_refit_kernel<<<ceil_div(3ull * T, bs), bs, 0, s>>>(nodes, ws->toFix, ws->counter, ws->mail, ws->itemMesh,
+    batch_refit_kernel<<<ceil_div(3ull * T, bs / 32), bs, 0, s>>>(nodes, ws->toFix, ws->counter, ws->mail, ws->itemMesh,
                                                              ws->itemOff, ws->faceOff, ws->nodeOff, T, ws->err);
     BVHGB_LAUNCH_CHECK("batch refit");
   }

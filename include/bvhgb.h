@@ -380,7 +380,7 @@ typedef struct bvhgb_batch_config {
   uint32_t numChunks;    /* Bittner13 chunks per iteration (32) */
   float batchPercent;    /* Bittner13 batch, % of each mesh's nodes (1.0) */
   uint32_t sortTileKeys; /* tuning: keys per CTA in the sort passes (2048, 4096, 8192) */
-  uint32_t refitBlock;   /* tuning: threads per block of the apply / count / refit kernels */
+  uint32_t refitBlock;   /* tuning: threads per block of the apply / count / refit kernels (count and refit run one climb per warp) */
   uint32_t traceBlock;   /* tuning: threads per block of the tracer */
 } bvhgb_batch_config;
 
