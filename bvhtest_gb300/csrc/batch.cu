@@ -237,19 +237,22 @@ __global__ void batch_apply_kernel(bvhgb_node *nodes, const PatchOut *__restrict
   apply_item(nodes + nb, in[q], valid + q, toFix + 3 * (size_t)q, owner + nb, it.k, stats);
 }
 
-// The count and refit climbs run one per warp (lane 0): climbs sharing a warp would each wait, level
-// by level, for the slowest lane's level.
-__device__ __forceinline__ uint32_t batch_path_index() {
-  return (threadIdx.x & 31u) ? 0xFFFFFFFFu : (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// The count and refit climbs run a few per warp (lanes 0 .. perWarp - 1): climbs sharing a warp
+// each wait, level by level, for the slowest lane's level, so a launch uses as few per warp as keep
+// it within two waves of resident warps.
+__device__ __forceinline__ uint32_t batch_path_index(uint32_t perWarp) {
+  const uint32_t lane = threadIdx.x & 31u;
+  if (lane >= perWarp) return 0xFFFFFFFFu;
+  return ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * perWarp + lane;
 }
 
 __global__ void batch_count_kernel(const bvhgb_node *__restrict__ nodes, const PatchOut *__restrict__ in,
                                    const uint32_t *__restrict__ toFix, uint32_t *__restrict__ owner,
                                    uint32_t *__restrict__ counter, const uint32_t *__restrict__ itemMesh,
                                    const uint32_t *__restrict__ itemOff, const uint32_t *__restrict__ faceOff,
-                                   const uint32_t *__restrict__ nodeOff, uint32_t items,
+                                   const uint32_t *__restrict__ nodeOff, uint32_t items, uint32_t perWarp,
                                    uint32_t *__restrict__ err) {
-  const uint32_t i = batch_path_index();
+  const uint32_t i = batch_path_index(perWarp);
   if (i >= 3 * items) return;
   const uint32_t q = i / 3;
   const MeshItem it = item_of(itemMesh, itemOff, q);
@@ -261,8 +264,9 @@ __global__ void batch_refit_kernel(bvhgb_node *nodes, const uint32_t *__restrict
                                    uint32_t *__restrict__ counter, unsigned long long *__restrict__ mail,
                                    const uint32_t *__restrict__ itemMesh,
                                    const uint32_t *__restrict__ itemOff, const uint32_t *__restrict__ faceOff,
-                                   const uint32_t *__restrict__ nodeOff, uint32_t items, uint32_t *__restrict__ err) {
-  const uint32_t i = batch_path_index();
+                                   const uint32_t *__restrict__ nodeOff, uint32_t items, uint32_t perWarp,
+                                   uint32_t *__restrict__ err) {
+  const uint32_t i = batch_path_index(perWarp);
   if (i >= 3 * items) return;
   const MeshItem it = item_of(itemMesh, itemOff, i / 3);
   const uint32_t n = __ldg(faceOff + it.m + 1) - __ldg(faceOff + it.m), nb = __ldg(nodeOff + it.m);
@@ -362,6 +366,15 @@ int batch_iteration(bvhgb_batch_workspace *ws, bvhgb_node *nodes, cudaStream_t s
   if (st) return st;
   if (T == 0) return BVHGB_OK;
   const uint32_t bs = ws->cfg.refitBlock;
+  // climbs per warp: one, unless that takes more than two waves of resident warps
+  auto perWarp = [&](const void *kernel) {
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, (int)bs, 0) != cudaSuccess || blocks <= 0)
+      blocks = 1;
+    const uint64_t slots = (uint64_t)blocks * (bs / 32) * (uint64_t)sm_count() * 2u;
+    return (uint32_t)std::min<uint64_t>(std::max<uint64_t>((3ull * T + slots - 1) / slots, 1), 32);
+  };
+  const uint32_t pc = perWarp((const void *)batch_count_kernel), pr = perWarp((const void *)batch_refit_kernel);
   for (uint32_t c = 0; c < ws->cfg.numChunks; ++c) {
     batch_patch_kernel<<<ceil_div(T, kWarpItemsPerBlock), kWarpItemsPerBlock * 32, 0, s>>>(
         nodes, ws->todo, ws->itemMesh, ws->itemOff, ws->chunk, ws->faceOff, ws->nodeOff, ws->innerOff, T, c,
@@ -370,12 +383,12 @@ int batch_iteration(bvhgb_batch_workspace *ws, bvhgb_node *nodes, cudaStream_t s
     batch_apply_kernel<<<ceil_div(T, bs), bs, 0, s>>>(nodes, ws->patches, ws->valid, ws->toFix, ws->owner,
                                                       ws->itemMesh, ws->itemOff, ws->nodeOff, T, ws->stats);
     BVHGB_LAUNCH_CHECK("batch apply");
-    batch_count_kernel<<<ceil_div(3ull * T, bs / 32), bs, 0, s>>>(nodes, ws->patches, ws->toFix, ws->owner, ws->counter,
-                                                             ws->itemMesh, ws->itemOff, ws->faceOff, ws->nodeOff, T,
-                                                             ws->err);
+    batch_count_kernel<<<ceil_div(3ull * T, (uint64_t)pc * (bs / 32)), bs, 0, s>>>(
+        nodes, ws->patches, ws->toFix, ws->owner, ws->counter, ws->itemMesh, ws->itemOff, ws->faceOff, ws->nodeOff, T,
+        pc, ws->err);
     BVHGB_LAUNCH_CHECK("batch count");
-    batch_refit_kernel<<<ceil_div(3ull * T, bs / 32), bs, 0, s>>>(nodes, ws->toFix, ws->counter, ws->mail, ws->itemMesh,
-                                                             ws->itemOff, ws->faceOff, ws->nodeOff, T, ws->err);
+    batch_refit_kernel<<<ceil_div(3ull * T, (uint64_t)pr * (bs / 32)), bs, 0, s>>>(
+        nodes, ws->toFix, ws->counter, ws->mail, ws->itemMesh, ws->itemOff, ws->faceOff, ws->nodeOff, T, pr, ws->err);
     BVHGB_LAUNCH_CHECK("batch refit");
   }
   return BVHGB_OK;

@@ -18,6 +18,7 @@
 // bvhgb_bn13_run captures one iteration into a CUDA graph and replays it. With a learned scorer
 // set, iteration i selects by the scorer unless plainEvery > 0 and i % plainEvery == plainEvery - 1,
 // in which case it selects by the inefficiency (one graph per kind of iteration).
+#include <algorithm>
 #include <vector>
 
 #include "bn13_device.cuh"
@@ -102,23 +103,28 @@ __global__ void __launch_bounds__(kWarpItemsPerBlock * 32, 5) patch_warp_kernel(
   warp_patch_item(t, root, numNodes, node, ok, k, out + k, valid + k, toFix + 3 * k, owner, stats, err);
 }
 
-// The climbs of the chunk tail run one per warp (lane 0; the other lanes leave at once). The paths
-// of one item, or of neighbouring items, have nothing in common: in a shared warp every level of
-// every path would wait for the slowest lane's level (an acq_rel arrival costs about four times a
-// plain L2 round trip), so a warp of its own keeps each climb at its own latency. The SMs have the
-// room: a chunk has at most a few thousand paths.
+// The climbs of the chunk tail run a few per warp, at most climbsPerWarp (lanes 0.. of each warp;
+// the other lanes leave at once). The paths of one item, or of neighbouring items, have nothing in
+// common: in a shared warp every level of every path waits for the slowest lane's level, so a
+// chunk whose paths fit in the resident warps of two waves gives each climb a warp of its own
+// (4.19M triangles: 7,863 paths), and only larger chunks share warps, just enough to stay within
+// two waves (33.5M triangles: 62,913 paths, 6 per warp).
 constexpr uint32_t kTailWarpsPerBlock = 4;
+constexpr uint32_t kTailMaxWaves = 2;
 
-__device__ __forceinline__ uint32_t tail_path_index() {
-  return (threadIdx.x & 31u) ? 0xFFFFFFFFu : (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__device__ __forceinline__ uint32_t tail_path_index(uint32_t climbsPerWarp) {
+  const uint32_t lane = threadIdx.x & 31u;
+  if (lane >= climbsPerWarp) return 0xFFFFFFFFu;
+  return ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * climbsPerWarp + lane;
 }
 
 // Apply + count (apply_count_path): three climbs per item.
 __global__ void __launch_bounds__(kTailWarpsPerBlock * 32) apply_count_kernel(
     bvhgb_node *t, uint32_t root, const PatchOut *__restrict__ in, const uint32_t *__restrict__ valid,
     uint32_t *__restrict__ toFix, const uint32_t *__restrict__ owner, uint32_t *__restrict__ counter,
-    uint32_t chunkSize, uint32_t numNodes, unsigned long long *__restrict__ stats, uint32_t *__restrict__ err) {
-  const uint32_t i = tail_path_index();
+    uint32_t chunkSize, uint32_t climbsPerWarp, uint32_t numNodes, unsigned long long *__restrict__ stats,
+    uint32_t *__restrict__ err) {
+  const uint32_t i = tail_path_index(climbsPerWarp);
   if (i >= 3 * chunkSize) return;
   const uint32_t k = i / 3;
   apply_count_path(t, root, numNodes, in, k, i - 3 * k, valid, toFix, owner, counter, stats, err);
@@ -128,12 +134,24 @@ __global__ void __launch_bounds__(kTailWarpsPerBlock * 32) apply_count_kernel(
 __global__ void __launch_bounds__(kTailWarpsPerBlock * 32) release_refit_kernel(
     bvhgb_node *t, uint32_t root, const PatchOut *__restrict__ in, const uint32_t *__restrict__ toFix,
     uint32_t *__restrict__ owner, uint32_t *__restrict__ counter, unsigned long long *__restrict__ mail,
-    uint32_t chunkSize, uint32_t numNodes, uint32_t *__restrict__ err) {
-  const uint32_t i = tail_path_index();
+    uint32_t chunkSize, uint32_t climbsPerWarp, uint32_t numNodes, uint32_t *__restrict__ err) {
+  const uint32_t i = tail_path_index(climbsPerWarp);
   if (i >= 3 * chunkSize) return;
   const uint32_t k = i / 3;
   release_claims(in[k], i - 3 * k, owner);
   refit_path(t, root, numNodes, toFix[i], counter, mail, err);
+}
+
+// Climbs per warp for 'paths' climbs of 'kernel' (blocks of kTailWarpsPerBlock warps): one, unless
+// one climb per warp would take more than kTailMaxWaves waves of resident warps.
+uint32_t climbs_per_warp(const void *kernel, uint64_t paths) {
+  int blocks = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, kTailWarpsPerBlock * 32, 0) != cudaSuccess ||
+      blocks <= 0)
+    blocks = 1;
+  const uint64_t slots = (uint64_t)blocks * kTailWarpsPerBlock * (uint64_t)sm_count() * kTailMaxWaves;
+  const uint64_t per = (paths + slots - 1) / slots;
+  return (uint32_t)std::min<uint64_t>(std::max<uint64_t>(per, 1), 32);
 }
 
 // Full bottom-up refit (kFixTree1, Bittner13CUDA.cu:372-404): every leaf starts a climb; at each
@@ -319,6 +337,7 @@ struct bvhgb_bn13_workspace {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [0] plain iteration, [1] learned iteration
   bvhgb_node *graphNodes = nullptr;
   uint32_t launchesPerIteration = 0;
+  uint32_t countClimbsPerWarp = 1, refitClimbsPerWarp = 1;  // chunk-tail climbs per warp
   uint32_t launchesKind[2] = {0, 0};  // kernels in each captured graph
   uint64_t iteration = 0;  // iterations run so far (selects the kind of the next one)
   uint32_t plainEvery = 0;
@@ -405,14 +424,13 @@ int run_chunk(bvhgb_bn13_workspace *ws, bvhgb_node *nodes, uint32_t c, cudaStrea
   if (prof) BVHGB_CUDA_TRY(record_event(ws->evStop[c], s));
   // apply + count in one launch (the count reads the winners' new parents from their patches),
   // then the release of the claims and the refit
-  const uint32_t tailBlocks = ceil_div(3ull * cs, kTailWarpsPerBlock);
-  apply_count_kernel<<<tailBlocks, kTailWarpsPerBlock * 32, 0, s>>>(nodes, ws->root, ws->patches, ws->valid,
-                                                                    ws->toFix, ws->owner, ws->counter, cs,
-                                                                    ws->numNodes, ws->stats, ws->err);
+  const uint32_t pc = ws->countClimbsPerWarp, pr = ws->refitClimbsPerWarp;
+  apply_count_kernel<<<ceil_div(3ull * cs, (uint64_t)pc * kTailWarpsPerBlock), kTailWarpsPerBlock * 32, 0, s>>>(
+      nodes, ws->root, ws->patches, ws->valid, ws->toFix, ws->owner, ws->counter, cs, pc, ws->numNodes, ws->stats,
+      ws->err);
   BVHGB_LAUNCH_CHECK("bn13 apply+count");
-  release_refit_kernel<<<tailBlocks, kTailWarpsPerBlock * 32, 0, s>>>(nodes, ws->root, ws->patches, ws->toFix,
-                                                                      ws->owner, ws->counter, ws->mail, cs,
-                                                                      ws->numNodes, ws->err);
+  release_refit_kernel<<<ceil_div(3ull * cs, (uint64_t)pr * kTailWarpsPerBlock), kTailWarpsPerBlock * 32, 0, s>>>(
+      nodes, ws->root, ws->patches, ws->toFix, ws->owner, ws->counter, ws->mail, cs, pr, ws->numNodes, ws->err);
   BVHGB_LAUNCH_CHECK("bn13 refit");
   return BVHGB_OK;
 }
@@ -529,6 +547,8 @@ extern "C" BVHGB_API int bvhgb_bn13_create(const bvhgb_node *nodes, uint32_t num
   if (e == cudaSuccess) e = dev_malloc(&ws->stats, sizeof(unsigned long long) * S_COUNT);
   if (e == cudaSuccess && inner.size())
     e = cudaMemcpyAsync(ws->inner, inner.data(), 4 * inner.size(), cudaMemcpyHostToDevice, s);
+  ws->countClimbsPerWarp = climbs_per_warp((const void *)apply_count_kernel, 3ull * cs);
+  ws->refitClimbsPerWarp = climbs_per_warp((const void *)release_refit_kernel, 3ull * cs);
   if (e == cudaSuccess) e = cudaMemsetAsync(ws->counter, 0, 4ull * numNodes, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ws->mail, 0xFF, 24ull * numNodes, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ws->owner, 0xFF, 4ull * numNodes, s);
