@@ -264,6 +264,10 @@ class Bittner13GPU:
               "bvhgb_bn13_set_scorer")
         self._scorer = scorer
 
+    def set_tail_packing(self, climbs_per_warp: int = 0):
+        """Climbs per warp of the chunk tail (1..32, 0 = automatic); the trees do not depend on it."""
+        check(self.lib.bvhgb_bn13_set_tail_packing(self.ws, climbs_per_warp), "bvhgb_bn13_set_tail_packing")
+
     @property
     def iteration(self) -> int:
         return self.lib.bvhgb_bn13_iteration(self.ws)

@@ -720,6 +720,15 @@ extern "C" BVHGB_API int bvhgb_bn13_set_scorer(bvhgb_bn13_workspace *ws, const b
 
 extern "C" BVHGB_API uint64_t bvhgb_bn13_iteration(const bvhgb_bn13_workspace *ws) { return ws ? ws->iteration : 0; }
 
+extern "C" BVHGB_API int bvhgb_bn13_set_tail_packing(bvhgb_bn13_workspace *ws, uint32_t climbsPerWarp) {
+  if (!ws || climbsPerWarp > 32) return BVHGB_INVALID_ARGUMENT;
+  const uint64_t paths = 3ull * ws->chunkSize;
+  ws->countClimbsPerWarp = climbsPerWarp ? climbsPerWarp : climbs_per_warp((const void *)apply_count_kernel, paths);
+  ws->refitClimbsPerWarp = climbsPerWarp ? climbsPerWarp : climbs_per_warp((const void *)release_refit_kernel, paths);
+  drop_graphs(ws);
+  return BVHGB_OK;
+}
+
 extern "C" BVHGB_API int bvhgb_bn13_set_iteration(bvhgb_bn13_workspace *ws, uint64_t iteration) {
   if (!ws) return BVHGB_INVALID_ARGUMENT;
   ws->iteration = iteration;

@@ -120,6 +120,7 @@ PROTOS = {
     "bvhgb_bn13_set_scorer": (I32, [VP, VP, U32]),
     "bvhgb_bn13_iteration": (U64, [VP]),
     "bvhgb_bn13_set_iteration": (I32, [VP, U64]),
+    "bvhgb_bn13_set_tail_packing": (I32, [VP, U32]),
     "bvhgb_bn13_read_selection": (I32, [VP, VP, U32, VP]),
     "bvhgb_bn13_set_selection": (I32, [VP, VP, U32, VP]),
     "bvhgb_batch_create": (I32, [U32, VP, C.POINTER(BatchConfig), C.POINTER(VP)]),

@@ -57,6 +57,28 @@ def test_bittner_bit_exact_vs_oracle(gpu, orc, n, iters, topo, mode):
     opt.close()
 
 
+@pytest.mark.parametrize("packing", [1, 3, 32])
+def test_chunk_tail_packing_gives_the_oracle_tree(gpu, orc, packing):
+    """The chunk tail's count and refit climbs, one per warp or packed several (3, 32) per warp
+    (what chunks too large for two waves of warps get), through the captured graph: the same tree
+    bytes as the oracle."""
+    import torch
+    n = 16384
+    vert, faces, nodes = _build(gpu, n, seed=29, topo="karras", bits=63)
+    start = gpu.nodes_to_numpy(nodes)
+    opt = gpu.Bittner13GPU(nodes, num_nodes=2 * n - 1)
+    opt.set_tail_packing(packing)
+    opt.run(4)
+    torch.cuda.synchronize()
+    got = gpu.nodes_to_numpy(nodes)[: 2 * n - 1]
+    ref, _, st = orc.bittner_chunked(start[: 2 * n - 1], 4, search_mode=0, heap_cap=4096)
+    assert np.array_equal(got.view(np.uint8), ref.view(np.uint8)), _diff(got, ref)
+    assert opt.stats()["applied"] == st["applied"]  # stats() raises on any device error bit
+    with pytest.raises(RuntimeError):
+        opt.set_tail_packing(33)
+    opt.close()
+
+
 def test_graph_replay_equals_steps(gpu):
     import torch
     n = 8192
