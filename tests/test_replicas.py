@@ -24,7 +24,7 @@ def _rank(rank, world, port, out):
 
 def test_two_replicas_report_the_slowest_rank():
     world, port = 2, 29517
-    out = mp.Manager().dict()
+    out = mp.get_context("spawn").Manager().dict()
     mp.start_processes(_rank, args=(world, port, out), nprocs=world, join=True, start_method="spawn")
     assert dict(out) == {0: 11.0, 1: 11.0}
 
