@@ -90,8 +90,10 @@ __device__ __forceinline__ float uniform01(uint64_t seed, uint64_t idx, uint32_t
 // primary rays only). The bounce starts on the hit point, offset along the normal that faces the
 // incoming ray; the direction follows Malley's method around that normal in the orthonormal basis
 // of Duff et al. (JCGT 2017).
+// Incoherent rays (bounce, random) are bound by the latency of their record and triangle loads:
+// at most 48 registers keep 40 warps per SM resident instead of 36 (2.5% faster bounce phase).
 template <bool REC>
-__global__ void __launch_bounds__(128) trace_bounce_kernel(const bvhgb_node *__restrict__ nodes,
+__global__ void __launch_bounds__(128, 10) trace_bounce_kernel(const bvhgb_node *__restrict__ nodes,
                                                            const TravNode *__restrict__ trav, uint32_t numNodes,
                                                            uint32_t root, const float *__restrict__ vert,
                                                            const uint32_t *__restrict__ faces, CamParams cam,
@@ -209,7 +211,7 @@ __global__ void __launch_bounds__(128) trace_image_kernel(const bvhgb_node *__re
 }
 
 template <bool REC>
-__global__ void __launch_bounds__(128) trace_rays_kernel(const bvhgb_node *__restrict__ nodes,
+__global__ void __launch_bounds__(128, 10) trace_rays_kernel(const bvhgb_node *__restrict__ nodes,
                                                          const TravNode *__restrict__ trav, uint32_t numNodes,
                                                          uint32_t root, const float *__restrict__ vert,
                                                          const uint32_t *__restrict__ faces,
