@@ -791,7 +791,7 @@ __device__ __forceinline__ void apply_item(bvhgb_node *t, const PatchOut &in, ui
   atomicAdd(&stats[S_APPLIED], 1ull);
 }
 
-// Apply and count in one launch, three threads per item. The count climbs the new tree while the
+// Apply and count in one launch, three climbs per item. The count climbs the new tree while the
 // winners' patches are still being written: a node that a winning item patched takes its new parent
 // from that item's patch record, every other node keeps its parent (its record is not written in
 // this launch). A node y is patched by a winner iff its owner o (the lowest rank that claimed it;
@@ -820,9 +820,9 @@ __device__ __forceinline__ uint32_t new_parent(const PatchOut *__restrict__ in, 
   return p;
 }
 
-// Thread j of item k: all three decide the item's outcome (the owner array is final; valid[k], the
-// patch kernel's verdict, is only read here, so the three threads see the same value); thread 0
-// writes the patch and the statistics, thread j counts the arrivals along the item's j-th dirty
+// Climb j of item k: all three decide the item's outcome (the owner array is final; valid[k], the
+// patch kernel's decision, is only read here, so the three climbs see the same value); climb 0
+// writes the patch and the statistics, climb j counts the arrivals along the item's j-th dirty
 // path (kFixTree3_1) in the new tree. The start node gets bit 31 as in count_path.
 __device__ __forceinline__ void apply_count_path(bvhgb_node *t, uint32_t root, uint32_t numNodes,
                                                  const PatchOut *__restrict__ in, uint32_t k, uint32_t j,
