@@ -239,7 +239,7 @@ __global__ void batch_apply_kernel(bvhgb_node *nodes, const PatchOut *__restrict
 
 // The count and refit climbs run a few per warp (lanes 0 .. perWarp - 1): climbs sharing a warp
 // each wait, level by level, for the slowest lane's level, so a launch uses as few per warp as keep
-// it within two waves of resident warps.
+// it within one wave of resident warps.
 __device__ __forceinline__ uint32_t batch_path_index(uint32_t perWarp) {
   const uint32_t lane = threadIdx.x & 31u;
   if (lane >= perWarp) return 0xFFFFFFFFu;
@@ -366,12 +366,12 @@ int batch_iteration(bvhgb_batch_workspace *ws, bvhgb_node *nodes, cudaStream_t s
   if (st) return st;
   if (T == 0) return BVHGB_OK;
   const uint32_t bs = ws->cfg.refitBlock;
-  // climbs per warp: one, unless that takes more than two waves of resident warps
+  // climbs per warp: the fewest that fit in one wave of resident warps
   auto perWarp = [&](const void *kernel) {
     int blocks = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, (int)bs, 0) != cudaSuccess || blocks <= 0)
       blocks = 1;
-    const uint64_t slots = (uint64_t)blocks * (bs / 32) * (uint64_t)sm_count() * 2u;
+    const uint64_t slots = (uint64_t)blocks * (bs / 32) * (uint64_t)sm_count();
     return (uint32_t)std::min<uint64_t>(std::max<uint64_t>((3ull * T + slots - 1) / slots, 1), 32);
   };
   const uint32_t pc = perWarp((const void *)batch_count_kernel), pr = perWarp((const void *)batch_refit_kernel);

@@ -103,14 +103,15 @@ __global__ void __launch_bounds__(kWarpItemsPerBlock * 32, 5) patch_warp_kernel(
   warp_patch_item(t, root, numNodes, node, ok, k, out + k, valid + k, toFix + 3 * k, owner, stats, err);
 }
 
-// The climbs of the chunk tail run a few per warp, at most climbsPerWarp (lanes 0.. of each warp;
-// the other lanes leave at once). The paths of one item, or of neighbouring items, have nothing in
-// common: in a shared warp every level of every path waits for the slowest lane's level, so a
-// chunk whose paths fit in the resident warps of two waves gives each climb a warp of its own
-// (4.19M triangles: 7,863 paths), and only larger chunks share warps, just enough to stay within
-// two waves (33.5M triangles: 62,913 paths, 6 per warp).
+// The climbs of the chunk tail run a few per warp, climbsPerWarp (lanes 0.. of each warp; the other
+// lanes leave at once). The paths of one item, or of neighbouring items, have nothing in common: in
+// a shared warp every level of every path waits for the slowest lane's level, so few per warp is
+// better, but a second wave of warps starts its climbs late: the chunk packs just enough per warp
+// to fit in one wave of resident warps (4.19M triangles: 7,863 paths, 2 per warp; 33.5M: 62,913
+// paths, 12 per warp). Measured (20 plain iterations of the 4.19M-triangle scene): 1 per warp
+// 52.8 ms, 2: 51.8, 4: 52.8; (5 of the 33.5M scene) 4: 73.1, 6: 71.3, 12: 70.7, 16: 70.5.
 constexpr uint32_t kTailWarpsPerBlock = 4;
-constexpr uint32_t kTailMaxWaves = 2;
+constexpr uint32_t kTailMaxWaves = 1;
 
 __device__ __forceinline__ uint32_t tail_path_index(uint32_t climbsPerWarp) {
   const uint32_t lane = threadIdx.x & 31u;
@@ -142,8 +143,8 @@ __global__ void __launch_bounds__(kTailWarpsPerBlock * 32) release_refit_kernel(
   refit_path(t, root, numNodes, toFix[i], counter, mail, err);
 }
 
-// Climbs per warp for 'paths' climbs of 'kernel' (blocks of kTailWarpsPerBlock warps): one, unless
-// one climb per warp would take more than kTailMaxWaves waves of resident warps.
+// Climbs per warp for 'paths' climbs of 'kernel' (blocks of kTailWarpsPerBlock warps): the fewest
+// that fit in kTailMaxWaves waves of resident warps.
 uint32_t climbs_per_warp(const void *kernel, uint64_t paths) {
   int blocks = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, kTailWarpsPerBlock * 32, 0) != cudaSuccess ||

@@ -353,9 +353,9 @@ BVHGB_API int bvhgb_bn13_set_scorer(bvhgb_bn13_workspace *ws, const bvhgb_mlp *s
  * its reset for a new optimisation of a rebuilt tree of the same mesh. */
 BVHGB_API uint64_t bvhgb_bn13_iteration(const bvhgb_bn13_workspace *ws);
 BVHGB_API int bvhgb_bn13_set_iteration(bvhgb_bn13_workspace *ws, uint64_t iteration);
-/* Climbs per warp of the chunk tail's count and refit kernels (1..32; 0 = automatic: one per warp
- * unless that needs more than two waves of resident warps). Results never depend on it; the
- * captured iteration graphs are rebuilt. */
+/* Climbs per warp of the chunk tail's count and refit kernels (1..32; 0 = automatic: the fewest that
+ * fit in one wave of resident warps). Results never depend on it; the captured iteration graphs
+ * are rebuilt. */
 BVHGB_API int bvhgb_bn13_set_tail_packing(bvhgb_bn13_workspace *ws, uint32_t climbsPerWarp);
 /* Replaces the selection of the current iteration by a caller order (numInner node ids, device, in
  * batch position order) for the following bvhgb_bn13_chunk calls; a later select overwrites it. */
