@@ -505,7 +505,7 @@ def run_ours(args, w, rank, world, local):
             line["optimize_ms_per_iteration"] = round(big["optimize_ms"] / big["iterations"], 4)
             line["ms_per_step"] = big["build_optimize_ms"]
             if big.get("roofline"):
-                line["roofline_search"] = line["roofline"]
+                line["roofline_plain"] = line["roofline"]  # the plain arm's search, for comparison
                 line["roofline"] = big["roofline"]
         line["learned_vs_plain"] = learned_arm(args, dev, flush, stream)
     if not args.no_batch:
@@ -798,6 +798,36 @@ def learned_large(args, w, dev, flush, stream, vert, faces, nodes, lbvh, target,
         torch.cuda.synchronize()
         if i >= args.warmup:
             e2e.append(e0.elapsed_time(e1))
+    # The reinsertion search of the learned run, timed with kernel events in an untimed pass (that
+    # workspace records events around every search launch; the timed runs above have none).
+    prof = api.Bittner13GPU(rebuild(), num_nodes=n_nodes, profile=True)
+    prof.set_scorer(scorer, 2)
+    for _ in range(2):  # warm-up: both iteration graphs captured
+        rebuild()
+        prof.iteration = 0
+        prof.run(k)
+    rebuild()
+    prof.iteration = 0
+    visits0 = prof.stats()["nodesVisited"]
+    s_ms, s_launches = 0.0, 0
+    for _ in range(k):
+        prof.run(1)
+        torch.cuda.synchronize()
+        ms_i, n_i = prof.search_time()
+        s_ms += ms_i
+        s_launches += n_i
+    s_visits = prof.stats()["nodesVisited"] - visits0
+    prof.close()
+    search_roof = None
+    if s_launches and s_ms > 0:
+        peak, peak_kind = measured_peaks()
+        bpl = s_visits * NODE_BYTES / s_launches
+        mpl = s_ms / s_launches
+        ach_s = bpl / (mpl * 1e-3) / 1e9
+        search_roof = {"kernel": "bn13 patch (reinsertion search), learned run", "bound": "hbm",
+                       "achieved": round(ach_s, 1), "peak": peak, "unit": "GB/s", "frac": round(ach_s / peak, 5),
+                       "traffic": None, "peak_kind": peak_kind, "ms_per_launch": round(mpl, 4),
+                       "algorithmic_bytes_per_launch": int(bpl), "launches": int(s_launches)}
     # the scorer's inference kernel, timed alone on this scene's feature rows
     inner = lopt.inner_nodes()
     x = api.LrFeatures(n_nodes)(nodes, inner)
@@ -814,8 +844,8 @@ def learned_large(args, w, dev, flush, stream, vert, faces, nodes, lbvh, target,
     flops = 2.0 * (24 * 64 + 64 * 64 + 64) * inner.shape[0]
     tf_peak, tf_kind = measured_tflops()
     learned_iters = (k + 1) // 2
-    roof = None
-    if mlp_ms * learned_iters >= search_ms_per_iteration * k:
+    roof = search_roof  # the dominant kernel of the learned run: the search, unless the scorer outweighs it
+    if mlp_ms * learned_iters >= (s_ms if s_launches else search_ms_per_iteration * k):
         ach = flops / (mlp_ms * 1e-3) / 1e12
         roof = {"kernel": "scorer MLP forward (24-64-64-1, BF16 in, FP32 accumulate)", "bound": "tensor",
                 "achieved": round(ach, 2), "peak": tf_peak, "unit": "TFLOP/s", "frac": round(ach / tf_peak, 5),
