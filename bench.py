@@ -824,9 +824,12 @@ def learned_large(args, w, dev, flush, stream, vert, faces, nodes, lbvh, target,
         bpl = s_visits * NODE_BYTES / s_launches
         mpl = s_ms / s_launches
         ach_s = bpl / (mpl * 1e-3) / 1e9
+        tfile = ROOT / "profiles" / "traffic.json"
+        traffic_l = (json.loads(tfile.read_text()).get(w["name"], {}).get("bn13_patch_learned")
+                     if tfile.exists() else None)
         search_roof = {"kernel": "bn13 patch (reinsertion search), learned run", "bound": "hbm",
                        "achieved": round(ach_s, 1), "peak": peak, "unit": "GB/s", "frac": round(ach_s / peak, 5),
-                       "traffic": None, "peak_kind": peak_kind, "ms_per_launch": round(mpl, 4),
+                       "traffic": traffic_l, "peak_kind": peak_kind, "ms_per_launch": round(mpl, 4),
                        "algorithmic_bytes_per_launch": int(bpl), "launches": int(s_launches)}
     # the scorer's inference kernel, timed alone on this scene's feature rows
     inner = lopt.inner_nodes()
