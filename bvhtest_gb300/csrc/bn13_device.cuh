@@ -405,9 +405,8 @@ constexpr int kFrontier = 4;  // slots per lane (128 entries)
 constexpr uint32_t kFrontierCap = 32u * kFrontier;
 
 // The k-th smallest (1 <= k <= number of flagged entries) of the 32-bit keys of the slots flagged
-// in 'in' (bit s: this lane's slot s), S slots per lane: a most-significant-bit-first radix
-// selection, one warp sum per bit (of each lane's flagged keys with the bit clear), starting below
-// the bits that all flagged keys share.
+// in 'in' (bit s: this lane's slot s), S slots per lane: a most-significant-first radix selection
+// over 2-bit digits, one warp sum per digit, starting below the bits that all flagged keys share.
 template <int S>
 __device__ __forceinline__ uint32_t warp_select_kth(const uint32_t (&key)[S], uint32_t in, uint32_t k) {
   uint32_t lo = 0xFFFFFFFFu, hi = 0u;
@@ -423,18 +422,42 @@ __device__ __forceinline__ uint32_t warp_select_kth(const uint32_t (&key)[S], ui
   const int top = 31 - __clz(lo ^ hi);
   uint32_t res = lo & ~((2u << top) - 1u);  // 2u << 31 wraps to 0: no common bits
   uint32_t alive = in;
-  for (int bit = top; bit >= 0; --bit) {
-    uint32_t ones = 0;  // this lane's slots whose key has the bit set
+  int bit = top;
+  // two bits per step: the counts of the digits 00, 01 and 10 (at most 1,023 each) travel packed
+  // 10 bits apart in one warp sum
+  for (; bit >= 1; bit -= 2) {
+    uint32_t hi1 = 0, lo1 = 0;  // this lane's slots whose key has bit / bit - 1 set
 #pragma unroll
-    for (int s = 0; s < S; ++s) ones |= ((key[s] >> bit) & 1u) << s;
-    const uint32_t zeros = __reduce_add_sync(kFull, (uint32_t)__popc(alive & ~ones));  // one collective per bit
-    if (k > zeros) {
-      k -= zeros;
-      res |= 1u << bit;
-      alive &= ones;
-    } else {
-      alive &= ~ones;
+    for (int s = 0; s < S; ++s) {
+      hi1 |= ((key[s] >> bit) & 1u) << s;
+      lo1 |= ((key[s] >> (bit - 1)) & 1u) << s;
     }
+    const uint32_t m00 = alive & ~hi1 & ~lo1, m01 = alive & ~hi1 & lo1, m10 = alive & hi1 & ~lo1;
+    const uint32_t c = __reduce_add_sync(kFull, (uint32_t)__popc(m00) | ((uint32_t)__popc(m01) << 10) |
+                                                    ((uint32_t)__popc(m10) << 20));
+    const uint32_t c00 = c & 1023u, c01 = (c >> 10) & 1023u, c10 = c >> 20;
+    if (k <= c00) {
+      alive = m00;
+    } else if (k <= c00 + c01) {
+      k -= c00;
+      alive = m01;
+      res |= 1u << (bit - 1);
+    } else if (k <= c00 + c01 + c10) {
+      k -= c00 + c01;
+      alive = m10;
+      res |= 1u << bit;
+    } else {
+      k -= c00 + c01 + c10;
+      alive &= hi1 & lo1;
+      res |= 3u << (bit - 1);
+    }
+  }
+  if (bit == 0) {
+    uint32_t ones = 0;
+#pragma unroll
+    for (int s = 0; s < S; ++s) ones |= (key[s] & 1u) << s;
+    const uint32_t zeros = __reduce_add_sync(kFull, (uint32_t)__popc(alive & ~ones));
+    if (k > zeros) res |= 1u;
   }
   return res;
 }
