@@ -91,24 +91,6 @@ __device__ __forceinline__ uint32_t atom_add_acq_rel(uint32_t *p, uint32_t v) {
   asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(r) : "l"(p), "r"(v) : "memory");
   return r;
 }
-__device__ __forceinline__ uint32_t atom_add_acquire(uint32_t *p, uint32_t v) {
-  uint32_t r;
-  asm volatile("atom.acquire.gpu.global.add.u32 %0, [%1], %2;" : "=r"(r) : "l"(p), "r"(v) : "memory");
-  return r;
-}
-__device__ __forceinline__ uint32_t atom_add_relaxed(uint32_t *p, uint32_t v) {
-  uint32_t r;
-  asm volatile("atom.relaxed.gpu.global.add.u32 %0, [%1], %2;" : "=r"(r) : "l"(p), "r"(v) : "memory");
-  return r;
-}
-__device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
-  uint32_t r;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(r) : "l"(p) : "memory");
-  return r;
-}
-__device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t *p) {
   uint32_t r;
   asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(r) : "l"(p) : "memory");
